@@ -1,0 +1,503 @@
+/* Test infrastructure (oracle), never shipped.  CPU restatement of the
+ * reference's 2D Barnes-Hut step; see oracle.h for the conventions.  Each
+ * function cites the part of the reference (pentilm/StellarSolver) it restates.
+ * Parity against the reference itself is pinned by the golden fixtures in
+ * tests/golden/, produced by running the reference's kernels.cu on the host.
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <omp.h>
+#include <stdlib.h>
+#include <string.h>
+
+int orc_num_threads(void) { return omp_get_max_threads(); }
+
+/* kernels.cu:51-58 (box reset to 0) and :62-114 (min/max merge). */
+int orc_bbox(int n, const float* x, const float* y, float* box) {
+    float l = 0.0f, r = 0.0f, b = 0.0f, t = 0.0f;
+    for (int i = 0; i < n; ++i) {
+        if (!isfinite(x[i]) || !isfinite(y[i])) return ORC_ERR_NONFINITE;
+        l = fminf(l, x[i]);
+        r = fmaxf(r, x[i]);
+        b = fminf(b, y[i]);
+        t = fmaxf(t, y[i]);
+    }
+    box[0] = l;
+    box[1] = r;
+    box[2] = b;
+    box[3] = t;
+    return ORC_OK;
+}
+
+/* kernels.cu:137-185: per level, mid = 0.5*(lo+hi) (the double literal makes
+ * no difference: halving a float sum is exact), digit bit 0 = (x < mid_x),
+ * bit 1 = (y < mid_y); the body's half becomes the new interval. */
+static uint64_t key_of(float px, float py, const float* box) {
+    float l = box[0], r = box[1], b = box[2], t = box[3];
+    uint64_t key = 0;
+    for (int level = 0; level < 32; ++level) {
+        float mx = (l + r) * 0.5f;
+        float my = (b + t) * 0.5f;
+        unsigned c = 0;
+        if (px < mx) {
+            c |= 1u;
+            r = mx;
+        } else {
+            l = mx;
+        }
+        if (py < my) {
+            c |= 2u;
+            t = my;
+        } else {
+            b = my;
+        }
+        key = (key << 2) | c;
+    }
+    return key;
+}
+
+void orc_keys(int n, const float* x, const float* y, const float* box, uint64_t* keys) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) keys[i] = key_of(x[i], y[i], box);
+}
+
+/* Leaves in DFS order over child slots 0..3 (sort_kernel, kernels.cu:292-336)
+ * are the bodies in ascending key order.  LSD radix sort, 8 passes of 8 bits. */
+int orc_sort_keys(int n, const uint64_t* keys, uint32_t* perm) {
+    if (n <= 0) return 0;
+    uint64_t* k0 = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)n);
+    uint64_t* k1 = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)n);
+    uint32_t* p1 = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)n);
+    memcpy(k0, keys, sizeof(uint64_t) * (size_t)n);
+    for (int i = 0; i < n; ++i) perm[i] = (uint32_t)i;
+    uint32_t* p0 = perm;
+    for (int pass = 0; pass < 8; ++pass) {
+        int shift = 8 * pass;
+        size_t cnt[257];
+        memset(cnt, 0, sizeof cnt);
+        for (int i = 0; i < n; ++i) cnt[((k0[i] >> shift) & 255u) + 1]++;
+        for (int d = 0; d < 256; ++d) cnt[d + 1] += cnt[d];
+        for (int i = 0; i < n; ++i) {
+            size_t dst = cnt[(k0[i] >> shift) & 255u]++;
+            k1[dst] = k0[i];
+            p1[dst] = p0[i];
+        }
+        uint64_t* tk = k0;
+        k0 = k1;
+        k1 = tk;
+        uint32_t* tp = p0;
+        p0 = p1;
+        p1 = tp;
+    }
+    /* 8 passes: an even count, so the result is back in `perm` */
+    int dups = 0;
+    for (int i = 1; i < n; ++i) dups += (k0[i] == k0[i - 1]);
+    free(k0);
+    free(k1);
+    free(p1);
+    return dups;
+}
+
+static int lcp_bits(uint64_t a, uint64_t b) { return a == b ? 64 : __builtin_clzll(a ^ b); }
+
+typedef struct {
+    const uint64_t* k;
+    int32_t *left, *right, *split, *first, *last, *parent, *leaf_parent;
+} TreeCtx;
+
+/* Internal node `id` covers sorted bodies [a, b], a < b. */
+static void build_node(TreeCtx* t, int a, int b, int id, int parent) {
+    int p = lcp_bits(t->k[a], t->k[b]);
+    int bit = 63 - p;
+    int lo = a, hi = b; /* bit of k[lo] is 0, bit of k[hi] is 1 */
+    while (hi - lo > 1) {
+        int mid = lo + (hi - lo) / 2;
+        if ((t->k[mid] >> bit) & 1u)
+            hi = mid;
+        else
+            lo = mid;
+    }
+    int g = lo;
+    t->split[id] = p;
+    t->first[id] = a;
+    t->last[id] = b;
+    t->parent[id] = parent;
+    if (g == a) {
+        t->left[id] = ~a;
+        t->leaf_parent[a] = id;
+    } else {
+        t->left[id] = g;
+        build_node(t, a, g, g, id);
+    }
+    if (g + 1 == b) {
+        t->right[id] = ~b;
+        t->leaf_parent[b] = id;
+    } else {
+        t->right[id] = g + 1;
+        build_node(t, g + 1, b, g + 1, id);
+    }
+}
+
+/* The reference's tree (kernels.cu:117-271) holds one cell per key prefix
+ * shared by >= 2 bodies; the binary radix tree below has the same leaves and,
+ * after the digit merge, exactly the reference's branching cells (chain cells
+ * with one child are implicit: they carry their only child's sums). */
+int orc_build_tree(int n, const uint64_t* skeys, int32_t* left, int32_t* right,
+                   int32_t* split_bit, int32_t* first, int32_t* last, int32_t* parent,
+                   int32_t* leaf_parent, uint8_t* qmerged) {
+    if (n < 2) return ORC_ERR_ARG;
+    for (int i = 1; i < n; ++i)
+        if (skeys[i] == skeys[i - 1]) return ORC_ERR_DUPLICATE_KEYS;
+    TreeCtx t = {skeys, left, right, split_bit, first, last, parent, leaf_parent};
+    build_node(&t, 0, n - 1, 0, -1);
+    for (int i = 0; i < n - 1; ++i) {
+        int s = split_bit[i];
+        qmerged[i] = (uint8_t)(i != 0 && (s & 1) && split_bit[parent[i]] == s - 1);
+    }
+    return ORC_OK;
+}
+
+typedef struct {
+    const float *sx, *sy, *sm;
+    const int32_t *left, *right;
+    float *m, *mx, *my;
+} SumCtx;
+
+static void child_sums(const SumCtx* c, int32_t ch, float* m, float* mx, float* my);
+
+static void node_sums(const SumCtx* c, int id) {
+    float lm, lmx, lmy, rm, rmx, rmy;
+    child_sums(c, c->left[id], &lm, &lmx, &lmy);
+    child_sums(c, c->right[id], &rm, &rmx, &rmy);
+    c->m[id] = lm + rm;
+    c->mx[id] = lmx + rmx;
+    c->my[id] = lmy + rmy;
+}
+
+static void child_sums(const SumCtx* c, int32_t ch, float* m, float* mx, float* my) {
+    if (ch < 0) {
+        int j = ~ch;
+        float mj = c->sm[j];
+        *m = mj;
+        *mx = mj * c->sx[j]; /* kernels.cu:180-181: mass*x */
+        *my = mj * c->sy[j];
+    } else {
+        node_sums(c, ch);
+        *m = c->m[ch];
+        *mx = c->mx[ch];
+        *my = c->my[ch];
+    }
+}
+
+/* kernels.cu:180-183 (sums) and :275-288 (x /= mass). */
+void orc_node_sums(int n, const float* sx, const float* sy, const float* sm,
+                   const int32_t* left, const int32_t* right, float* node_m, float* node_mx,
+                   float* node_my, float* node_cx, float* node_cy) {
+    if (n < 2) return;
+    SumCtx c = {sx, sy, sm, left, right, node_m, node_mx, node_my};
+    node_sums(&c, 0);
+    for (int i = 0; i < n - 1; ++i) {
+        node_cx[i] = node_mx[i] / node_m[i];
+        node_cy[i] = node_my[i] / node_m[i];
+    }
+}
+
+void orc_quad_children(int n, const int32_t* left, const int32_t* right,
+                       const int32_t* split_bit, const uint8_t* qmerged, int32_t* qchild) {
+    (void)split_bit;
+    for (int i = 0; i < n - 1; ++i) {
+        int k = 0;
+        int32_t* out = qchild + 4 * (size_t)i;
+        for (int s = 0; s < 4; ++s) out[s] = INT32_MIN;
+        if (qmerged[i]) continue;
+        int32_t cs[2] = {left[i], right[i]};
+        for (int s = 0; s < 2; ++s) {
+            int32_t c = cs[s];
+            if (c >= 0 && qmerged[c]) {
+                out[k++] = left[c];
+                out[k++] = right[c];
+            } else {
+                out[k++] = c;
+            }
+        }
+    }
+}
+
+/* kernels.cu:340-435: one group = 32 consecutive sorted bodies (a warp).
+ * dp for a cell at level L is radius^2/theta scaled by 0.25 per level below
+ * the root's children (:349, :376, :395); the test is dp <= dx*dx+dy*dy+eps2
+ * on every lane (:405-406); the force is m * d * rsqrt(r)^3 (:407-411). */
+int64_t orc_walk_ref(int n, const float* sx, const float* sy, const float* sm,
+                     const int32_t* split_bit, const int32_t* qchild, const float* node_m,
+                     const float* node_cx, const float* node_cy, const float* box, float theta,
+                     float eps2, float* sax, float* say) {
+    if (n == 1) {
+        sax[0] = 0.0f;
+        say[0] = 0.0f;
+        return 0;
+    }
+    if (n < 1) return 0;
+    float radius = (box[1] - box[0]) * 0.5f;
+    float dp1 = (radius * radius) / theta;
+    int groups = (n + 31) / 32;
+    int64_t total = 0;
+#pragma omp parallel reduction(+ : total)
+    {
+        int cap = 1024;
+        int32_t* stack = (int32_t*)malloc(sizeof(int32_t) * (size_t)cap);
+#pragma omp for schedule(dynamic, 16)
+        for (int g = 0; g < groups; ++g) {
+            int g0 = 32 * g;
+            int cnt = n - g0 < 32 ? n - g0 : 32;
+            float px[32], py[32], ax[32], ay[32], rr[32];
+            for (int k = 0; k < cnt; ++k) {
+                px[k] = sx[g0 + k];
+                py[k] = sy[g0 + k];
+                ax[k] = 0.0f;
+                ay[k] = 0.0f;
+            }
+            int64_t inter = 0;
+            int top = 0;
+            /* the root is never approximated unless its chain reaches level 2 */
+            int32_t pending[1] = {0};
+            for (int pi = 0; pi < 1; ++pi) {
+                int32_t q = pending[pi];
+                int L = split_bit[q] >> 1;
+                int accept = 0;
+                if (L >= 2) {
+                    float dp = ldexpf(dp1, -2 * (L - 1));
+                    accept = 1;
+                    for (int k = 0; k < cnt; ++k) {
+                        float dx = node_cx[q] - px[k];
+                        float dy = node_cy[q] - py[k];
+                        float r = dx * dx;
+                        r = r + dy * dy;
+                        r = r + eps2;
+                        rr[k] = r;
+                        accept &= (dp <= r);
+                    }
+                }
+                if (accept) {
+                    for (int k = 0; k < cnt; ++k) {
+                        float dx = node_cx[q] - px[k];
+                        float dy = node_cy[q] - py[k];
+                        float ri = 1.0f / sqrtf(rr[k]);
+                        float f = node_m[q] * ri;
+                        f = f * ri;
+                        f = f * ri;
+                        ax[k] = ax[k] + f * dx;
+                        ay[k] = ay[k] + f * dy;
+                    }
+                    inter += cnt;
+                } else {
+                    stack[top++] = q;
+                }
+            }
+            while (top > 0) {
+                int32_t node = stack[--top];
+                for (int s = 0; s < 4; ++s) {
+                    int32_t c = qchild[4 * (size_t)node + s];
+                    if (c == INT32_MIN) continue;
+                    float cxv, cyv, mv;
+                    int L = 0;
+                    if (c < 0) {
+                        cxv = sx[~c];
+                        cyv = sy[~c];
+                        mv = sm[~c];
+                    } else {
+                        cxv = node_cx[c];
+                        cyv = node_cy[c];
+                        mv = node_m[c];
+                        L = split_bit[c] >> 1;
+                    }
+                    int accept = 1;
+                    float dp = L >= 2 ? ldexpf(dp1, -2 * (L - 1)) : 0.0f;
+                    for (int k = 0; k < cnt; ++k) {
+                        float dx = cxv - px[k];
+                        float dy = cyv - py[k];
+                        float r = dx * dx;
+                        r = r + dy * dy;
+                        r = r + eps2;
+                        rr[k] = r;
+                        if (c >= 0) accept &= (L >= 2) && (dp <= r);
+                    }
+                    if (accept) {
+                        for (int k = 0; k < cnt; ++k) {
+                            float dx = cxv - px[k];
+                            float dy = cyv - py[k];
+                            float ri = 1.0f / sqrtf(rr[k]);
+                            float f = mv * ri;
+                            f = f * ri;
+                            f = f * ri;
+                            ax[k] = ax[k] + f * dx;
+                            ay[k] = ay[k] + f * dy;
+                        }
+                        inter += cnt;
+                    } else {
+                        if (top == cap) {
+                            cap *= 2;
+                            stack = (int32_t*)realloc(stack, sizeof(int32_t) * (size_t)cap);
+                        }
+                        stack[top++] = c;
+                    }
+                }
+            }
+            for (int k = 0; k < cnt; ++k) {
+                sax[g0 + k] = ax[k];
+                say[g0 + k] = ay[k];
+            }
+            total += inter;
+        }
+        free(stack);
+    }
+    return total;
+}
+
+int orc_step_ref(int n, float* x, float* y, float* vx, float* vy, const float* m, float* ax,
+                 float* ay, float theta, float eps2, float dt, float damp,
+                 int64_t* interactions) {
+    if (n < 1) return ORC_ERR_ARG;
+    float box[4];
+    int st = orc_bbox(n, x, y, box);
+    if (st) return st;
+    size_t N = (size_t)n;
+    uint64_t* keys = (uint64_t*)malloc(8 * N);
+    uint64_t* skeys = (uint64_t*)malloc(8 * N);
+    uint32_t* perm = (uint32_t*)malloc(4 * N);
+    float* sx = (float*)malloc(4 * N);
+    float* sy = (float*)malloc(4 * N);
+    float* sm = (float*)malloc(4 * N);
+    float* sax = (float*)malloc(4 * N);
+    float* say = (float*)malloc(4 * N);
+    size_t nn = N > 1 ? N - 1 : 1;
+    int32_t* left = (int32_t*)malloc(4 * nn);
+    int32_t* right = (int32_t*)malloc(4 * nn);
+    int32_t* split = (int32_t*)malloc(4 * nn);
+    int32_t* first = (int32_t*)malloc(4 * nn);
+    int32_t* last = (int32_t*)malloc(4 * nn);
+    int32_t* parent = (int32_t*)malloc(4 * nn);
+    int32_t* lparent = (int32_t*)malloc(4 * N);
+    uint8_t* qm = (uint8_t*)malloc(nn);
+    int32_t* qc = (int32_t*)malloc(16 * nn);
+    float* nm = (float*)malloc(4 * nn);
+    float* nmx = (float*)malloc(4 * nn);
+    float* nmy = (float*)malloc(4 * nn);
+    float* ncx = (float*)malloc(4 * nn);
+    float* ncy = (float*)malloc(4 * nn);
+    int64_t inter = 0;
+
+    orc_keys(n, x, y, box, keys);
+    orc_sort_keys(n, keys, perm);
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < n; ++j) {
+        uint32_t i = perm[j];
+        skeys[j] = keys[i];
+        sx[j] = x[i];
+        sy[j] = y[i];
+        sm[j] = m[i];
+    }
+    if (n >= 2) {
+        st = orc_build_tree(n, skeys, left, right, split, first, last, parent, lparent, qm);
+        if (st == ORC_OK) {
+            orc_node_sums(n, sx, sy, sm, left, right, nm, nmx, nmy, ncx, ncy);
+            orc_quad_children(n, left, right, split, qm, qc);
+            inter = orc_walk_ref(n, sx, sy, sm, split, qc, nm, ncx, ncy, box, theta, eps2, sax,
+                                 say);
+        }
+    } else {
+        sax[0] = 0.0f;
+        say[0] = 0.0f;
+    }
+    if (st == ORC_OK) {
+#pragma omp parallel for schedule(static)
+        for (int j = 0; j < n; ++j) {
+            ax[perm[j]] = sax[j];
+            ay[perm[j]] = say[j];
+        }
+        /* kernels.cu:529-533 */
+        float ddt = damp * dt;
+#pragma omp parallel for schedule(static)
+        for (int i = 0; i < n; ++i) {
+            vx[i] = vx[i] + dt * ax[i];
+            vy[i] = vy[i] + dt * ay[i];
+            x[i] = x[i] + ddt * vx[i];
+            y[i] = y[i] + ddt * vy[i];
+        }
+    }
+    if (interactions) *interactions = inter;
+    free(keys);
+    free(skeys);
+    free(perm);
+    free(sx);
+    free(sy);
+    free(sm);
+    free(sax);
+    free(say);
+    free(left);
+    free(right);
+    free(split);
+    free(first);
+    free(last);
+    free(parent);
+    free(lparent);
+    free(qm);
+    free(qc);
+    free(nm);
+    free(nmx);
+    free(nmy);
+    free(ncx);
+    free(ncy);
+    return st;
+}
+
+void orc_direct_f64_hilo(int n, const float* xh, const float* xl, const float* yh,
+                         const float* yl, const float* m, int ns, const int32_t* idx,
+                         double eps2, double G, double* ax, double* ay) {
+#pragma omp parallel for schedule(dynamic, 8)
+    for (int k = 0; k < ns; ++k) {
+        int i = idx[k];
+        double xi = (double)xh[i] + (xl ? (double)xl[i] : 0.0);
+        double yi = (double)yh[i] + (yl ? (double)yl[i] : 0.0);
+        double sx = 0.0, sy = 0.0;
+        for (int j = 0; j < n; ++j) {
+            if (j == i) continue;
+            double dx = (double)xh[j] + (xl ? (double)xl[j] : 0.0) - xi;
+            double dy = (double)yh[j] + (yl ? (double)yl[j] : 0.0) - yi;
+            double r2 = dx * dx + dy * dy + eps2;
+            double inv = 1.0 / (r2 * sqrt(r2));
+            sx += (double)m[j] * dx * inv;
+            sy += (double)m[j] * dy * inv;
+        }
+        ax[k] = G * sx;
+        ay[k] = G * sy;
+    }
+}
+
+void orc_direct_f64(int n, const float* x, const float* y, const float* m, int ns,
+                    const int32_t* idx, double eps2, double G, double* ax, double* ay) {
+    orc_direct_f64_hilo(n, x, NULL, y, NULL, m, ns, idx, eps2, G, ax, ay);
+}
+
+void orc_energy_f64(int n, const float* x, const float* y, const float* vx, const float* vy,
+                    const float* m, double eps2, double G, double* out) {
+    double ke = 0.0, pe = 0.0, px = 0.0, py = 0.0;
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : ke, pe, px, py)
+    for (int i = 0; i < n; ++i) {
+        double mi = m[i];
+        ke += 0.5 * mi * ((double)vx[i] * vx[i] + (double)vy[i] * vy[i]);
+        px += mi * vx[i];
+        py += mi * vy[i];
+        double s = 0.0;
+        for (int j = i + 1; j < n; ++j) {
+            double dx = (double)x[j] - x[i];
+            double dy = (double)y[j] - y[i];
+            s += (double)m[j] / sqrt(dx * dx + dy * dy + eps2);
+        }
+        pe -= G * mi * s;
+    }
+    out[0] = ke;
+    out[1] = pe;
+    out[2] = px;
+    out[3] = py;
+}
