@@ -1,0 +1,437 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 2D Barnes-Hut step (one JSON line on rank 0).
+
+Workload: 2D-projected Plummer sphere, N = 2^20, a = 1, M = 1, equal masses,
+eps = 0.01, dt = 1e-4, theta = 0.5 (seeded synthetic input).  A "step" is one
+full pass of the pipeline: box, keys, radix sort, reorder, tree, moments,
+force walk fused with the integration.
+
+  value   steps/s of the MIXED engine (quadrupole walk, compensated sums,
+          hi/lo positions) replayed as a CUDA graph, inputs resident in HBM,
+          CUDA events per step, L2 flushed between timed steps.
+  e2e     the same metric through the C ABI with host buffers: every step
+          copies the state in from pinned host memory, steps, and reads the
+          positions back.
+  roofline  the force walk against the measured FP32 FMA peak (14 flops per
+          body-node interaction); per-phase HBM fractions beside it.
+
+--impl reference times the reference's algorithm on the host cores (the CPU
+restatement in oracle/, the reference having no CPU path) on the same
+workload.  With torchrun (N > 1) every rank runs an independent replica.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "steps/s & interactions/s, N=2^20 Plummer θ=0.5, mixed vs plain FP32 at ≤1e-3 err"
+WORKLOAD = "plummer2d_2^20"
+N_BODIES = 1 << 20
+EPS = 0.01
+DT = 1e-4
+THETA = 0.5
+FLOPS_PER_INTERACTION = 14  # dx,dy 2; r^2 4; rsqrt 1; r^-3 2; m*r^-3 1; two FMAs 4
+LAUNCHES_PER_STEP = 31       # bbox 1, keys 1, sort 8x3, reorder 1, build 1, moments 1, records 1, walk 1
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def phase_bytes(n, mixed, passes=8):
+    """Algorithmic bytes per launch of each HBM-bound phase (each array once)."""
+    lo = 16 * n if mixed else 0
+    return {
+        "bbox": 8 * n,
+        "keys": 20 * n,
+        "sort": 24 * n * passes,
+        "reorder": 52 * n + lo,
+        "build": 36 * n,
+        "moments": 68 * n,
+        "records": 108 * n,
+    }
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v == "Active"})
+        return {"sm_mhz": float(np.median([r[0] for r in rows])),
+                "sm_max_mhz": float(max(r[1] for r in rows)),
+                "power_w_max": float(max(r[2] for r in rows)),
+                "samples": len(rows), "reasons": reasons}
+
+
+def run_engine(args):
+    import torch
+
+    from stellarsolver_gb300 import bh, models
+
+    world, rank, local = dist_init()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    stream = torch.cuda.current_stream()
+    sp = ctypes_stream(stream)
+    hbm_peak, hbm_kind = peaks()
+
+    x, y, vx, vy, m = models.plummer(N_BODIES, models.SEED_BASE + 1)
+    n = len(x)
+    eps2 = EPS * EPS
+    common = dict(theta=THETA, eps2=eps2, gravity=1.0, timestep=DT, dampening=1.0,
+                  leaf_bucket=args.bucket)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    def timed_steps(s, k):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(k)]
+        for a, b in evs:
+            flush.zero_()
+            a.record(stream)
+            s.step(1, sp)
+            b.record(stream)
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in evs) / 1e3
+
+    result = {}
+    # ---------------------------------------------------------------- force error
+    idx = np.sort(np.random.default_rng(7).choice(n, size=4096, replace=False)).astype(np.int32)
+    errors = {}
+    inter = {}
+    for mode in ("mixed", "plain"):
+        with bh.BarnesHutSystem(n, device=local, mode=mode, **common) as s:
+            s.set_state(x, y, vx, vy, m)
+            if mode == "mixed":
+                rx, ry = s.direct_sum_f64(idx)
+            s.step(1)
+            s.sync()
+            ax, ay = s.get_accel()
+            inter[mode] = s.stats()["interactions"]
+        rel = np.hypot(ax[idx] - rx, ay[idx] - ry) / np.hypot(rx, ry)
+        errors[mode] = {"rms_rel": float(np.sqrt(np.mean(rel ** 2))), "max_rel": float(rel.max())}
+
+    # ---------------------------------------------------------------- steps/s
+    sysm = bh.BarnesHutSystem(n, device=local, mode=args.mode, use_graph=True, **common)
+    sysm.set_state(x, y, vx, vy, m)
+    for _ in range(args.warmup):
+        sysm.step(1, sp)
+    sysm.sync(sp)
+    st0 = sysm.get_state()
+    barrier()
+    with ClockSampler(local) as clk:
+        t_wall0 = time.perf_counter()
+        secs = timed_steps(sysm, args.steps)
+        t_wall = time.perf_counter() - t_wall0
+    barrier()
+    sysm.sync(sp)
+    st1 = sysm.get_state()
+    stats = sysm.stats()
+    clocks = clk.summary()
+    if world > 1:
+        t = torch.tensor([secs], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        secs = float(t.item())
+    value = world * args.steps / secs
+    ms_per_step = 1e3 * secs / args.steps
+    p0 = np.array([np.sum(st0["m"].astype(np.float64) * st0["vx"]),
+                   np.sum(st0["m"].astype(np.float64) * st0["vy"])])
+    p1 = np.array([np.sum(st1["m"].astype(np.float64) * st1["vx"]),
+                   np.sum(st1["m"].astype(np.float64) * st1["vy"])])
+    pscale = float(np.sum(st0["m"].astype(np.float64) * np.hypot(st0["vx"], st0["vy"])))
+
+    # plain FP32 side by side: graph replay, and the single-system path without a graph
+    sides = {}
+    for label, kw in (("plain_graph", dict(mode="plain", use_graph=True)),
+                      ("plain_single_system_nograph", dict(mode="plain", use_graph=False))):
+        with bh.BarnesHutSystem(n, device=local, **kw, **common) as s:
+            s.set_state(x, y, vx, vy, m)
+            for _ in range(args.warmup):
+                s.step(1, sp)
+            s.sync(sp)
+            sides[label] = args.steps / timed_steps(s, args.steps)
+
+    # ---------------------------------------------------------------- per-phase roofline
+    phase_ms = np.zeros(bh.PHASES_N, np.float32)
+    prof_steps = max(3, min(args.steps, 10))
+    for _ in range(prof_steps):
+        flush.zero_()
+        sysm.step_profiled(phase_ms, sp)
+    phase_ms /= prof_steps
+    sysm.sync(sp)
+    walk_ms = float(phase_ms[bh.PHASES.index("walk")])
+    fp32_peak = bh.measure_fp32_peak(local)
+    walk_flops = FLOPS_PER_INTERACTION * stats["interactions"]
+    achieved = walk_flops / (walk_ms * 1e-3) / 1e12
+    traffic = recorded_traffic("walk")
+    pb = phase_bytes(n, args.mode == "mixed")
+    phases = {}
+    for i, name in enumerate(bh.PHASES):
+        ms = float(phase_ms[i])
+        entry = {"ms": round(ms, 4)}
+        if name in pb:
+            gbs = pb[name] / (ms * 1e-3) / 1e9 if ms > 0 else None
+            entry.update({"algorithmic_bytes": pb[name], "GB/s": round(gbs, 1) if gbs else None,
+                          "frac_hbm": round(gbs / hbm_peak, 4) if gbs else None})
+        phases[name] = entry
+
+    # ---------------------------------------------------------------- e2e through the C ABI
+    e2e = run_e2e(bh, torch, stream, sp, n, x, y, vx, vy, m, common, local, args)
+    sysm.close()
+
+    result = {
+        "metric": METRIC,
+        "value": round(value, 3),
+        "unit": "steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_per_step, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded 2D Plummer, models.plummer)",
+        "config": {"workload": WORKLOAD, "n_bodies": n, "theta": THETA, "eps": EPS, "dt": DT,
+                   "mode": args.mode, "leaf_bucket": args.bucket or "default", "cuda_graph": True,
+                   "l2": "flushed (256 MB write) before every timed step",
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "timed_wall_s_incl_flush": round(t_wall, 3)},
+        "interactions_per_step": stats["interactions"],
+        "interactions_per_s": round(stats["interactions"] * value / world, 1) * world,
+        "force_error_vs_fp64": errors,
+        "plain_fp32": {"steps_per_s_graph": round(sides["plain_graph"], 3),
+                       "steps_per_s_single_system_nograph":
+                           round(sides["plain_single_system_nograph"], 3),
+                       "interactions_per_step": inter["plain"]},
+        "mixed_over_plain_single_system": round(value / world / sides["plain_single_system_nograph"], 3),
+        "momentum_drift_rel": float(np.abs(p1 - p0).max() / pscale),
+        "tree": {"cells": stats["cells"], "nodes": stats["nodes"], "max_depth": stats["max_depth"]},
+        "roofline": {"bound": "fp32", "kernel": "k_walk_acc", "achieved": round(achieved, 3),
+                     "peak": round(fp32_peak, 2), "unit": "TFLOP/s",
+                     "frac": round(achieved / fp32_peak, 4),
+                     "peak_source": "measured FFMA probe (bh_measure_fp32_peak)",
+                     "traffic": traffic, "phases": phases,
+                     "hbm_peak_gbs": hbm_peak, "hbm_peak_source": hbm_kind},
+        "e2e": e2e,
+        "gpu_launches": LAUNCHES_PER_STEP * args.steps,
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(x, y, vx, vy, m)
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def ctypes_stream(stream):
+    import ctypes
+
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def recorded_traffic(kernel):
+    """DRAM bytes per launch from the committed ncu summary (None until captured)."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d.get(WORKLOAD, {}).get(kernel)
+    except Exception:
+        return None
+
+
+def run_e2e(bh, torch, stream, sp, n, x, y, vx, vy, m, common, local, args):
+    pin = {k: torch.from_numpy(v.copy()).pin_memory() for k, v in
+           (("x", x), ("y", y), ("vx", vx), ("vy", vy), ("m", m))}
+    outx = torch.empty(n, dtype=torch.float32).pin_memory()
+    outy = torch.empty(n, dtype=torch.float32).pin_memory()
+    ptr = {k: v.data_ptr() for k, v in pin.items()}
+    lib = bh.lib()
+    with bh.BarnesHutSystem(n, device=local, mode=args.mode, use_graph=True, **common) as s:
+        def one():
+            rc = lib.bh_set_state(s.handle, ptr["x"], ptr["y"], ptr["vx"], ptr["vy"], ptr["m"], sp)
+            rc |= lib.bh_step(s.handle, 1, sp)
+            rc |= lib.bh_get_state(s.handle, outx.data_ptr(), outy.data_ptr(), None, None, None, sp)
+            if rc:
+                raise RuntimeError(f"e2e C-ABI call failed: {rc}")
+
+        for _ in range(args.warmup):
+            one()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(args.steps):
+            one()
+        b.record(stream)
+        torch.cuda.synchronize()
+        secs = a.elapsed_time(b) / 1e3
+        s.sync(sp)
+    return {"value": round(args.steps / secs, 3), "unit": "steps/s",
+            "h2d_bytes_per_step": 20 * n, "d2h_bytes_per_step": 8 * n,
+            "path": "bh_set_state(pinned host) + bh_step + bh_get_state(x, y -> pinned host)"}
+
+
+def cpu_baseline(x, y, vx, vy, m):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+
+    po.lib()
+    t0 = time.perf_counter()
+    po.step_ref(x, y, vx, vy, m, THETA, EPS * EPS, DT, 1.0)
+    secs = time.perf_counter() - t0
+    return {"value": round(1.0 / secs, 4), "unit": "steps/s", "cores": po.num_threads(),
+            "kind": "port",
+            "sample": f"1 full reference-rule step of the {WORKLOAD} workload (box, keys, sort, "
+                      "tree, centre of mass, warp-vote walk, update), OpenMP over all host threads"}
+
+
+def run_reference(args):
+    world, rank, _ = dist_init()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+
+    from stellarsolver_gb300 import models
+
+    po.lib()
+    x, y, vx, vy, m = models.plummer(N_BODIES, models.SEED_BASE + 1)
+    state = (x, y, vx, vy)
+    for _ in range(args.warmup):
+        state = po.step_ref(*state, m, THETA, EPS * EPS, DT, 1.0)[:4]
+    t0 = time.perf_counter()
+    inter = 0
+    for _ in range(args.steps):
+        out = po.step_ref(*state, m, THETA, EPS * EPS, DT, 1.0)
+        state = out[:4]
+        inter = out[6]
+    secs = time.perf_counter() - t0
+    value = args.steps / secs
+    cores = po.num_threads()
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": round(value, 4),
+        "unit": "steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(1e3 * secs / args.steps, 2),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded 2D Plummer, models.plummer)",
+        "config": {"workload": WORKLOAD, "n_bodies": N_BODIES, "theta": THETA, "eps": EPS,
+                   "dt": DT, "mode": "reference rule (monopole, warp vote)"},
+        "interactions_per_step": inter,
+        "interactions_per_s": round(inter * value, 1),
+        "cpu_baseline": {"value": round(value, 4), "unit": "steps/s", "cores": cores,
+                         "kind": "port",
+                         "sample": "full steps of the workload: the reference's algorithm "
+                                   "(kernels.cu) restated in C, OpenMP over all host threads; "
+                                   "the reference has no CPU path and its CUDA kernels are not "
+                                   "run on the shared GPUs (spin-waits that can hang)"},
+        "e2e": {"value": round(value, 4), "unit": "steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
+    ap.add_argument("--mode", choices=["mixed", "plain", "reference"], default="mixed")
+    ap.add_argument("--bucket", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "engine":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_engine(args)
+
+
+if __name__ == "__main__":
+    main()

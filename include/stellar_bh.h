@@ -1,0 +1,167 @@
+/* stellar_bh.h -- C ABI of the GB300 (sm_103a) 2D Barnes-Hut engine.
+ *
+ * Drop-in boundary for the per-step pipeline of pentilm/StellarSolver:
+ *   BarnesHutParticleSystem::update()   BarnesHutParticleSystem.cpp:301-347
+ *   the nine launch wrappers            Particle_cuda.cuh:5-13 / Particle_cuda.cu:8-59
+ * Plain C types only: pointers, sizes, ints and floats.  Every call returns a
+ * status code (BH_OK == 0); the reference's wrappers return void and never
+ * check errors (Particle_cuda.cu:8-59).  Streams are passed as `void*`
+ * (a cudaStream_t, NULL = the legacy default stream).  Calls on one handle are
+ * not thread-safe; different handles are independent.
+ *
+ * Body arrays at this boundary are in the caller's order (the order in which
+ * bh_set_state received them), like the reference's d_x/d_y/... arrays
+ * (BarnesHutParticleSystem.cpp:63-69).
+ */
+#ifndef STELLAR_BH_H
+#define STELLAR_BH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define BH_OK 0
+#define BH_ERR_ARG 1            /* bad argument (NULL handle, n < 1, bad mode ...) */
+#define BH_ERR_DUPLICATE_KEYS 2 /* two bodies share all 32 key levels; the reference
+                                   would split forever (kernels.cu:197-252) */
+#define BH_ERR_NONFINITE 3      /* NaN/Inf position */
+#define BH_ERR_CAPACITY 4       /* more bodies/cells than the buffers hold */
+#define BH_ERR_STACK 5          /* walk stack overflow (raise stack_depth) */
+#define BH_ERR_CUDA 6           /* a CUDA runtime call failed; see bh_last_error() */
+#define BH_ERR_NOMEM 7          /* device or host allocation failed */
+#define BH_ERR_STATE 8          /* call out of order (e.g. step before set_state) */
+#define BH_ERR_NO_DEVICE 9      /* no CUDA device, or not an sm_103 device */
+
+/* ---------------------------------------------------------------- modes */
+/* REFERENCE: the reference's force law and opening rule, bit-for-bit tree:
+ *   monopole, cell accepted iff every body of the 32-body group has
+ *   (w^2/theta) <= |d|^2 + eps2 (kernels.cu:395-406), root children always
+ *   opened, G not applied (kernels.cu:340: `g` unused), Euler-Cromer update
+ *   v += dt*a; x += (d*dt)*v (kernels.cu:529-533).
+ * PLAIN: accuracy mode in FP32: quadrupole moments, group opening test
+ *   dist(COM, group box) > bmax/theta, leaf buckets, G applied.
+ * MIXED: PLAIN plus compensated (Kahan) force sums and positions kept as
+ *   hi + lo float pairs. */
+#define BH_MODE_REFERENCE 0
+#define BH_MODE_PLAIN 1
+#define BH_MODE_MIXED 2
+
+/* Mirrors SimulationParameters (SimulationParameters.h:14-25) plus the
+ * constants the reference fixes at compile time (kernels.cu:5-9). */
+typedef struct bh_params {
+    int mode;          /* BH_MODE_* */
+    float theta;       /* opening angle; reference constant 0.5 (kernels.cu:9) */
+    float eps2;        /* softening squared; reference constant 0.025 (kernels.cu:8) */
+    float gravity;     /* G (SimulationParameters.gravity); ignored in REFERENCE mode */
+    float timestep;    /* dt (SimulationParameters.timestep) */
+    float dampening;   /* d: x += d*dt*v (SimulationParameters.dampening) */
+    int leaf_bucket;   /* bodies per leaf in PLAIN/MIXED walks; 0 = tuned default */
+    int block_size;    /* walk threads per block; 0 = tuned default */
+    int stack_depth;   /* walk stack entries per warp; 0 = tuned default */
+    int use_graph;     /* 1 = replay the step as a CUDA graph */
+} bh_params;
+
+typedef struct bh_system bh_system;
+
+/* Counters of the last bh_step call (device-side, read back on request). */
+typedef struct bh_stats {
+    int64_t interactions;  /* body-node interactions in the last step */
+    int32_t cells;         /* reference-tree cells (key prefixes shared by >= 2 bodies) */
+    int32_t nodes;         /* branching quadtree nodes */
+    int32_t max_depth;     /* deepest leaf level */
+    int32_t status;        /* sticky device status (BH_* code) */
+    float box[4];          /* left, right, bottom, top of the last step */
+} bh_stats;
+
+/* Fill p with the reference's defaults: mode REFERENCE, theta 0.5, eps2 0.025,
+ * G 1, dt 0.001, dampening 1 (main.cpp:92-95, kernels.cu:8-9). */
+void bh_default_params(bh_params* p);
+
+/* BarnesHutParticleSystem(p, n) (BarnesHutParticleSystem.cpp:28-84): allocate
+ * device storage for n bodies.  No reference counterpart for `device`:
+ * device ordinal (-1 = current). */
+int bh_create(const bh_params* p, int n, int device, bh_system** out);
+
+/* ~BarnesHutParticleSystem (BarnesHutParticleSystem.cpp:249-292). */
+int bh_destroy(bh_system* s);
+
+int bh_set_params(bh_system* s, const bh_params* p);
+int bh_get_params(const bh_system* s, bh_params* p);
+int bh_num_bodies(const bh_system* s); /* getNumParticles() (BarnesHutParticleSystem.cpp:295) */
+
+/* reset()'s host-to-device copy (BarnesHutParticleSystem.cpp:364-371).  Any
+ * pointer may be host or device memory (cudaMemcpyDefault).  Accelerations
+ * start at zero. */
+int bh_set_state(bh_system* s, const float* x, const float* y, const float* vx,
+                 const float* vy, const float* mass, void* stream);
+
+/* Copy the current state out in the caller's order (any of the pointers may be
+ * NULL to skip it).  For MIXED mode x/y are hi+lo rounded to float. */
+int bh_get_state(bh_system* s, float* x, float* y, float* vx, float* vy, float* mass,
+                 void* stream);
+
+/* Accelerations of the last step, caller's order (d_ax/d_ay of the reference). */
+int bh_get_accel(bh_system* s, float* ax, float* ay, void* stream);
+
+/* Positions as hi/lo pairs (MIXED keeps lo; other modes return lo = 0). */
+int bh_get_positions_hilo(bh_system* s, float* xhi, float* xlo, float* yhi, float* ylo,
+                          void* stream);
+
+/* update() x steps (BarnesHutParticleSystem.cpp:301-347): bbox, keys, radix
+ * sort, tree, moments, force walk fused with the integration.  Asynchronous on
+ * `stream`; the returned status covers launch errors only.  Device-side errors
+ * (duplicate keys, non-finite input, stack overflow) are sticky and reported
+ * by bh_sync / bh_get_stats. */
+int bh_step(bh_system* s, int steps, void* stream);
+
+/* Wait for `stream`, then return the sticky device status. */
+int bh_sync(bh_system* s, void* stream);
+
+int bh_get_stats(bh_system* s, bh_stats* out, void* stream);
+
+/* Copy a named internal array of the last step to host memory (test and
+ * debugging aid).  Names and element types:
+ *   "box" f32[4], "keys" u64[n] (sorted), "perm" i32[n] (caller index of each
+ *   sorted position), "node_left" "node_right" "node_split" "node_first"
+ *   "node_last" "node_parent" i32[n], "node_m" "node_mx" "node_my" "node_cx"
+ *   "node_cy" f32[n] (node arrays have n entries; entry n-1 is unused),
+ *   "accel_sorted" f32[2n] (ax then ay).
+ * Returns BH_ERR_ARG for an unknown name or a too small buffer. */
+int bh_get_debug(bh_system* s, const char* name, void* host_out, size_t bytes, void* stream);
+
+/* Phases timed by bh_step_profiled, in order. */
+#define BH_NUM_PHASES 8 /* bbox, keys, sort, reorder, build, moments, records, walk */
+
+/* One step (never graph-replayed) with CUDA events at the phase boundaries;
+ * synchronises, then ADDS each phase's milliseconds to phase_ms[0..7].
+ * No reference counterpart (the reference times the whole step only,
+ * BarnesHutParticleSystem.cpp:303-321). */
+int bh_step_profiled(bh_system* s, void* stream, float* phase_ms);
+
+/* FP64 O(N^2) direct-sum accelerations at ns caller indices idx[] for the
+ * current state (hi+lo positions in MIXED mode), times G (1 in REFERENCE
+ * mode).  Results to host arrays.  Diagnostic for the force-error report; no
+ * reference counterpart.  Synchronous. */
+int bh_direct_sum_f64(bh_system* s, int ns, const int* idx, double* ax, double* ay);
+
+/* Measure the device's FP32 FMA throughput (TFLOP/s, 2 flops per FMA) with a
+ * register-only kernel on every SM; the roofline denominator of the force
+ * walk.  device -1 = current.  No reference counterpart. */
+int bh_measure_fp32_peak(int device, double* tflops);
+
+/* Human-readable text for a status code, and the last CUDA error seen by the
+ * library in this thread. */
+const char* bh_status_string(int status);
+const char* bh_last_error(void);
+
+/* Library build identification: "<version> sm_103a". */
+const char* bh_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* STELLAR_BH_H */

@@ -1,0 +1,249 @@
+"""ctypes binding of the C ABI in include/stellar_bh.h.
+
+`BarnesHutSystem` mirrors the reference's host class
+(BarnesHutParticleSystem.h:62-71): construct for n bodies, load a state
+(reset()), advance (update()), read positions back (getOutputBuffer()).
+Arrays are numpy float32 in the caller's body order.  All compute runs on the
+GPU through the library; a missing library or a failing call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+MODES = {"reference": 0, "plain": 1, "mixed": 2}
+PHASES = ("bbox", "keys", "sort", "reorder", "build", "moments", "records", "walk")
+PHASES_N = len(PHASES)
+
+BH_OK = 0
+STATUS_NAMES = {
+    0: "BH_OK", 1: "BH_ERR_ARG", 2: "BH_ERR_DUPLICATE_KEYS", 3: "BH_ERR_NONFINITE",
+    4: "BH_ERR_CAPACITY", 5: "BH_ERR_STACK", 6: "BH_ERR_CUDA", 7: "BH_ERR_NOMEM",
+    8: "BH_ERR_STATE", 9: "BH_ERR_NO_DEVICE",
+}
+
+
+class BHError(RuntimeError):
+    def __init__(self, code: int, what: str):
+        self.code = code
+        super().__init__(f"{what}: {STATUS_NAMES.get(code, code)} ({_status_string(code)})"
+                         + (f" [{last_error()}]" if code == 6 else ""))
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int), ("theta", ctypes.c_float), ("eps2", ctypes.c_float),
+                ("gravity", ctypes.c_float), ("timestep", ctypes.c_float),
+                ("dampening", ctypes.c_float), ("leaf_bucket", ctypes.c_int),
+                ("block_size", ctypes.c_int), ("stack_depth", ctypes.c_int),
+                ("use_graph", ctypes.c_int)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("interactions", ctypes.c_int64), ("cells", ctypes.c_int32),
+                ("nodes", ctypes.c_int32), ("max_depth", ctypes.c_int32),
+                ("status", ctypes.c_int32), ("box", ctypes.c_float * 4)]
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def lib() -> ctypes.CDLL:
+    """Load lib/libstellar_bh.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: run `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = ctypes.CDLL(path)
+    vp, i32, sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t
+    P = ctypes.POINTER
+    L.bh_default_params.argtypes = [P(Params)]
+    L.bh_default_params.restype = None
+    L.bh_create.argtypes = [P(Params), i32, i32, P(vp)]
+    L.bh_destroy.argtypes = [vp]
+    L.bh_set_params.argtypes = [vp, P(Params)]
+    L.bh_get_params.argtypes = [vp, P(Params)]
+    L.bh_num_bodies.argtypes = [vp]
+    L.bh_set_state.argtypes = [vp] + [vp] * 5 + [vp]
+    L.bh_get_state.argtypes = [vp] + [vp] * 5 + [vp]
+    L.bh_get_accel.argtypes = [vp, vp, vp, vp]
+    L.bh_get_positions_hilo.argtypes = [vp, vp, vp, vp, vp, vp]
+    L.bh_step.argtypes = [vp, i32, vp]
+    L.bh_sync.argtypes = [vp, vp]
+    L.bh_get_stats.argtypes = [vp, P(Stats), vp]
+    L.bh_get_debug.argtypes = [vp, ctypes.c_char_p, vp, sz, vp]
+    L.bh_step_profiled.argtypes = [vp, vp, vp]
+    L.bh_direct_sum_f64.argtypes = [vp, i32, vp, vp, vp]
+    L.bh_measure_fp32_peak.argtypes = [i32, P(ctypes.c_double)]
+    L.bh_status_string.argtypes = [i32]
+    L.bh_status_string.restype = ctypes.c_char_p
+    L.bh_last_error.restype = ctypes.c_char_p
+    L.bh_version.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+def _status_string(code: int) -> str:
+    try:
+        return lib().bh_status_string(code).decode()
+    except Exception:  # pragma: no cover - only while the library is absent
+        return "?"
+
+
+def last_error() -> str:
+    return lib().bh_last_error().decode()
+
+
+def _check(code: int, what: str):
+    if code != BH_OK:
+        raise BHError(code, what)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def measure_fp32_peak(device: int = -1) -> float:
+    """Measured FP32 FMA throughput of the device in TFLOP/s."""
+    v = ctypes.c_double(0.0)
+    _check(lib().bh_measure_fp32_peak(device, ctypes.byref(v)), "bh_measure_fp32_peak")
+    return float(v.value)
+
+
+def make_params(mode="reference", theta=0.5, eps2=0.025, gravity=1.0, timestep=1e-3,
+                dampening=1.0, leaf_bucket=0, use_graph=False, stack_depth=0,
+                block_size=0) -> Params:
+    p = Params()
+    lib().bh_default_params(ctypes.byref(p))
+    p.mode = MODES[mode] if isinstance(mode, str) else int(mode)
+    p.theta, p.eps2, p.gravity = theta, eps2, gravity
+    p.timestep, p.dampening = timestep, dampening
+    p.leaf_bucket, p.use_graph = int(leaf_bucket), int(bool(use_graph))
+    p.stack_depth, p.block_size = int(stack_depth), int(block_size)
+    return p
+
+
+class BarnesHutSystem:
+    """One system of n bodies on one GPU (BarnesHutParticleSystem.cpp:28-84)."""
+
+    def __init__(self, n: int, device: int = 0, **params):
+        self.n = int(n)
+        self.params = make_params(**params)
+        h = ctypes.c_void_p()
+        _check(lib().bh_create(ctypes.byref(self.params), self.n, device, ctypes.byref(h)),
+               "bh_create")
+        self._h = h
+
+    # lifecycle -----------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().bh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    # state ----------------------------------------------------------------
+    def set_params(self, **params):
+        p = make_params(**params)
+        _check(lib().bh_set_params(self._h, ctypes.byref(p)), "bh_set_params")
+        self.params = p
+
+    def set_state(self, x, y, vx, vy, m, stream=None):
+        arrs = [_f32(a) for a in (x, y, vx, vy, m)]
+        for a in arrs:
+            if a.shape != (self.n,):
+                raise ValueError(f"expected arrays of shape ({self.n},), got {a.shape}")
+        _check(lib().bh_set_state(self._h, *[_p(a) for a in arrs], stream), "bh_set_state")
+        self.sync(stream)
+
+    def set_state_ptrs(self, x, y, vx, vy, m, stream=None):
+        """Raw pointers (host or device), no copy of the arrays on the Python side."""
+        _check(lib().bh_set_state(self._h, x, y, vx, vy, m, stream), "bh_set_state")
+
+    def get_state(self, stream=None):
+        out = {k: np.empty(self.n, np.float32) for k in ("x", "y", "vx", "vy", "m")}
+        _check(lib().bh_get_state(self._h, *[_p(out[k]) for k in ("x", "y", "vx", "vy", "m")],
+                                  stream), "bh_get_state")
+        self.sync(stream)
+        return out
+
+    def get_positions_hilo(self, stream=None):
+        out = [np.empty(self.n, np.float32) for _ in range(4)]
+        _check(lib().bh_get_positions_hilo(self._h, *[_p(a) for a in out], stream),
+               "bh_get_positions_hilo")
+        self.sync(stream)
+        return out  # xhi, xlo, yhi, ylo
+
+    def get_accel(self, stream=None):
+        ax = np.empty(self.n, np.float32)
+        ay = np.empty(self.n, np.float32)
+        _check(lib().bh_get_accel(self._h, _p(ax), _p(ay), stream), "bh_get_accel")
+        self.sync(stream)
+        return ax, ay
+
+    # stepping ---------------------------------------------------------------
+    def step(self, steps: int = 1, stream=None):
+        _check(lib().bh_step(self._h, int(steps), stream), "bh_step")
+
+    def step_profiled(self, phase_ms: np.ndarray, stream=None):
+        """One non-graph step with events at the phase boundaries; adds each
+        phase's milliseconds to phase_ms (float32[8]: bbox, keys, sort,
+        reorder, build, moments, records, walk)."""
+        assert phase_ms.dtype == np.float32 and phase_ms.shape == (PHASES_N,)
+        _check(lib().bh_step_profiled(self._h, stream, _p(phase_ms)), "bh_step_profiled")
+
+    def direct_sum_f64(self, idx):
+        """FP64 direct-sum accelerations (times G) at caller indices idx."""
+        idx = np.ascontiguousarray(idx, dtype=np.int32)
+        ax = np.empty(len(idx), np.float64)
+        ay = np.empty(len(idx), np.float64)
+        _check(lib().bh_direct_sum_f64(self._h, len(idx), _p(idx), _p(ax), _p(ay)),
+               "bh_direct_sum_f64")
+        return ax, ay
+
+    def sync(self, stream=None):
+        _check(lib().bh_sync(self._h, stream), "bh_sync")
+
+    def stats(self, stream=None) -> dict:
+        s = Stats()
+        _check(lib().bh_get_stats(self._h, ctypes.byref(s), stream), "bh_get_stats")
+        return dict(interactions=int(s.interactions), cells=int(s.cells), nodes=int(s.nodes),
+                    max_depth=int(s.max_depth), status=int(s.status), box=np.array(s.box[:]))
+
+    def debug(self, name: str):
+        n = self.n
+        spec = {"box": (np.float32, 4), "keys": (np.uint64, n), "perm": (np.int32, n),
+                "accel_sorted": (np.float32, 2 * n)}
+        dt, cnt = spec.get(name, (np.float32 if name in ("node_m", "node_mx", "node_my",
+                                                          "node_cx", "node_cy") else np.int32, n))
+        out = np.empty(cnt, dt)
+        _check(lib().bh_get_debug(self._h, name.encode(), _p(out), out.nbytes, None),
+               f"bh_get_debug({name})")
+        return out

@@ -1,0 +1,604 @@
+// Device kernels of the GB300 (sm_103a) 2D Barnes-Hut step.
+//
+// Pipeline per step (one launch per phase over every system of the batch):
+//   k_bbox     box of each system, origin included      kernels.cu:51-58, 62-114
+//   k_keys     32-level quadrant keys by float bisection  kernels.cu:137-185
+//   k_radix_*  LSD radix sort of (key, position)         replaces build+sort, kernels.cu:117-336
+//   k_gather   bodies into key order                      (reference never reorders)
+//   k_build    binary radix tree over the sorted keys     replaces kernels.cu:117-271
+//   k_moments  bottom-up mass sums / quadrupoles           kernels.cu:180-183, 275-288
+//   k_records  walk records of the branching nodes
+//   k_walk_*   warp-cooperative walk fused with update    kernels.cu:340-435, 522-537
+//
+// Layout: bodies are SoA float arrays kept in key order between steps, so
+// consecutive warps read consecutive memory.  Systems ("segments") are
+// contiguous ranges [off[s], off[s+1]).  Internal tree node i (Karras
+// numbering) covers a body range that starts or ends at position i; the node
+// at a segment's first position is that segment's root and the node at its
+// last position is unused.  A child reference >= 0 is a node, < 0 is ~body.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <climits>
+
+namespace ssg {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kNoChild = INT_MIN;
+
+// sticky device status bits, mapped to BH_* codes by the host
+enum : int { ST_DUP = 1, ST_NONFINITE = 2, ST_STACK = 4, ST_CAPACITY = 8 };
+
+// ------------------------------------------------------------------ helpers
+
+// float <-> int with the same ordering, for lock-free atomicMin/Max
+__device__ __forceinline__ int f2ord(float f) {
+    int i = __float_as_int(f);
+    return i >= 0 ? i : (i ^ 0x7fffffff);
+}
+__device__ __forceinline__ float ord2f(int i) { return __int_as_float(i >= 0 ? i : (i ^ 0x7fffffff)); }
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+struct Segs {
+    int nseg;               // number of systems
+    const int* off;         // [nseg+1] body offsets
+    const int* seg_of_pos;  // [n] system of each position (nullptr when nseg == 1)
+};
+
+__device__ __forceinline__ int seg_of(const Segs& s, int i) {
+    return s.nseg == 1 ? 0 : __ldg(s.seg_of_pos + i);
+}
+
+struct Box {
+    float l, r, b, t;
+};
+
+__device__ __forceinline__ Box load_box(const int* box_ord, int seg) {
+    int4 o = *reinterpret_cast<const int4*>(box_ord + 4 * seg);
+    return Box{ord2f(o.x), ord2f(o.y), ord2f(o.z), ord2f(o.w)};
+}
+
+// exclusive scan over a block of THREADS threads (one value each)
+template <int THREADS>
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* total, uint32_t* s_tmp) {
+    constexpr int W = THREADS / 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(kFull, x, o);
+        if (lane >= o) x += t;
+    }
+    if (lane == 31) s_tmp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < W ? s_tmp[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t t = __shfl_up_sync(kFull, w, o);
+            if (lane >= o) w += t;
+        }
+        if (lane < W) s_tmp[lane] = w;
+    }
+    __syncthreads();
+    uint32_t prefix = warp > 0 ? s_tmp[warp - 1] : 0u;
+    *total = s_tmp[W - 1];
+    __syncthreads();
+    return prefix + x - v;
+}
+
+// ------------------------------------------------------------------ (a) box
+
+// One block per chunk of one system.  Each thread folds its bodies into a box
+// that starts at the origin (the reference resets the box to 0, kernels.cu:54-57),
+// then warp shuffles, shared memory, and one atomicMin/Max per value and block.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) k_bbox(const float* __restrict__ x,
+                                                  const float* __restrict__ y,
+                                                  const int* __restrict__ chunk_seg,
+                                                  const int* __restrict__ chunk_begin,
+                                                  const int* __restrict__ chunk_end,
+                                                  int* __restrict__ box_ord, int* __restrict__ status) {
+    const int c = blockIdx.x;
+    const int seg = chunk_seg[c], beg = chunk_begin[c], end = chunk_end[c];
+    float l = 0.0f, r = 0.0f, b = 0.0f, t = 0.0f;
+    bool bad = false;
+    // 16-byte vector loads over the aligned middle of the chunk
+    int a0 = (beg + 3) & ~3;
+    if (a0 > end) a0 = end;
+    int a1 = a0 + ((end - a0) & ~3);
+    for (int i = beg + threadIdx.x; i < a0; i += THREADS) {
+        float xv = x[i], yv = y[i];
+        bad |= !isfinite(xv) || !isfinite(yv);
+        l = fminf(l, xv); r = fmaxf(r, xv); b = fminf(b, yv); t = fmaxf(t, yv);
+    }
+    const float4* x4 = reinterpret_cast<const float4*>(x + a0);
+    const float4* y4 = reinterpret_cast<const float4*>(y + a0);
+    for (int i = threadIdx.x; i < (a1 - a0) / 4; i += THREADS) {
+        float4 xv = __ldcs(x4 + i), yv = __ldcs(y4 + i);
+        bad |= !isfinite(xv.x) || !isfinite(xv.y) || !isfinite(xv.z) || !isfinite(xv.w);
+        bad |= !isfinite(yv.x) || !isfinite(yv.y) || !isfinite(yv.z) || !isfinite(yv.w);
+        l = fminf(fminf(l, fminf(xv.x, xv.y)), fminf(xv.z, xv.w));
+        r = fmaxf(fmaxf(r, fmaxf(xv.x, xv.y)), fmaxf(xv.z, xv.w));
+        b = fminf(fminf(b, fminf(yv.x, yv.y)), fminf(yv.z, yv.w));
+        t = fmaxf(fmaxf(t, fmaxf(yv.x, yv.y)), fmaxf(yv.z, yv.w));
+    }
+    for (int i = a1 + threadIdx.x; i < end; i += THREADS) {
+        float xv = x[i], yv = y[i];
+        bad |= !isfinite(xv) || !isfinite(yv);
+        l = fminf(l, xv); r = fmaxf(r, xv); b = fminf(b, yv); t = fmaxf(t, yv);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        l = fminf(l, __shfl_xor_sync(kFull, l, o));
+        r = fmaxf(r, __shfl_xor_sync(kFull, r, o));
+        b = fminf(b, __shfl_xor_sync(kFull, b, o));
+        t = fmaxf(t, __shfl_xor_sync(kFull, t, o));
+    }
+    __shared__ float s[4][THREADS / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        s[0][warp] = l; s[1][warp] = r; s[2][warp] = b; s[3][warp] = t;
+    }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(status, ST_NONFINITE);
+    if (warp == 0) {
+        l = lane < THREADS / 32 ? s[0][lane] : 0.0f;
+        r = lane < THREADS / 32 ? s[1][lane] : 0.0f;
+        b = lane < THREADS / 32 ? s[2][lane] : 0.0f;
+        t = lane < THREADS / 32 ? s[3][lane] : 0.0f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            l = fminf(l, __shfl_xor_sync(kFull, l, o));
+            r = fmaxf(r, __shfl_xor_sync(kFull, r, o));
+            b = fminf(b, __shfl_xor_sync(kFull, b, o));
+            t = fmaxf(t, __shfl_xor_sync(kFull, t, o));
+        }
+        if (lane == 0) {
+            int* bo = box_ord + 4 * seg;
+            atomicMin(bo + 0, f2ord(l));
+            atomicMax(bo + 1, f2ord(r));
+            atomicMin(bo + 2, f2ord(b));
+            atomicMax(bo + 3, f2ord(t));
+        }
+    }
+}
+
+// ------------------------------------------------------------------ (b1) keys
+
+// Level by level: mid = (lo+hi)*0.5 in float, digit bit 0 = x < mid_x,
+// bit 1 = y < mid_y, the body's half becomes the interval (kernels.cu:144-157,
+// 165-177).  Explicit _rn intrinsics: no contraction may change a midpoint.
+__device__ __forceinline__ uint64_t quad_key(float px, float py, Box bx) {
+    float l = bx.l, r = bx.r, b = bx.b, t = bx.t;
+    uint64_t key = 0;
+#pragma unroll 8
+    for (int level = 0; level < 32; ++level) {
+        float mx = __fmul_rn(__fadd_rn(l, r), 0.5f);
+        float my = __fmul_rn(__fadd_rn(b, t), 0.5f);
+        bool xl = px < mx, yl = py < my;
+        r = xl ? mx : r;
+        l = xl ? l : mx;
+        t = yl ? my : t;
+        b = yl ? b : my;
+        key = (key << 2) | (uint64_t)((xl ? 1u : 0u) | (yl ? 2u : 0u));
+    }
+    return key;
+}
+
+__global__ void k_keys(const float* __restrict__ x, const float* __restrict__ y, int n, Segs segs,
+                       const int* __restrict__ box_ord, uint64_t* __restrict__ keys,
+                       uint32_t* __restrict__ vals) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Box bx = load_box(box_ord, seg_of(segs, i));
+    keys[i] = quad_key(x[i], y[i], bx);
+    vals[i] = (uint32_t)i;
+}
+
+// ------------------------------------------------------------------ (b2) radix sort
+
+// Digit of one element: 8 bits of the key, or of the element's system index
+// (the final passes group the systems; stable LSD keeps key order inside).
+__device__ __forceinline__ uint32_t radix_digit(uint64_t k, uint32_t v, int shift, int use_seg,
+                                                const int* __restrict__ seg_of_pos) {
+    return use_seg ? ((uint32_t)__ldg(seg_of_pos + v) >> shift) & 255u
+                   : (uint32_t)(k >> shift) & 255u;
+}
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;
+
+// per-tile digit counts, written digit-major: hist[d * tiles + tile]
+__global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint64_t* __restrict__ keys,
+                                                             const uint32_t* __restrict__ vals, int n,
+                                                             int shift, int use_seg,
+                                                             const int* __restrict__ seg_of_pos,
+                                                             uint32_t* __restrict__ hist, int tiles) {
+    __shared__ uint32_t s_hist[256];
+    s_hist[threadIdx.x] = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int base = blockIdx.x * kSortTile;
+#pragma unroll
+    for (int it = 0; it < kSortItems; ++it) {
+        int idx = base + it * kSortThreads + threadIdx.x;
+        bool valid = idx < n;
+        uint32_t d = valid ? radix_digit(keys[idx], use_seg ? vals[idx] : 0u, shift, use_seg,
+                                         seg_of_pos)
+                           : 0u;
+        unsigned peers = __match_any_sync(kFull, valid ? d : 256u + lane);
+        if (valid && (__ffs(peers) - 1) == lane) atomicAdd(&s_hist[d], (uint32_t)__popc(peers));
+    }
+    __syncthreads();
+    hist[threadIdx.x * tiles + blockIdx.x] = s_hist[threadIdx.x];
+}
+
+// block d turns column d of hist into exclusive offsets; totals[d] = column sum
+__global__ void __launch_bounds__(kSortThreads) k_radix_scan(uint32_t* __restrict__ hist, int tiles,
+                                                             uint32_t* __restrict__ totals) {
+    __shared__ uint32_t s_tmp[kSortThreads / 32];
+    uint32_t* col = hist + (size_t)blockIdx.x * tiles;
+    uint32_t running = 0;
+    for (int base = 0; base < tiles; base += kSortThreads) {
+        int i = base + threadIdx.x;
+        uint32_t v = i < tiles ? col[i] : 0u;
+        uint32_t tot;
+        uint32_t ex = block_excl_scan<kSortThreads>(v, &tot, s_tmp);
+        if (i < tiles) col[i] = running + ex;
+        running += tot;
+    }
+    if (threadIdx.x == 0) totals[blockIdx.x] = running;
+}
+
+// Stable scatter of one tile: warp w owns 256 consecutive elements, ranks are
+// (earlier rounds of the warp) + (lower lanes with the same digit); warps are
+// then offset by the counts of lower warps.  Elements are staged in shared
+// memory in digit order and written out as contiguous runs.
+__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(
+    const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
+    uint32_t* __restrict__ vout, int n, int shift, int use_seg, const int* __restrict__ seg_of_pos,
+    const uint32_t* __restrict__ hist, const uint32_t* __restrict__ totals, int tiles) {
+    constexpr int W = kSortThreads / 32;
+    constexpr int WCHUNK = 32 * kSortItems;
+    __shared__ uint32_t s_wh[W][256];
+    __shared__ uint32_t s_gbase[256];
+    __shared__ uint32_t s_lstart[256];
+    __shared__ uint32_t s_tmp[W];
+    __shared__ uint64_t s_k[kSortTile];
+    __shared__ uint32_t s_v[kSortTile];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i < W * 256; i += kSortThreads) (&s_wh[0][0])[i] = 0u;
+    {
+        uint32_t tot;
+        uint32_t ex = block_excl_scan<kSortThreads>(totals[tid], &tot, s_tmp);
+        s_gbase[tid] = ex + hist[(size_t)tid * tiles + blockIdx.x];
+    }
+    __syncthreads();
+    const int base = blockIdx.x * kSortTile;
+    uint64_t k[kSortItems];
+    uint32_t v[kSortItems];
+    uint32_t rank[kSortItems];
+    int dg[kSortItems];
+    const unsigned lt = lanemask_lt();
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        int idx = base + warp * WCHUNK + r * 32 + lane;
+        bool valid = idx < n;
+        k[r] = valid ? kin[idx] : 0ull;
+        v[r] = valid ? vin[idx] : 0u;
+        uint32_t d = valid ? radix_digit(k[r], v[r], shift, use_seg, seg_of_pos) : 0u;
+        dg[r] = valid ? (int)d : -1;
+        unsigned peers = __match_any_sync(kFull, valid ? d : 256u + lane);
+        rank[r] = valid ? s_wh[warp][d] + (uint32_t)__popc(peers & lt) : 0u;
+        __syncwarp();
+        if (valid && (__ffs(peers) - 1) == lane) s_wh[warp][d] += (uint32_t)__popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    {
+        uint32_t run = 0;
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            uint32_t c = s_wh[w][tid];
+            s_wh[w][tid] = run;
+            run += c;
+        }
+        uint32_t tot;
+        s_lstart[tid] = block_excl_scan<kSortThreads>(run, &tot, s_tmp);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        if (dg[r] >= 0) {
+            uint32_t pos = s_lstart[dg[r]] + s_wh[warp][dg[r]] + rank[r];
+            s_k[pos] = k[r];
+            s_v[pos] = v[r];
+        }
+    }
+    __syncthreads();
+    const int tile_n = min(kSortTile, n - base);
+    for (int i = tid; i < tile_n; i += kSortThreads) {
+        uint64_t kk = s_k[i];
+        uint32_t vv = s_v[i];
+        uint32_t d = radix_digit(kk, vv, shift, use_seg, seg_of_pos);
+        uint32_t o = s_gbase[d] + ((uint32_t)i - s_lstart[d]);
+        kout[o] = kk;
+        vout[o] = vv;
+    }
+}
+
+// ------------------------------------------------------------------ (d) reorder
+
+struct BodyPtrs {
+    float *x, *y, *vx, *vy, *m, *xlo, *ylo;  // xlo/ylo may be null
+    int* id;
+};
+
+__global__ void k_gather(int n, const uint32_t* __restrict__ perm, BodyPtrs src, BodyPtrs dst) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    uint32_t i = perm[j];
+    dst.x[j] = src.x[i];
+    dst.y[j] = src.y[i];
+    dst.vx[j] = src.vx[i];
+    dst.vy[j] = src.vy[i];
+    dst.m[j] = src.m[i];
+    dst.id[j] = src.id[i];
+    if (src.xlo) {
+        dst.xlo[j] = src.xlo[i];
+        dst.ylo[j] = src.ylo[i];
+    }
+}
+
+// ------------------------------------------------------------------ (b3) tree
+
+// Leading equal bits of sorted keys i and j inside [lo, hi]; equal keys are
+// told apart by position (bits 64..95) so the tree stays binary.
+__device__ __forceinline__ int kdelta(const uint64_t* __restrict__ k, int i, int j, int lo, int hi) {
+    if (j < lo || j > hi) return -1;
+    uint64_t a = k[i], b = k[j];
+    return a != b ? __clzll(a ^ b) : 64 + __clz(i ^ j);
+}
+
+struct TreePtrs {
+    int *left, *right, *parent, *leaf_parent, *split, *first, *last;
+};
+
+// Karras (2012) radix-tree construction, one thread per internal node.
+__global__ void k_build(const uint64_t* __restrict__ k, int n, Segs segs, TreePtrs t,
+                        int* __restrict__ status) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int s = seg_of(segs, i);
+    int lo = segs.off[s], hi = segs.off[s + 1] - 1;
+    if (i < hi && k[i] == k[i + 1]) atomicOr(status, ST_DUP);
+    if (i == hi) {  // last position of a system: not an internal node
+        t.left[i] = kNoChild;
+        t.right[i] = kNoChild;
+        t.split[i] = -1;
+        t.first[i] = i;
+        t.last[i] = i;
+        if (lo == hi) {
+            t.leaf_parent[i] = -1;
+            t.parent[i] = -1;
+        }
+        return;
+    }
+    if (i == lo) t.parent[i] = -1;
+    int dl = kdelta(k, i, i - 1, lo, hi), dr = kdelta(k, i, i + 1, lo, hi);
+    int d = dr > dl ? 1 : -1;
+    int dmin = min(dl, dr);
+    int lmax = 2;
+    while (kdelta(k, i, i + lmax * d, lo, hi) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int step = lmax >> 1; step >= 1; step >>= 1)
+        if (kdelta(k, i, i + (l + step) * d, lo, hi) > dmin) l += step;
+    int j = i + l * d;
+    int dnode = kdelta(k, i, j, lo, hi);
+    int sp = 0;
+    for (int div = 2;; div <<= 1) {
+        int step = (l + div - 1) / div;
+        if (kdelta(k, i, i + (sp + step) * d, lo, hi) > dnode) sp += step;
+        if (step <= 1) break;
+    }
+    int g = i + sp * d + min(d, 0);
+    int a = min(i, j), b = max(i, j);
+    if (a == g) {
+        t.left[i] = ~g;
+        t.leaf_parent[g] = i;
+    } else {
+        t.left[i] = g;
+        t.parent[g] = i;
+    }
+    if (b == g + 1) {
+        t.right[i] = ~(g + 1);
+        t.leaf_parent[g + 1] = i;
+    } else {
+        t.right[i] = g + 1;
+        t.parent[g + 1] = i;
+    }
+    t.split[i] = dnode;
+    t.first[i] = a;
+    t.last[i] = b;
+}
+
+// ------------------------------------------------------------------ (c) moments
+
+struct NodeSums {
+    float *m, *mx, *my, *cx, *cy;
+    float4* quad;  // Sxx, Sxy, Syy about the centre of mass (accuracy modes)
+};
+
+struct ChildVals {
+    float m, mx, my, cx, cy, sxx, sxy, syy;
+};
+
+__device__ __forceinline__ ChildVals load_child(int c, const float* __restrict__ sx,
+                                                const float* __restrict__ sy,
+                                                const float* __restrict__ sm, const NodeSums& ns,
+                                                bool quad) {
+    ChildVals v;
+    if (c < 0) {
+        int bi = ~c;
+        v.m = sm[bi];
+        v.cx = sx[bi];
+        v.cy = sy[bi];
+        v.mx = __fmul_rn(v.m, v.cx);  // kernels.cu:180: mass*x
+        v.my = __fmul_rn(v.m, v.cy);
+        v.sxx = v.sxy = v.syy = 0.0f;
+    } else {
+        // written by another thread of this launch: read through L2
+        v.m = __ldcg(ns.m + c);
+        v.mx = __ldcg(ns.mx + c);
+        v.my = __ldcg(ns.my + c);
+        v.cx = __ldcg(ns.cx + c);
+        v.cy = __ldcg(ns.cy + c);
+        if (quad) {
+            float4 q = __ldcg(ns.quad + c);
+            v.sxx = q.x;
+            v.sxy = q.y;
+            v.syy = q.z;
+        } else {
+            v.sxx = v.sxy = v.syy = 0.0f;
+        }
+    }
+    return v;
+}
+
+// Bottom-up: each body climbs from its leaf; the second thread to reach a node
+// combines both children (left + right, so the sums do not depend on which
+// thread arrives last) and continues.  REFERENCE mode keeps the reference's
+// definition com = (sum m*x) / (sum m) (kernels.cu:283-284); accuracy modes
+// combine centres relative to each other and add second moments.
+__global__ void k_moments(int n, int accuracy, const float* __restrict__ sx,
+                          const float* __restrict__ sy, const float* __restrict__ sm,
+                          const int* __restrict__ left, const int* __restrict__ right,
+                          const int* __restrict__ parent, const int* __restrict__ leaf_parent,
+                          int* __restrict__ counter, NodeSums ns) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    int p = leaf_parent[j];
+    while (p >= 0) {
+        __threadfence();
+        if (atomicAdd(counter + p, 1) == 0) return;
+        __threadfence();
+        ChildVals a = load_child(left[p], sx, sy, sm, ns, accuracy);
+        ChildVals b = load_child(right[p], sx, sy, sm, ns, accuracy);
+        float M = __fadd_rn(a.m, b.m);
+        float MX = __fadd_rn(a.mx, b.mx);
+        float MY = __fadd_rn(a.my, b.my);
+        float cx, cy;
+        if (!accuracy) {
+            cx = __fdiv_rn(MX, M);
+            cy = __fdiv_rn(MY, M);
+        } else {
+            float w = M > 0.0f ? b.m / M : 0.5f;
+            cx = fmaf(w, b.cx - a.cx, a.cx);
+            cy = fmaf(w, b.cy - a.cy, a.cy);
+            float ax = a.cx - cx, ay = a.cy - cy, bx = b.cx - cx, by = b.cy - cy;
+            float sxx = a.sxx + b.sxx + a.m * ax * ax + b.m * bx * bx;
+            float sxy = a.sxy + b.sxy + a.m * ax * ay + b.m * bx * by;
+            float syy = a.syy + b.syy + a.m * ay * ay + b.m * by * by;
+            ns.quad[p] = make_float4(sxx, sxy, syy, 0.0f);
+        }
+        ns.m[p] = M;
+        ns.mx[p] = MX;
+        ns.my[p] = MY;
+        ns.cx[p] = cx;
+        ns.cy[p] = cy;
+        p = parent[p];
+    }
+}
+
+// ------------------------------------------------------------------ walk records
+
+// Branching quadtree nodes: a binary node splitting the low bit of a digit is
+// folded into its parent when the parent splits the high bit of the same digit.
+__device__ __forceinline__ bool merged_into(int c_split, int p_split) {
+    return (c_split & 1) && p_split == c_split - 1;
+}
+
+struct Records {
+    float4* A;  // cx, cy, M, criterion (REFERENCE: dp of the node's level; accuracy: ropen^2)
+    float4* B;  // accuracy: 3Sxx, 3Sxy, 3Syy, 1.5 (Sxx+Syy)
+    int4* C;    // up to four children, kNoChild padded
+    int2* D;    // first body, body count
+};
+
+// dp_L = w_L^2/theta with w_L the level-L cell width from the x extent only:
+// radius = (right-left)*0.5 (kernels.cu:349), root children pushed with
+// radius^2/theta (:376), times 0.25 per level (:395).  Cells at level <= 1 are
+// never approximated (+inf).
+__device__ __forceinline__ float ref_dp(Box bx, float theta, int level) {
+    if (level < 2) return __int_as_float(0x7f800000);
+    float radius = __fmul_rn(__fsub_rn(bx.r, bx.l), 0.5f);
+    float dp1 = __fdiv_rn(__fmul_rn(radius, radius), theta);
+    return ldexpf(dp1, -2 * (level - 1));
+}
+
+__global__ void k_records(int n, Segs segs, int accuracy, float theta,
+                          const int* __restrict__ box_ord, const uint64_t* __restrict__ skeys,
+                          const int* __restrict__ left, const int* __restrict__ right,
+                          const int* __restrict__ parent, const int* __restrict__ split,
+                          const int* __restrict__ first, const int* __restrict__ last,
+                          NodeSums ns, Records rec) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int sp = split[i];
+    if (sp < 0) return;  // unused slot
+    int pa = parent[i];
+    if (pa >= 0 && merged_into(sp, split[pa])) return;  // folded into its parent
+    int ch[4] = {kNoChild, kNoChild, kNoChild, kNoChild};
+    int nc = 0;
+    int lr[2] = {left[i], right[i]};
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+        int c = lr[s];
+        if (c >= 0 && merged_into(split[c], sp)) {
+            ch[nc++] = left[c];
+            ch[nc++] = right[c];
+        } else {
+            ch[nc++] = c;
+        }
+    }
+    rec.C[i] = make_int4(ch[0], ch[1], ch[2], ch[3]);
+    int f = first[i], cnt = last[i] - f + 1;
+    rec.D[i] = make_int2(f, cnt);
+    int level = sp >> 1;
+    Box bx = load_box(box_ord, seg_of(segs, i));
+    float cx = ns.cx[i], cy = ns.cy[i], M = ns.m[i];
+    if (!accuracy) {
+        rec.A[i] = make_float4(cx, cy, M, ref_dp(bx, theta, level));
+        return;
+    }
+    // cell rectangle of the node's level from its key prefix (x bit 1 = left half)
+    int L = level < 32 ? level : 32;
+    uint64_t pre = L > 0 ? skeys[f] >> (64 - 2 * L) : 0ull;
+    unsigned long long ix = 0, iy = 0;
+    for (int q = L - 1; q >= 0; --q) {
+        unsigned dgt = (unsigned)(pre >> (2 * q)) & 3u;
+        ix = (ix << 1) | ((dgt & 1u) ? 0ull : 1ull);
+        iy = (iy << 1) | ((dgt & 2u) ? 0ull : 1ull);
+    }
+    double wx = ((double)bx.r - (double)bx.l), wy = ((double)bx.t - (double)bx.b);
+    double scale = ldexp(1.0, -L);
+    double x0 = bx.l + wx * scale * (double)ix, x1 = x0 + wx * scale;
+    double y0 = bx.b + wy * scale * (double)iy, y1 = y0 + wy * scale;
+    double ex = fmax(fabs(cx - x0), fabs(x1 - cx));
+    double ey = fmax(fabs(cy - y0), fabs(y1 - cy));
+    double bmax2 = ex * ex + ey * ey;
+    float ropen2 = (float)(bmax2 / ((double)theta * (double)theta));
+    rec.A[i] = make_float4(cx, cy, M, ropen2);
+    float4 q = ns.quad[i];  // S about the centre of mass -> T = 3S, h = 1.5 tr S
+    rec.B[i] = make_float4(3.0f * q.x, 3.0f * q.y, 3.0f * q.z, 1.5f * (q.x + q.z));
+}
+
+}  // namespace ssg

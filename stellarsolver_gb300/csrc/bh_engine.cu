@@ -1,0 +1,924 @@
+// Host side of the C ABI (include/stellar_bh.h): owns the device arena of one
+// batch of systems and enqueues the per-step pipeline of bh_device.cuh /
+// bh_walk.cuh on the caller's stream, optionally as a replayed CUDA graph.
+//
+// Replaces BarnesHutParticleSystem (BarnesHutParticleSystem.cpp:28-378):
+// allocation in one arena instead of 19 cudaMalloc calls (:54-83), update() as
+// bh_step (:301-347) without the per-step event synchronisation (:318).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bh_engine.h"
+#include "bh_walk.cuh"
+#include "stellar_bh.h"
+
+using namespace ssg;
+
+namespace ssg {
+thread_local std::string g_last_error;
+
+int cuda_fail(cudaError_t e, const char* what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return BH_ERR_CUDA;
+}
+}  // namespace ssg
+
+#define CK(call)                                                     \
+    do {                                                             \
+        cudaError_t e_ = (call);                                     \
+        if (e_ != cudaSuccess) return ssg::cuda_fail(e_, #call);     \
+    } while (0)
+
+namespace {
+
+constexpr int kWalkWarps = 8;
+constexpr int kRefStack = 256;
+constexpr int kAccStack = 1024;
+constexpr int kBboxThreads = 256;
+constexpr int kBboxChunk = 8192;
+
+int walk_grid_cap(int device_sms, int blocks_per_sm) { return device_sms * std::max(1, blocks_per_sm); }
+
+template <typename T>
+T* carve(char*& cur, size_t count) {
+    T* p = reinterpret_cast<T*>(cur);
+    size_t bytes = (sizeof(T) * count + 255) & ~size_t(255);
+    cur += bytes;
+    return p;
+}
+
+template <typename T>
+size_t span(size_t count) {
+    return (sizeof(T) * count + 255) & ~size_t(255);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ walk dispatch
+
+namespace ssg {
+
+template <int BUCKET, bool MIXED>
+static cudaError_t set_acc_attr() {
+    using Sm = AccSmem<kWalkWarps, kAccStack, BUCKET>;
+    return cudaFuncSetAttribute(k_walk_acc<kWalkWarps, kAccStack, BUCKET, MIXED>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Sm));
+}
+
+// Opt every accuracy-walk instantiation into its shared-memory size once, at
+// creation (never while a graph is being captured).
+cudaError_t init_walk_attributes() {
+    cudaError_t e = cudaSuccess;
+    cudaError_t r[8] = {set_acc_attr<1, false>(), set_acc_attr<4, false>(), set_acc_attr<8, false>(),
+                        set_acc_attr<16, false>(), set_acc_attr<1, true>(), set_acc_attr<4, true>(),
+                        set_acc_attr<8, true>(), set_acc_attr<16, true>()};
+    for (cudaError_t x : r)
+        if (x != cudaSuccess) e = x;
+    return e;
+}
+
+template <int BUCKET, bool MIXED>
+static cudaError_t launch_acc(const StepArgs& a, cudaStream_t st) {
+    using Sm = AccSmem<kWalkWarps, kAccStack, BUCKET>;
+    auto kern = k_walk_acc<kWalkWarps, kAccStack, BUCKET, MIXED>;
+    int grid = std::min(a.walk_grid_acc, (a.groups.ngroups + kWalkWarps - 1) / kWalkWarps);
+    if (grid < 1) grid = 1;
+    kern<<<grid, kWalkWarps * 32, sizeof(Sm), st>>>(a.segs, a.groups, a.in, a.recA, a.recB, a.recC,
+                                                    a.recD, a.eps2, a.G, a.dt, a.ddt, a.out,
+                                                    a.status, a.inter);
+    return cudaGetLastError();
+}
+
+template <bool MIXED>
+static cudaError_t launch_acc_bucket(const StepArgs& a, cudaStream_t st) {
+    switch (a.bucket) {
+        case 1: return launch_acc<1, MIXED>(a, st);
+        case 4: return launch_acc<4, MIXED>(a, st);
+        case 16: return launch_acc<16, MIXED>(a, st);
+        default: return launch_acc<8, MIXED>(a, st);
+    }
+}
+
+cudaError_t launch_walk(const StepArgs& a, cudaStream_t st) {
+    if (a.mode == BH_MODE_REFERENCE) {
+        int grid = std::min(a.walk_grid_ref, (a.groups.ngroups + kWalkWarps - 1) / kWalkWarps);
+        if (grid < 1) grid = 1;
+        k_walk_ref<kWalkWarps, kRefStack><<<grid, kWalkWarps * 32, 0, st>>>(
+            a.segs, a.groups, a.in, a.recA, a.recC, a.eps2, a.dt, a.ddt, a.out, a.status, a.inter);
+        return cudaGetLastError();
+    }
+    return a.mode == BH_MODE_MIXED ? launch_acc_bucket<true>(a, st)
+                                   : launch_acc_bucket<false>(a, st);
+}
+
+int normalized_bucket(int b) {
+    if (b <= 1) return b <= 0 ? 8 : 1;
+    if (b <= 4) return 4;
+    if (b <= 8) return 8;
+    return 16;
+}
+
+}  // namespace ssg
+
+// ------------------------------------------------------------------ bh_system
+
+struct bh_system {
+    bh_params p{};
+    int n = 0;
+    int device = 0;
+    int sms = 0;
+    int nseg = 1;
+    std::vector<int> h_off;
+
+    char* arena = nullptr;
+    size_t arena_bytes = 0;
+
+    // state: [0] current (key order of the last step), [1] scratch / gathered
+    BodyPtrs st[2]{};
+    uint64_t *keys = nullptr, *keys_alt = nullptr;
+    uint32_t *vals = nullptr, *vals_alt = nullptr;
+    uint64_t* kfinal = nullptr;  // sorted keys after the last pass
+    uint32_t* vfinal = nullptr;  // permutation after the last pass
+    uint32_t *hist = nullptr, *totals = nullptr;
+    int tiles = 0;
+    int* box_ord = nullptr;
+    int *seg_off = nullptr, *seg_of_pos = nullptr, *gseg_off = nullptr;
+    int *chunk_seg = nullptr, *chunk_begin = nullptr, *chunk_end = nullptr;
+    int nchunks = 0;
+    int ngroups = 0;
+    TreePtrs tree{};
+    int* counter = nullptr;
+    NodeSums sums{};
+    Records rec{};
+    float *ax = nullptr, *ay = nullptr;
+    int* status = nullptr;
+    unsigned long long* inter = nullptr;
+    int seg_passes = 0;
+
+    int walk_grid_ref = 0, walk_grid_acc = 0;
+    bool have_state = false;
+
+    cudaStream_t cap_stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+};
+
+namespace {
+
+void drop_graph(bh_system* s) {
+    if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+    if (s->graph) cudaGraphDestroy(s->graph);
+    s->graph_exec = nullptr;
+    s->graph = nullptr;
+}
+
+bool params_ok(const bh_params* p) {
+    if (!p) return false;
+    if (p->mode < BH_MODE_REFERENCE || p->mode > BH_MODE_MIXED) return false;
+    if (!(p->theta > 0.0f) || !(p->eps2 >= 0.0f)) return false;
+    if (p->mode == BH_MODE_REFERENCE && !(p->eps2 > 0.0f)) return false;
+    return true;
+}
+
+ssg::StepArgs step_args(bh_system* s) {
+    ssg::StepArgs a{};
+    a.mode = s->p.mode;
+    a.segs = Segs{s->nseg, s->seg_off, s->nseg > 1 ? s->seg_of_pos : nullptr};
+    a.groups = Groups{s->ngroups, s->nseg > 1 ? s->gseg_off : nullptr};
+    const BodyPtrs& g = s->st[1];
+    const BodyPtrs& c = s->st[0];
+    bool mixed = s->p.mode == BH_MODE_MIXED;
+    a.in = WalkIn{g.x, g.y, g.vx, g.vy, g.m, mixed ? g.xlo : nullptr, mixed ? g.ylo : nullptr, g.id};
+    a.out = WalkOut{c.x, c.y, c.vx, c.vy, c.m, mixed ? c.xlo : nullptr, mixed ? c.ylo : nullptr, c.id,
+                    s->ax, s->ay};
+    a.recA = s->rec.A;
+    a.recB = s->rec.B;
+    a.recC = s->rec.C;
+    a.recD = s->rec.D;
+    a.eps2 = s->p.eps2;
+    a.G = s->p.gravity;
+    a.dt = s->p.timestep;
+    a.ddt = s->p.dampening * s->p.timestep;  // kernels.cu:532: d*dt, in float
+    a.status = s->status;
+    a.inter = s->inter;
+    a.bucket = normalized_bucket(s->p.leaf_bucket);
+    a.walk_grid_ref = s->walk_grid_ref;
+    a.walk_grid_acc = s->walk_grid_acc;
+    return a;
+}
+
+// ev (optional): kPhases+1 events recorded at the phase boundaries
+int enqueue_step(bh_system* s, cudaStream_t st, cudaEvent_t* ev = nullptr) {
+    const int n = s->n;
+    auto mark = [&](int k) -> cudaError_t { return ev ? cudaEventRecord(ev[k], st) : cudaSuccess; };
+    const bool accuracy = s->p.mode != BH_MODE_REFERENCE;
+    const bool mixed = s->p.mode == BH_MODE_MIXED;
+    Segs segs{s->nseg, s->seg_off, s->nseg > 1 ? s->seg_of_pos : nullptr};
+    CK(cudaMemsetAsync(s->box_ord, 0, sizeof(int) * 4 * s->nseg, st));  // origin box
+    CK(cudaMemsetAsync(s->counter, 0, sizeof(int) * n, st));
+    CK(cudaMemsetAsync(s->inter, 0, sizeof(unsigned long long), st));
+
+    BodyPtrs cur = s->st[0];
+    CK(mark(0));
+    k_bbox<kBboxThreads><<<s->nchunks, kBboxThreads, 0, st>>>(cur.x, cur.y, s->chunk_seg,
+                                                              s->chunk_begin, s->chunk_end,
+                                                              s->box_ord, s->status);
+    const int tb = 256, nb = (n + tb - 1) / tb;
+    CK(mark(1));
+    k_keys<<<nb, tb, 0, st>>>(cur.x, cur.y, n, segs, s->box_ord, s->keys, s->vals);
+    CK(mark(2));
+
+    // LSD radix sort: 8 passes over the key, then the system index
+    uint64_t *ka = s->keys, *kb = s->keys_alt;
+    uint32_t *va = s->vals, *vb = s->vals_alt;
+    const int passes = 8 + s->seg_passes;
+    for (int ps = 0; ps < passes; ++ps) {
+        int use_seg = ps >= 8;
+        int shift = use_seg ? 8 * (ps - 8) : 8 * ps;
+        k_radix_hist<<<s->tiles, kSortThreads, 0, st>>>(ka, va, n, shift, use_seg, s->seg_of_pos,
+                                                        s->hist, s->tiles);
+        k_radix_scan<<<256, kSortThreads, 0, st>>>(s->hist, s->tiles, s->totals);
+        k_radix_scatter<<<s->tiles, kSortThreads, 0, st>>>(ka, va, kb, vb, n, shift, use_seg,
+                                                           s->seg_of_pos, s->hist, s->totals,
+                                                           s->tiles);
+        std::swap(ka, kb);
+        std::swap(va, vb);
+    }
+    s->kfinal = ka;
+    s->vfinal = va;
+    CK(mark(3));
+
+    BodyPtrs src = cur, dst = s->st[1];
+    if (!mixed) {
+        src.xlo = src.ylo = nullptr;
+        dst.xlo = dst.ylo = nullptr;
+    }
+    k_gather<<<nb, tb, 0, st>>>(n, va, src, dst);
+    CK(mark(4));
+    k_build<<<nb, tb, 0, st>>>(ka, n, segs, s->tree, s->status);
+    CK(mark(5));
+    k_moments<<<nb, tb, 0, st>>>(n, accuracy ? 1 : 0, dst.x, dst.y, dst.m, s->tree.left,
+                                 s->tree.right, s->tree.parent, s->tree.leaf_parent, s->counter,
+                                 s->sums);
+    CK(mark(6));
+    k_records<<<nb, tb, 0, st>>>(n, segs, accuracy ? 1 : 0, s->p.theta, s->box_ord, ka,
+                                 s->tree.left, s->tree.right, s->tree.parent, s->tree.split,
+                                 s->tree.first, s->tree.last, s->sums, s->rec);
+    CK(cudaGetLastError());
+    CK(mark(7));
+    StepArgs a = step_args(s);
+    CK(launch_walk(a, st));
+    CK(mark(8));
+    return BH_OK;
+}
+
+// FP32 FMA throughput probe: 8 independent FMA chains per thread, no memory
+// traffic except one store per thread (kept so the chains are not removed).
+__global__ void __launch_bounds__(256) k_ffma_peak(float* out, int iters, float a, float b) {
+    float v0 = threadIdx.x * 1e-3f, v1 = v0 + 1.f, v2 = v0 + 2.f, v3 = v0 + 3.f;
+    float v4 = v0 + 4.f, v5 = v0 + 5.f, v6 = v0 + 6.f, v7 = v0 + 7.f;
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+            v0 = fmaf(v0, a, b); v1 = fmaf(v1, a, b); v2 = fmaf(v2, a, b); v3 = fmaf(v3, a, b);
+            v4 = fmaf(v4, a, b); v5 = fmaf(v5, a, b); v6 = fmaf(v6, a, b); v7 = fmaf(v7, a, b);
+        }
+    }
+    out[blockIdx.x * blockDim.x + threadIdx.x] = v0 + v1 + v2 + v3 + v4 + v5 + v6 + v7;
+}
+
+// FP64 direct sum for a sample of targets: grid (target tiles, source chunks),
+// partial sums per chunk, reduced in a fixed order by k_direct_reduce.
+constexpr int kDirThreads = 256;
+constexpr int kDirChunks = 64;
+
+__global__ void __launch_bounds__(kDirThreads) k_direct_partial(
+    int n, const float* __restrict__ xh, const float* __restrict__ xl, const float* __restrict__ yh,
+    const float* __restrict__ yl, const float* __restrict__ m, int ns, const int* __restrict__ idx,
+    double eps2, double* __restrict__ part) {
+    __shared__ double sx[kDirThreads], sy[kDirThreads], sm[kDirThreads];
+    __shared__ int sid[kDirThreads];
+    const int t = blockIdx.x * kDirThreads + threadIdx.x;
+    const bool active = t < ns;
+    const int ti = active ? idx[t] : -1;
+    const double px = active ? (double)xh[ti] + (xl ? (double)xl[ti] : 0.0) : 0.0;
+    const double py = active ? (double)yh[ti] + (yl ? (double)yl[ti] : 0.0) : 0.0;
+    const int per = (n + gridDim.y - 1) / gridDim.y;
+    const int beg = blockIdx.y * per, end = min(n, beg + per);
+    double ax = 0.0, ay = 0.0;
+    for (int base = beg; base < end; base += kDirThreads) {
+        int j = base + threadIdx.x;
+        __syncthreads();
+        if (j < end) {
+            sx[threadIdx.x] = (double)xh[j] + (xl ? (double)xl[j] : 0.0);
+            sy[threadIdx.x] = (double)yh[j] + (yl ? (double)yl[j] : 0.0);
+            sm[threadIdx.x] = m[j];
+            sid[threadIdx.x] = j;
+        } else {
+            sid[threadIdx.x] = -1;
+        }
+        __syncthreads();
+        const int cnt = min(kDirThreads, end - base);
+        if (active) {
+            for (int k = 0; k < cnt; ++k) {
+                if (sid[k] == ti) continue;
+                double dx = sx[k] - px, dy = sy[k] - py;
+                double r2 = dx * dx + dy * dy + eps2;
+                double inv = 1.0 / (r2 * sqrt(r2));
+                ax += sm[k] * dx * inv;
+                ay += sm[k] * dy * inv;
+            }
+        }
+    }
+    if (active) {
+        part[(size_t)blockIdx.y * 2 * ns + t] = ax;
+        part[(size_t)blockIdx.y * 2 * ns + ns + t] = ay;
+    }
+}
+
+__global__ void k_direct_reduce(int ns, int chunks, const double* __restrict__ part, double G,
+                                double* __restrict__ out) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 2 * ns) return;
+    double acc = 0.0;
+    for (int c = 0; c < chunks; ++c) acc += part[(size_t)c * 2 * ns + t];
+    out[t] = G * acc;
+}
+
+int build_graph(bh_system* s) {
+    drop_graph(s);
+    if (!s->cap_stream) CK(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
+    CK(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal));
+    int st = enqueue_step(s, s->cap_stream);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s->cap_stream, &g);
+    if (st != BH_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    s->graph = g;
+    CK(cudaGraphInstantiate(&s->graph_exec, g, 0));
+    return BH_OK;
+}
+
+__global__ void k_iota(int* id, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) id[i] = i;
+}
+
+// out[id[j]] = in[j] for up to four arrays
+__global__ void k_scatter4(int n, const int* __restrict__ id, const float* a0, const float* a1,
+                           const float* a2, const float* a3, float* o0, float* o1, float* o2,
+                           float* o3) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    int i = id[j];
+    if (a0) o0[i] = a0[j];
+    if (a1) o1[i] = a1[j];
+    if (a2) o2[i] = a2[j];
+    if (a3) o3[i] = a3[j];
+}
+
+int status_code(int bits, int mode) {
+    if (bits & ST_NONFINITE) return BH_ERR_NONFINITE;
+    if ((bits & ST_DUP) && mode == BH_MODE_REFERENCE) return BH_ERR_DUPLICATE_KEYS;
+    if (bits & ST_STACK) return BH_ERR_STACK;
+    if (bits & ST_CAPACITY) return BH_ERR_CAPACITY;
+    return BH_OK;
+}
+
+}  // namespace
+
+namespace ssg {
+
+int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh_system** out) {
+    if (!out || !params_ok(p) || nseg < 1 || !sizes) return BH_ERR_ARG;
+    *out = nullptr;
+    long long total = 0;
+    for (int i = 0; i < nseg; ++i) {
+        if (sizes[i] < 1) return BH_ERR_ARG;
+        total += sizes[i];
+    }
+    if (total > (1ll << 30)) return BH_ERR_CAPACITY;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        g_last_error = "no CUDA device";
+        return BH_ERR_NO_DEVICE;
+    }
+    if (device < 0) CK(cudaGetDevice(&device));
+    CK(cudaSetDevice(device));
+    cudaDeviceProp prop;
+    CK(cudaGetDeviceProperties(&prop, device));
+    if (prop.major < 10) {
+        g_last_error = "device is not Blackwell (sm_103a build)";
+        return BH_ERR_NO_DEVICE;
+    }
+
+    bh_system* s = new bh_system();
+    s->p = *p;
+    s->n = (int)total;
+    s->device = device;
+    s->sms = prop.multiProcessorCount;
+    s->nseg = nseg;
+    s->h_off.resize(nseg + 1);
+    s->h_off[0] = 0;
+    for (int i = 0; i < nseg; ++i) s->h_off[i + 1] = s->h_off[i] + sizes[i];
+    const size_t N = (size_t)s->n;
+    s->tiles = (int)((N + kSortTile - 1) / kSortTile);
+    s->seg_passes = nseg == 1 ? 0 : (nseg <= 256 ? 1 : 2);
+
+    // chunk table for the box reduction and group table for the walks
+    std::vector<int> cseg, cbeg, cend, goff(nseg + 1, 0);
+    for (int sg = 0; sg < nseg; ++sg) {
+        for (int b = s->h_off[sg]; b < s->h_off[sg + 1]; b += kBboxChunk) {
+            cseg.push_back(sg);
+            cbeg.push_back(b);
+            cend.push_back(std::min(b + kBboxChunk, s->h_off[sg + 1]));
+        }
+        goff[sg + 1] = goff[sg] + (sizes[sg] + 31) / 32;
+    }
+    s->nchunks = (int)cseg.size();
+    s->ngroups = goff[nseg];
+
+    size_t bytes = 0;
+    bytes += 2 * (7 * span<float>(N) + span<int>(N));
+    bytes += 2 * span<uint64_t>(N) + 2 * span<uint32_t>(N);
+    bytes += span<uint32_t>((size_t)256 * s->tiles) + span<uint32_t>(256);
+    bytes += span<int>(4 * (size_t)nseg) + 2 * span<int>(nseg + 1) + span<int>(N);
+    bytes += 3 * span<int>(s->nchunks);
+    bytes += 8 * span<int>(N);
+    bytes += 5 * span<float>(N) + span<float4>(N);
+    bytes += 2 * span<float4>(N) + span<int4>(N) + span<int2>(N);
+    bytes += 2 * span<float>(N) + span<int>(1) + span<unsigned long long>(1);
+    cudaError_t e = cudaMalloc(&s->arena, bytes);
+    if (e != cudaSuccess) {
+        cuda_fail(e, "cudaMalloc(arena)");
+        delete s;
+        return BH_ERR_NOMEM;
+    }
+    s->arena_bytes = bytes;
+    char* c = s->arena;
+    for (int k = 0; k < 2; ++k) {
+        BodyPtrs& b = s->st[k];
+        b.x = carve<float>(c, N);
+        b.y = carve<float>(c, N);
+        b.vx = carve<float>(c, N);
+        b.vy = carve<float>(c, N);
+        b.m = carve<float>(c, N);
+        b.xlo = carve<float>(c, N);
+        b.ylo = carve<float>(c, N);
+        b.id = carve<int>(c, N);
+    }
+    s->keys = carve<uint64_t>(c, N);
+    s->keys_alt = carve<uint64_t>(c, N);
+    s->vals = carve<uint32_t>(c, N);
+    s->vals_alt = carve<uint32_t>(c, N);
+    s->hist = carve<uint32_t>(c, (size_t)256 * s->tiles);
+    s->totals = carve<uint32_t>(c, 256);
+    s->box_ord = carve<int>(c, 4 * (size_t)nseg);
+    s->seg_off = carve<int>(c, nseg + 1);
+    s->gseg_off = carve<int>(c, nseg + 1);
+    s->seg_of_pos = carve<int>(c, N);
+    s->chunk_seg = carve<int>(c, s->nchunks);
+    s->chunk_begin = carve<int>(c, s->nchunks);
+    s->chunk_end = carve<int>(c, s->nchunks);
+    s->tree.left = carve<int>(c, N);
+    s->tree.right = carve<int>(c, N);
+    s->tree.parent = carve<int>(c, N);
+    s->tree.leaf_parent = carve<int>(c, N);
+    s->tree.split = carve<int>(c, N);
+    s->tree.first = carve<int>(c, N);
+    s->tree.last = carve<int>(c, N);
+    s->counter = carve<int>(c, N);
+    s->sums.m = carve<float>(c, N);
+    s->sums.mx = carve<float>(c, N);
+    s->sums.my = carve<float>(c, N);
+    s->sums.cx = carve<float>(c, N);
+    s->sums.cy = carve<float>(c, N);
+    s->sums.quad = carve<float4>(c, N);
+    s->rec.A = carve<float4>(c, N);
+    s->rec.B = carve<float4>(c, N);
+    s->rec.C = carve<int4>(c, N);
+    s->rec.D = carve<int2>(c, N);
+    s->ax = carve<float>(c, N);
+    s->ay = carve<float>(c, N);
+    s->status = carve<int>(c, 1);
+    s->inter = carve<unsigned long long>(c, 1);
+
+    std::vector<int> sop;
+    if (nseg > 1) {
+        sop.resize(N);
+        for (int sg = 0; sg < nseg; ++sg)
+            for (int b = s->h_off[sg]; b < s->h_off[sg + 1]; ++b) sop[b] = sg;
+    }
+    int rc = BH_OK;
+    auto up = [&](void* dst, const void* src, size_t b) {
+        if (rc == BH_OK && b) {
+            cudaError_t e2 = cudaMemcpy(dst, src, b, cudaMemcpyHostToDevice);
+            if (e2 != cudaSuccess) rc = cuda_fail(e2, "cudaMemcpy(tables)");
+        }
+    };
+    up(s->seg_off, s->h_off.data(), sizeof(int) * (nseg + 1));
+    up(s->gseg_off, goff.data(), sizeof(int) * (nseg + 1));
+    if (nseg > 1) up(s->seg_of_pos, sop.data(), sizeof(int) * N);
+    up(s->chunk_seg, cseg.data(), sizeof(int) * s->nchunks);
+    up(s->chunk_begin, cbeg.data(), sizeof(int) * s->nchunks);
+    up(s->chunk_end, cend.data(), sizeof(int) * s->nchunks);
+    if (rc == BH_OK && cudaMemset(s->status, 0, sizeof(int)) != cudaSuccess) rc = BH_ERR_CUDA;
+    if (rc == BH_OK) {
+        cudaError_t ea = init_walk_attributes();
+        if (ea != cudaSuccess) rc = cuda_fail(ea, "cudaFuncSetAttribute(walk)");
+    }
+    if (rc == BH_OK) {
+        int bref = 0, bacc = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &bref, k_walk_ref<kWalkWarps, kRefStack>, kWalkWarps * 32, 0);
+        using Sm = AccSmem<kWalkWarps, kAccStack, 16>;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &bacc, k_walk_acc<kWalkWarps, kAccStack, 16, true>, kWalkWarps * 32, sizeof(Sm));
+        s->walk_grid_ref = walk_grid_cap(s->sms, bref) * 4;
+        s->walk_grid_acc = walk_grid_cap(s->sms, bacc) * 4;
+        cudaGetLastError();
+    }
+    if (rc != BH_OK) {
+        cudaFree(s->arena);
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return BH_OK;
+}
+
+}  // namespace ssg
+
+// ------------------------------------------------------------------ C ABI
+
+extern "C" {
+
+void bh_default_params(bh_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->mode = BH_MODE_REFERENCE;
+    p->theta = 0.5f;   // kernels.cu:9
+    p->eps2 = 0.025f;  // kernels.cu:8
+    p->gravity = 1.0f;     // main.cpp:94
+    p->timestep = 0.001f;  // main.cpp:93
+    p->dampening = 1.0f;   // main.cpp:95
+    p->leaf_bucket = 0;
+    p->block_size = 0;
+    p->stack_depth = 0;
+    p->use_graph = 0;
+}
+
+int bh_create(const bh_params* p, int n, int device, bh_system** out) {
+    return ssg::system_create(p, &n, 1, device, out);
+}
+
+int bh_destroy(bh_system* s) {
+    if (!s) return BH_ERR_ARG;
+    cudaSetDevice(s->device);
+    drop_graph(s);
+    if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
+    cudaFree(s->arena);
+    delete s;
+    return BH_OK;
+}
+
+int bh_set_params(bh_system* s, const bh_params* p) {
+    if (!s || !params_ok(p)) return BH_ERR_ARG;
+    bool mode_change = p->mode != s->p.mode;
+    s->p = *p;
+    drop_graph(s);
+    if (mode_change && s->have_state) {
+        // lo words only exist in MIXED mode; start them at zero
+        CK(cudaSetDevice(s->device));
+        CK(cudaMemset(s->st[0].xlo, 0, sizeof(float) * s->n));
+        CK(cudaMemset(s->st[0].ylo, 0, sizeof(float) * s->n));
+    }
+    return BH_OK;
+}
+
+int bh_get_params(const bh_system* s, bh_params* p) {
+    if (!s || !p) return BH_ERR_ARG;
+    *p = s->p;
+    return BH_OK;
+}
+
+int bh_num_bodies(const bh_system* s) { return s ? s->n : -1; }
+
+int bh_set_state(bh_system* s, const float* x, const float* y, const float* vx, const float* vy,
+                 const float* mass, void* stream) {
+    if (!s || !x || !y || !vx || !vy || !mass) return BH_ERR_ARG;
+    CK(cudaSetDevice(s->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t b = sizeof(float) * s->n;
+    const BodyPtrs& c = s->st[0];
+    CK(cudaMemcpyAsync(c.x, x, b, cudaMemcpyDefault, st));
+    CK(cudaMemcpyAsync(c.y, y, b, cudaMemcpyDefault, st));
+    CK(cudaMemcpyAsync(c.vx, vx, b, cudaMemcpyDefault, st));
+    CK(cudaMemcpyAsync(c.vy, vy, b, cudaMemcpyDefault, st));
+    CK(cudaMemcpyAsync(c.m, mass, b, cudaMemcpyDefault, st));
+    CK(cudaMemsetAsync(c.xlo, 0, b, st));
+    CK(cudaMemsetAsync(c.ylo, 0, b, st));
+    CK(cudaMemsetAsync(s->ax, 0, b, st));
+    CK(cudaMemsetAsync(s->ay, 0, b, st));
+    CK(cudaMemsetAsync(s->status, 0, sizeof(int), st));
+    k_iota<<<(s->n + 255) / 256, 256, 0, st>>>(c.id, s->n);
+    CK(cudaGetLastError());
+    s->have_state = true;
+    return BH_OK;
+}
+
+static int scatter_out(bh_system* s, const float* a0, const float* a1, const float* a2,
+                       const float* a3, float* o0, float* o1, float* o2, float* o3,
+                       cudaStream_t st) {
+    // stage in the scratch body arrays, then one copy per requested output
+    BodyPtrs& tmp = s->st[1];
+    float* t[4] = {tmp.x, tmp.y, tmp.vx, tmp.vy};
+    const float* in[4] = {a0, a1, a2, a3};
+    float* outp[4] = {o0, o1, o2, o3};
+    k_scatter4<<<(s->n + 255) / 256, 256, 0, st>>>(
+        s->n, s->st[0].id, outp[0] ? in[0] : nullptr, outp[1] ? in[1] : nullptr,
+        outp[2] ? in[2] : nullptr, outp[3] ? in[3] : nullptr, t[0], t[1], t[2], t[3]);
+    CK(cudaGetLastError());
+    const size_t b = sizeof(float) * s->n;
+    for (int k = 0; k < 4; ++k)
+        if (outp[k]) CK(cudaMemcpyAsync(outp[k], t[k], b, cudaMemcpyDefault, st));
+    return BH_OK;
+}
+
+int bh_get_state(bh_system* s, float* x, float* y, float* vx, float* vy, float* mass,
+                 void* stream) {
+    if (!s) return BH_ERR_ARG;
+    if (!s->have_state) return BH_ERR_STATE;
+    CK(cudaSetDevice(s->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    const BodyPtrs& c = s->st[0];
+    int rc = scatter_out(s, c.x, c.y, c.vx, c.vy, x, y, vx, vy, st);
+    if (rc != BH_OK || !mass) return rc;
+    return scatter_out(s, c.m, nullptr, nullptr, nullptr, mass, nullptr, nullptr, nullptr, st);
+}
+
+int bh_get_accel(bh_system* s, float* ax, float* ay, void* stream) {
+    if (!s) return BH_ERR_ARG;
+    if (!s->have_state) return BH_ERR_STATE;
+    CK(cudaSetDevice(s->device));
+    return scatter_out(s, s->ax, s->ay, nullptr, nullptr, ax, ay, nullptr, nullptr,
+                       (cudaStream_t)stream);
+}
+
+int bh_get_positions_hilo(bh_system* s, float* xhi, float* xlo, float* yhi, float* ylo,
+                          void* stream) {
+    if (!s) return BH_ERR_ARG;
+    if (!s->have_state) return BH_ERR_STATE;
+    CK(cudaSetDevice(s->device));
+    const BodyPtrs& c = s->st[0];
+    return scatter_out(s, c.x, c.xlo, c.y, c.ylo, xhi, xlo, yhi, ylo, (cudaStream_t)stream);
+}
+
+int bh_step(bh_system* s, int steps, void* stream) {
+    if (!s || steps < 0) return BH_ERR_ARG;
+    if (!s->have_state) return BH_ERR_STATE;
+    CK(cudaSetDevice(s->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    if (s->p.use_graph) {
+        if (!s->graph_exec) {
+            // the capture stream must see the state that `stream` produced
+            cudaEvent_t ev;
+            CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            CK(cudaEventRecord(ev, st));
+            if (!s->cap_stream) CK(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
+            CK(cudaStreamWaitEvent(s->cap_stream, ev, 0));
+            cudaEventDestroy(ev);
+            int rc = build_graph(s);
+            if (rc != BH_OK) return rc;
+        }
+        for (int k = 0; k < steps; ++k) CK(cudaGraphLaunch(s->graph_exec, st));
+        return BH_OK;
+    }
+    for (int k = 0; k < steps; ++k) {
+        int rc = enqueue_step(s, st);
+        if (rc != BH_OK) return rc;
+    }
+    return BH_OK;
+}
+
+int bh_sync(bh_system* s, void* stream) {
+    if (!s) return BH_ERR_ARG;
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize((cudaStream_t)stream));
+    int bits = 0;
+    CK(cudaMemcpy(&bits, s->status, sizeof(int), cudaMemcpyDeviceToHost));
+    return status_code(bits, s->p.mode);
+}
+
+int bh_get_stats(bh_system* s, bh_stats* out, void* stream) {
+    if (!s || !out) return BH_ERR_ARG;
+    std::memset(out, 0, sizeof(*out));
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize((cudaStream_t)stream));
+    int bits = 0;
+    unsigned long long inter = 0;
+    int box[4] = {0, 0, 0, 0};
+    CK(cudaMemcpy(&bits, s->status, sizeof(int), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&inter, s->inter, sizeof(inter), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(box, s->box_ord, sizeof(box), cudaMemcpyDeviceToHost));
+    out->status = status_code(bits, s->p.mode);
+    out->interactions = (int64_t)inter;
+    for (int k = 0; k < 4; ++k) {
+        int i = box[k];
+        int b = i >= 0 ? i : (i ^ 0x7fffffff);
+        std::memcpy(&out->box[k], &b, 4);
+    }
+    // tree shape from the split levels (host pass over n ints; debugging aid)
+    std::vector<int> split(s->n), parent(s->n);
+    CK(cudaMemcpy(split.data(), s->tree.split, sizeof(int) * s->n, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(parent.data(), s->tree.parent, sizeof(int) * s->n, cudaMemcpyDeviceToHost));
+    long long cells = 0;
+    int nodes = 0, maxd = 0;
+    for (int i = 0; i < s->n; ++i) {
+        int sp = split[i];
+        if (sp < 0) continue;
+        int pa = parent[i];
+        if (pa >= 0 && (sp & 1) && split[pa] == sp - 1) continue;  // merged
+        ++nodes;
+        int L = sp >> 1;
+        int Lp = pa >= 0 ? (split[pa] >> 1) : 0;
+        // cells of the reference tree owned by this node: its chain and itself
+        cells += (pa >= 0) ? (L - Lp) : L;
+        maxd = std::max(maxd, L + 1);
+    }
+    out->cells = (int32_t)cells;
+    out->nodes = nodes;
+    out->max_depth = maxd;
+    return BH_OK;
+}
+
+int bh_get_debug(bh_system* s, const char* name, void* host_out, size_t bytes, void* stream) {
+    if (!s || !name || !host_out) return BH_ERR_ARG;
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize((cudaStream_t)stream));
+    const size_t N = (size_t)s->n;
+    const void* src = nullptr;
+    size_t need = 0;
+    std::string nm(name);
+    if (nm == "box") {
+        if (bytes < 16) return BH_ERR_ARG;
+        int box[4];
+        CK(cudaMemcpy(box, s->box_ord, sizeof(box), cudaMemcpyDeviceToHost));
+        float* f = (float*)host_out;
+        for (int k = 0; k < 4; ++k) {
+            int i = box[k];
+            int b = i >= 0 ? i : (i ^ 0x7fffffff);
+            std::memcpy(&f[k], &b, 4);
+        }
+        return BH_OK;
+    }
+    if (nm == "accel_sorted") {
+        if (bytes < 8 * N) return BH_ERR_ARG;
+        CK(cudaMemcpy(host_out, s->ax, 4 * N, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy((char*)host_out + 4 * N, s->ay, 4 * N, cudaMemcpyDeviceToHost));
+        return BH_OK;
+    }
+    if (nm == "keys") { src = s->kfinal; need = 8 * N; }
+    else if (nm == "perm") { src = s->st[0].id; need = 4 * N; }
+    else if (nm == "node_left") { src = s->tree.left; need = 4 * N; }
+    else if (nm == "node_right") { src = s->tree.right; need = 4 * N; }
+    else if (nm == "node_split") { src = s->tree.split; need = 4 * N; }
+    else if (nm == "node_first") { src = s->tree.first; need = 4 * N; }
+    else if (nm == "node_last") { src = s->tree.last; need = 4 * N; }
+    else if (nm == "node_parent") { src = s->tree.parent; need = 4 * N; }
+    else if (nm == "node_m") { src = s->sums.m; need = 4 * N; }
+    else if (nm == "node_mx") { src = s->sums.mx; need = 4 * N; }
+    else if (nm == "node_my") { src = s->sums.my; need = 4 * N; }
+    else if (nm == "node_cx") { src = s->sums.cx; need = 4 * N; }
+    else if (nm == "node_cy") { src = s->sums.cy; need = 4 * N; }
+    else return BH_ERR_ARG;
+    if (!src) return BH_ERR_STATE;
+    if (bytes < need) return BH_ERR_ARG;
+    CK(cudaMemcpy(host_out, src, need, cudaMemcpyDeviceToHost));
+    return BH_OK;
+}
+
+int bh_step_profiled(bh_system* s, void* stream, float* phase_ms) {
+    if (!s || !phase_ms) return BH_ERR_ARG;
+    if (!s->have_state) return BH_ERR_STATE;
+    CK(cudaSetDevice(s->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaEvent_t ev[BH_NUM_PHASES + 1];
+    for (auto& e : ev) CK(cudaEventCreate(&e));
+    int rc = enqueue_step(s, st, ev);
+    if (rc == BH_OK) {
+        CK(cudaEventSynchronize(ev[BH_NUM_PHASES]));
+        for (int k = 0; k < BH_NUM_PHASES; ++k) {
+            float ms = 0.0f;
+            CK(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+            phase_ms[k] += ms;
+        }
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    return rc;
+}
+
+int bh_direct_sum_f64(bh_system* s, int ns, const int* idx, double* ax, double* ay) {
+    if (!s || ns < 1 || !idx || !ax || !ay) return BH_ERR_ARG;
+    if (!s->have_state) return BH_ERR_STATE;
+    for (int k = 0; k < ns; ++k)
+        if (idx[k] < 0 || idx[k] >= s->n) return BH_ERR_ARG;
+    CK(cudaSetDevice(s->device));
+    const BodyPtrs& c = s->st[0];
+    BodyPtrs& t = s->st[1];
+    bool mixed = s->p.mode == BH_MODE_MIXED;
+    // caller-order copies in the scratch body arrays: x, y, m and the lo words
+    k_scatter4<<<(s->n + 255) / 256, 256>>>(s->n, c.id, c.x, c.y, c.m, nullptr, t.x, t.y, t.vx,
+                                             nullptr);
+    CK(cudaGetLastError());
+    if (mixed) {
+        k_scatter4<<<(s->n + 255) / 256, 256>>>(s->n, c.id, c.xlo, c.ylo, nullptr, nullptr, t.xlo,
+                                                 t.ylo, nullptr, nullptr);
+        CK(cudaGetLastError());
+    }
+    int* d_idx = nullptr;
+    double* d_part = nullptr;
+    double* d_out = nullptr;
+    CK(cudaMalloc(&d_idx, sizeof(int) * ns));
+    CK(cudaMalloc(&d_part, sizeof(double) * 2 * (size_t)ns * kDirChunks));
+    CK(cudaMalloc(&d_out, sizeof(double) * 2 * (size_t)ns));
+    CK(cudaMemcpy(d_idx, idx, sizeof(int) * ns, cudaMemcpyHostToDevice));
+    dim3 grid((ns + kDirThreads - 1) / kDirThreads, kDirChunks);
+    k_direct_partial<<<grid, kDirThreads>>>(s->n, t.x, mixed ? t.xlo : nullptr, t.y,
+                                            mixed ? t.ylo : nullptr, t.vx, ns, d_idx,
+                                            (double)s->p.eps2, d_part);
+    k_direct_reduce<<<(2 * ns + 255) / 256, 256>>>(ns, kDirChunks, d_part,
+                                                   s->p.mode == BH_MODE_REFERENCE ? 1.0 : (double)s->p.gravity,
+                                                   d_out);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpy(ax, d_out, sizeof(double) * ns, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(ay, d_out + ns, sizeof(double) * ns, cudaMemcpyDeviceToHost);
+    cudaFree(d_idx);
+    cudaFree(d_part);
+    cudaFree(d_out);
+    if (e != cudaSuccess) return cuda_fail(e, "bh_direct_sum_f64");
+    return BH_OK;
+}
+
+int bh_measure_fp32_peak(int device, double* tflops) {
+    if (!tflops) return BH_ERR_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return BH_ERR_NO_DEVICE;
+    if (device >= 0) CK(cudaSetDevice(device));
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    int sms = 0;
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    float* out = nullptr;
+    CK(cudaMalloc(&out, sizeof(float) * blocks * threads));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int rep = 0; rep < 6; ++rep) {
+        CK(cudaEventRecord(e0));
+        k_ffma_peak<<<blocks, threads>>>(out, iters, 0.999f, 1e-6f);
+        CK(cudaEventRecord(e1));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (rep > 0) best = ms < best ? ms : best;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    double flops = 2.0 * 8.0 * 16.0 * iters * (double)blocks * threads;
+    *tflops = flops / (best * 1e-3) / 1e12;
+    return BH_OK;
+}
+
+const char* bh_status_string(int st) {
+    switch (st) {
+        case BH_OK: return "ok";
+        case BH_ERR_ARG: return "invalid argument";
+        case BH_ERR_DUPLICATE_KEYS: return "two bodies share all 32 quadtree levels";
+        case BH_ERR_NONFINITE: return "non-finite position";
+        case BH_ERR_CAPACITY: return "capacity exceeded";
+        case BH_ERR_STACK: return "walk stack overflow";
+        case BH_ERR_CUDA: return "CUDA error";
+        case BH_ERR_NOMEM: return "out of memory";
+        case BH_ERR_STATE: return "call out of order";
+        case BH_ERR_NO_DEVICE: return "no suitable CUDA device";
+        default: return "unknown status";
+    }
+}
+
+const char* bh_last_error(void) { return ssg::g_last_error.c_str(); }
+
+const char* bh_version(void) { return "0.1.0 sm_103a"; }
+
+}  // extern "C"

@@ -1,0 +1,42 @@
+// Internal declarations shared by the engine's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "bh_walk.cuh"
+#include "stellar_bh.h"
+
+namespace ssg {
+
+extern thread_local std::string g_last_error;
+int cuda_fail(cudaError_t e, const char* what);
+
+// Everything the walk launch needs for one step of one batch.
+struct StepArgs {
+    int mode;
+    Segs segs;
+    Groups groups;
+    WalkIn in;
+    WalkOut out;
+    const float4* recA;
+    const float4* recB;
+    const int4* recC;
+    const int2* recD;
+    float eps2, G, dt, ddt;
+    int* status;
+    unsigned long long* inter;
+    int bucket;
+    int walk_grid_ref, walk_grid_acc;
+};
+
+cudaError_t launch_walk(const StepArgs& a, cudaStream_t st);
+cudaError_t init_walk_attributes();
+int normalized_bucket(int b);
+
+// Create a batch of independent systems of the given sizes (bh_create is the
+// single-system case).
+int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh_system** out);
+
+}  // namespace ssg

@@ -1,0 +1,117 @@
+"""PLAIN and MIXED modes on the GPU against the FP64 direct sum.
+
+Error definition (used everywhere in this repository): for a seeded sample of
+4096 bodies, rel_i = |a_i - a_i^64| / |a_i^64| with a^64 the FP64 O(N^2)
+direct sum (oracle/oracle.c) at the same softening; the RMS of rel_i must be
+<= 1e-3 at theta = 0.5 and the maximum is reported.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def bh():
+    from stellarsolver_gb300 import bh as _bh
+
+    _bh.lib()
+    return _bh
+
+
+def force_error(oracle, x, y, m, ax, ay, eps2, G=1.0, k=4096, seed=7):
+    n = len(x)
+    idx = np.sort(np.random.default_rng(seed).choice(n, size=min(k, n), replace=False))
+    rx, ry = oracle.direct_f64(x, y, m, idx, eps2, G)
+    rel = np.hypot(ax[idx] - rx, ay[idx] - ry) / np.hypot(rx, ry)
+    return float(np.sqrt(np.mean(rel ** 2))), float(rel.max())
+
+
+def run(bh, x, y, vx, vy, m, steps=1, **kw):
+    with bh.BarnesHutSystem(len(x), **kw) as s:
+        s.set_state(x, y, vx, vy, m)
+        s.step(steps)
+        s.sync()
+        ax, ay = s.get_accel()
+        st = s.get_state()
+        stats = s.stats()
+    return ax, ay, st, stats
+
+
+@pytest.mark.parametrize("mode", ["plain", "mixed"])
+@pytest.mark.parametrize("bucket", [1, 4, 8, 16])
+def test_plummer_2e17_error_bound(bh, oracle, mode, bucket):
+    from stellarsolver_gb300 import models
+
+    x, y, vx, vy, m = models.plummer(1 << 17, 0x5EED2000)
+    eps2 = 1e-4
+    ax, ay, _, stats = run(bh, x, y, vx, vy, m, mode=mode, theta=0.5, eps2=eps2, timestep=0.0,
+                           leaf_bucket=bucket)
+    rms, mx = force_error(oracle, x, y, m, ax, ay, eps2)
+    assert stats["status"] == 0
+    assert rms <= 1e-3, (rms, mx)
+    assert mx <= 5e-2, (rms, mx)
+
+
+def test_plummer_2e20_error_bound(bh, oracle):
+    from stellarsolver_gb300 import models
+
+    x, y, vx, vy, m = models.plummer(1 << 20, models.SEED_BASE + 1)
+    ax, ay, _, _ = run(bh, x, y, vx, vy, m, mode="mixed", theta=0.5, eps2=1e-4, timestep=0.0)
+    rms, mx = force_error(oracle, x, y, m, ax, ay, 1e-4)
+    assert rms <= 1e-3, (rms, mx)
+
+
+def test_disk_with_central_mass(bh, oracle):
+    from stellarsolver_gb300 import models
+
+    x, y, vx, vy, m = models.disk(1 << 15, models.SEED_BASE)
+    ax, ay, _, _ = run(bh, x, y, vx, vy, m, mode="plain", theta=0.5, eps2=0.01, timestep=0.0)
+    rms, mx = force_error(oracle, x, y, m, ax, ay, 0.01)
+    assert rms <= 1e-3, (rms, mx)
+
+
+def test_gravity_scales_forces(bh):
+    from stellarsolver_gb300 import models
+
+    x, y, vx, vy, m = models.plummer(1 << 12, 5)
+    a1 = run(bh, x, y, vx, vy, m, mode="plain", gravity=1.0, eps2=1e-4, timestep=0.0)[:2]
+    a2 = run(bh, x, y, vx, vy, m, mode="plain", gravity=2.5, eps2=1e-4, timestep=0.0)[:2]
+    assert np.allclose(a2[0], 2.5 * a1[0], rtol=1e-6, atol=0)
+
+
+def test_mixed_positions_do_not_drift(bh):
+    """G = 0: bodies move on straight lines; hi/lo positions follow the exact
+    FP64 drift x0 + k*dt*v far more closely than single floats."""
+    n = 4096
+    rng = np.random.default_rng(3)
+    x = rng.uniform(0.5, 2.0, n).astype(np.float32)
+    y = rng.uniform(0.5, 2.0, n).astype(np.float32)
+    vx = rng.uniform(-1, 1, n).astype(np.float32)
+    vy = rng.uniform(-1, 1, n).astype(np.float32)
+    m = np.ones(n, np.float32)
+    steps, dt = 200, 1e-5
+    inc = (np.float32(dt) * vx).astype(np.float32)  # the per-step float increment d*dt*v
+    exact = x.astype(np.float64) + steps * inc.astype(np.float64)
+    errs = {}
+    for mode in ("plain", "mixed"):
+        with bh.BarnesHutSystem(n, mode=mode, gravity=0.0, eps2=1e-4, timestep=dt) as s:
+            s.set_state(x, y, vx, vy, m)
+            s.step(steps)
+            s.sync()
+            xh, xl, _, _ = s.get_positions_hilo()
+        errs[mode] = np.abs(xh.astype(np.float64) + xl - exact).max()
+    assert errs["mixed"] < 1e-3 * errs["plain"], errs
+    assert errs["mixed"] < 1e-10, errs
+
+
+def test_momentum_nearly_conserved(bh):
+    from stellarsolver_gb300 import models
+
+    x, y, vx, vy, m = models.plummer(1 << 14, 11)
+    p0 = np.array([np.sum(m * vx, dtype=np.float64), np.sum(m * vy, dtype=np.float64)])
+    _, _, st, _ = run(bh, x, y, vx, vy, m, steps=20, mode="mixed", eps2=1e-4, timestep=1e-4)
+    p1 = np.array([np.sum(st["m"] * st["vx"], dtype=np.float64),
+                   np.sum(st["m"] * st["vy"], dtype=np.float64)])
+    scale = np.sum(m * np.hypot(vx, vy), dtype=np.float64)
+    assert np.abs(p1 - p0).max() <= 1e-4 * scale
