@@ -42,8 +42,11 @@ extern "C" {
  *   (w^2/theta) <= |d|^2 + eps2 (kernels.cu:395-406), root children always
  *   opened, G not applied (kernels.cu:340: `g` unused), Euler-Cromer update
  *   v += dt*a; x += (d*dt)*v (kernels.cu:529-533).
- * PLAIN: accuracy mode in FP32: quadrupole moments, group opening test
- *   dist(COM, group box) > bmax/theta, leaf buckets, G applied.
+ * PLAIN: accuracy mode in FP32: quadrupole moments; a node is approximated
+ *   iff min over the group's bodies |COM - p| > l/theta + |COM - cell centre|
+ *   (l = larger cell side) and G M l^3 / d^5 <= alpha |a_old| (previous
+ *   step's |a|; the first step after bh_set_state bootstraps it with a
+ *   geometric-only pass); leaf buckets; G applied.
  * MIXED: PLAIN plus compensated (Kahan) force sums and positions kept as
  *   hi + lo float pairs. */
 #define BH_MODE_REFERENCE 0
@@ -63,6 +66,9 @@ typedef struct bh_params {
     int block_size;    /* walk threads per block; 0 = tuned default */
     int stack_depth;   /* walk stack entries per warp; 0 = tuned default */
     int use_graph;     /* 1 = replay the step as a CUDA graph */
+    float alpha;       /* PLAIN/MIXED relative opening tolerance: a cell of mass M and size l
+                          at distance d is approximated only if G M l^3 / d^5 <= alpha |a_old|
+                          (Springel 2005-style); 0 = geometric rule only; default 0.01 */
 } bh_params;
 
 typedef struct bh_system bh_system;
@@ -98,6 +104,12 @@ int bh_num_bodies(const bh_system* s); /* getNumParticles() (BarnesHutParticleSy
  * start at zero. */
 int bh_set_state(bh_system* s, const float* x, const float* y, const float* vx,
                  const float* vy, const float* mass, void* stream);
+
+/* Accelerations of the state just loaded by bh_set_state (caller's order,
+ * host or device pointers), like the reference's reset() upload of d_ax/d_ay
+ * (BarnesHutParticleSystem.cpp:370-371).  PLAIN/MIXED use |a| as the scale of
+ * the relative opening rule, so the next step skips the bootstrap pass. */
+int bh_set_accel(bh_system* s, const float* ax, const float* ay, void* stream);
 
 /* Copy the current state out in the caller's order (any of the pointers may be
  * NULL to skip it).  For MIXED mode x/y are hi+lo rounded to float. */

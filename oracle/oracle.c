@@ -501,3 +501,182 @@ void orc_energy_f64(int n, const float* x, const float* y, const float* vx, cons
     out[2] = px;
     out[3] = py;
 }
+
+/* ------------------------------------------------------------------------
+ * CPU restatement of the engine's PLAIN-mode walk (no reference counterpart:
+ * the reference has one monopole walk).  Checks the GPU walk and its opening
+ * rule against the FP64 direct sum.  Per group of 32 consecutive sorted
+ * bodies, a node is approximated by its quadrupole expansion iff
+ *   geometric: min_j |COM - p_j| > l/theta + |COM - cell centre|
+ *              (l = larger side of the node's cell), and
+ *   relative : G M l^3 <= alpha * a_g * d^5, d = that minimum distance,
+ *              a_g = max(min_j |a_old_j|, 0.1 * mean_j |a_old_j|)
+ *              (skipped when aold == NULL or alpha <= 0);
+ * otherwise a node of <= bucket bodies interacts body by body and a larger
+ * node is opened.  Float arithmetic, as on the GPU.
+ * ---------------------------------------------------------------------- */
+typedef struct {
+    float m, cx, cy, sxx, sxy, syy;
+} Mom;
+
+static void acc_moments(int id, const int32_t* left, const int32_t* right, const float* sx,
+                        const float* sy, const float* sm, Mom* out) {
+    Mom c[2];
+    int32_t ch[2] = {left[id], right[id]};
+    for (int s = 0; s < 2; ++s) {
+        if (ch[s] < 0) {
+            int b = ~ch[s];
+            c[s].m = sm[b];
+            c[s].cx = sx[b];
+            c[s].cy = sy[b];
+            c[s].sxx = c[s].sxy = c[s].syy = 0.0f;
+        } else {
+            acc_moments(ch[s], left, right, sx, sy, sm, out);
+            c[s] = out[ch[s]];
+        }
+    }
+    Mom r;
+    r.m = c[0].m + c[1].m;
+    float w = r.m > 0.0f ? c[1].m / r.m : 0.5f;
+    r.cx = w * (c[1].cx - c[0].cx) + c[0].cx;
+    r.cy = w * (c[1].cy - c[0].cy) + c[0].cy;
+    float ax = c[0].cx - r.cx, ay = c[0].cy - r.cy, bx = c[1].cx - r.cx, by = c[1].cy - r.cy;
+    r.sxx = c[0].sxx + c[1].sxx + c[0].m * ax * ax + c[1].m * bx * bx;
+    r.sxy = c[0].sxy + c[1].sxy + c[0].m * ax * ay + c[1].m * bx * by;
+    r.syy = c[0].syy + c[1].syy + c[0].m * ay * ay + c[1].m * by * by;
+    out[id] = r;
+}
+
+static void p2p_cpu(float bx, float by, float bm, float px, float py, float eps2, float* ax,
+                    float* ay) {
+    float dx = bx - px, dy = by - py;
+    float u = dx * dx + dy * dy + eps2;
+    float ri = u > 0.0f ? 1.0f / sqrtf(u) : 0.0f;
+    float f = bm * ri * ri * ri;
+    *ax += f * dx;
+    *ay += f * dy;
+}
+
+int64_t orc_walk_acc(int n, const float* sx, const float* sy, const float* sm,
+                     const uint64_t* skeys, const int32_t* left, const int32_t* right,
+                     const int32_t* split, const int32_t* first, const int32_t* last,
+                     const int32_t* qchild, const float* box, float theta, float eps2, float G,
+                     int bucket, float alpha, const float* aold, float* sax, float* say) {
+    if (n < 2) {
+        for (int i = 0; i < n; ++i) sax[i] = say[i] = 0.0f;
+        return 0;
+    }
+    Mom* mom = (Mom*)malloc(sizeof(Mom) * (size_t)(n - 1));
+    acc_moments(0, left, right, sx, sy, sm, mom);
+    float* ropen2 = (float*)malloc(sizeof(float) * (size_t)(n - 1));
+    float* qerr = (float*)malloc(sizeof(float) * (size_t)(n - 1));
+    for (int i = 0; i < n - 1; ++i) {
+        int L = split[i] >> 1;
+        if (L > 32) L = 32;
+        uint64_t pre = L > 0 ? skeys[first[i]] >> (64 - 2 * L) : 0;
+        unsigned long long ix = 0, iy = 0;
+        for (int q = L - 1; q >= 0; --q) {
+            unsigned d = (unsigned)(pre >> (2 * q)) & 3u;
+            ix = (ix << 1) | ((d & 1u) ? 0ull : 1ull);
+            iy = (iy << 1) | ((d & 2u) ? 0ull : 1ull);
+        }
+        double wx = (double)box[1] - box[0], wy = (double)box[3] - box[2];
+        double sc = ldexp(1.0, -L);
+        double x0 = box[0] + wx * sc * (double)ix, y0 = box[2] + wy * sc * (double)iy;
+        double l = fmax(wx, wy) * sc;
+        double dx = mom[i].cx - (x0 + 0.5 * wx * sc), dy = mom[i].cy - (y0 + 0.5 * wy * sc);
+        double r = l / theta + sqrt(dx * dx + dy * dy);
+        ropen2[i] = (float)(r * r);
+        qerr[i] = (float)((double)G * mom[i].m * l * l * l);
+    }
+    const int relative = aold != NULL && alpha > 0.0f;
+    int groups = (n + 31) / 32;
+    int64_t total = 0;
+#pragma omp parallel reduction(+ : total)
+    {
+        int cap = 4096;
+        int32_t* stack = (int32_t*)malloc(sizeof(int32_t) * (size_t)cap);
+#pragma omp for schedule(dynamic, 4)
+        for (int g = 0; g < groups; ++g) {
+            int g0 = 32 * g, cnt = n - g0 < 32 ? n - g0 : 32;
+            float px[32], py[32], ax[32], ay[32];
+            float aa = INFINITY;
+            if (relative) {
+                float amin = INFINITY, amean = 0.0f;
+                for (int k = 0; k < cnt; ++k) {
+                    amin = fminf(amin, aold[g0 + k]);
+                    amean += aold[g0 + k];
+                }
+                amean /= (float)cnt;
+                aa = alpha * fmaxf(amin, 0.1f * amean);
+            }
+            for (int k = 0; k < cnt; ++k) {
+                px[k] = sx[g0 + k];
+                py[k] = sy[g0 + k];
+                ax[k] = ay[k] = 0.0f;
+            }
+            int64_t entries = 0;
+            int top = 0;
+            stack[top++] = 0;
+            while (top > 0) {
+                int32_t node = stack[--top];
+                float cx = mom[node].cx, cy = mom[node].cy;
+                float d2 = INFINITY;
+                for (int k = 0; k < cnt; ++k) {
+                    float dx = px[k] - cx, dy = py[k] - cy;
+                    float q = dx * dx + dy * dy;
+                    d2 = q < d2 ? q : d2;
+                }
+                int accept = d2 > ropen2[node];
+                if (accept && relative) accept = qerr[node] <= aa * d2 * d2 * sqrtf(d2);
+                if (accept) {
+                    const Mom* M = &mom[node];
+                    float T0 = 3.0f * M->sxx, T1 = 3.0f * M->sxy, T2 = 3.0f * M->syy;
+                    float h = 1.5f * (M->sxx + M->syy);
+                    for (int k = 0; k < cnt; ++k) {
+                        float dx = cx - px[k], dy = cy - py[k];
+                        float u = dx * dx + dy * dy + eps2;
+                        float ri = 1.0f / sqrtf(u), r2 = ri * ri, r3 = ri * r2;
+                        float tdx = T0 * dx + T1 * dy, tdy = T1 * dx + T2 * dy;
+                        float dtd = dx * tdx + dy * tdy;
+                        float coef = M->m + r2 * (2.5f * dtd * r2 - h);
+                        ax[k] += r3 * (coef * dx - r2 * tdx);
+                        ay[k] += r3 * (coef * dy - r2 * tdy);
+                    }
+                    entries += 1;
+                } else if (last[node] - first[node] + 1 <= bucket) {
+                    for (int b = first[node]; b <= last[node]; ++b) {
+                        for (int k = 0; k < cnt; ++k) p2p_cpu(sx[b], sy[b], sm[b], px[k], py[k], eps2, &ax[k], &ay[k]);
+                        entries += 1;
+                    }
+                } else {
+                    for (int s = 0; s < 4; ++s) {
+                        int32_t c = qchild[4 * (size_t)node + s];
+                        if (c == INT32_MIN) continue;
+                        if (c >= 0) {
+                            if (top == cap) {
+                                cap *= 2;
+                                stack = (int32_t*)realloc(stack, sizeof(int32_t) * (size_t)cap);
+                            }
+                            stack[top++] = c;
+                        } else {
+                            int b = ~c;
+                            for (int k = 0; k < cnt; ++k) p2p_cpu(sx[b], sy[b], sm[b], px[k], py[k], eps2, &ax[k], &ay[k]);
+                            entries += 1;
+                        }
+                    }
+                }
+            }
+            for (int k = 0; k < cnt; ++k) {
+                sax[g0 + k] = G * ax[k];
+                say[g0 + k] = G * ay[k];
+            }
+            total += entries * cnt;
+        }
+        free(stack);
+    }
+    free(mom);
+    free(ropen2);
+    free(qerr);
+    return total;
+}

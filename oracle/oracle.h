@@ -95,6 +95,16 @@ void orc_direct_f64_hilo(int n, const float* xh, const float* xl, const float* y
 void orc_energy_f64(int n, const float* x, const float* y, const float* vx, const float* vy,
                     const float* m, double eps2, double G, double* out);
 
+/* CPU restatement of the engine's PLAIN-mode group walk: quadrupoles, leaf
+ * buckets, geometric + relative opening rule (see oracle.c; aold = |a| of the
+ * previous step in sorted order, NULL for the geometric-only bootstrap pass).
+ * Output in sorted order; returns the interaction count. */
+int64_t orc_walk_acc(int n, const float* sx, const float* sy, const float* sm,
+                     const uint64_t* skeys, const int32_t* left, const int32_t* right,
+                     const int32_t* split, const int32_t* first, const int32_t* last,
+                     const int32_t* qchild, const float* box, float theta, float eps2, float G,
+                     int bucket, float alpha, const float* aold, float* sax, float* say);
+
 int orc_num_threads(void);
 
 #ifdef __cplusplus

@@ -39,7 +39,7 @@ class Params(ctypes.Structure):
                 ("gravity", ctypes.c_float), ("timestep", ctypes.c_float),
                 ("dampening", ctypes.c_float), ("leaf_bucket", ctypes.c_int),
                 ("block_size", ctypes.c_int), ("stack_depth", ctypes.c_int),
-                ("use_graph", ctypes.c_int)]
+                ("use_graph", ctypes.c_int), ("alpha", ctypes.c_float)]
 
 
 class Stats(ctypes.Structure):
@@ -75,6 +75,7 @@ def lib() -> ctypes.CDLL:
     L.bh_num_bodies.argtypes = [vp]
     L.bh_set_state.argtypes = [vp] + [vp] * 5 + [vp]
     L.bh_get_state.argtypes = [vp] + [vp] * 5 + [vp]
+    L.bh_set_accel.argtypes = [vp, vp, vp, vp]
     L.bh_get_accel.argtypes = [vp, vp, vp, vp]
     L.bh_get_positions_hilo.argtypes = [vp, vp, vp, vp, vp, vp]
     L.bh_step.argtypes = [vp, i32, vp]
@@ -125,7 +126,7 @@ def measure_fp32_peak(device: int = -1) -> float:
 
 def make_params(mode="reference", theta=0.5, eps2=0.025, gravity=1.0, timestep=1e-3,
                 dampening=1.0, leaf_bucket=0, use_graph=False, stack_depth=0,
-                block_size=0) -> Params:
+                block_size=0, alpha=0.01) -> Params:
     p = Params()
     lib().bh_default_params(ctypes.byref(p))
     p.mode = MODES[mode] if isinstance(mode, str) else int(mode)
@@ -133,6 +134,7 @@ def make_params(mode="reference", theta=0.5, eps2=0.025, gravity=1.0, timestep=1
     p.timestep, p.dampening = timestep, dampening
     p.leaf_bucket, p.use_graph = int(leaf_bucket), int(bool(use_graph))
     p.stack_depth, p.block_size = int(stack_depth), int(block_size)
+    p.alpha = alpha
     return p
 
 
@@ -181,6 +183,12 @@ class BarnesHutSystem:
             if a.shape != (self.n,):
                 raise ValueError(f"expected arrays of shape ({self.n},), got {a.shape}")
         _check(lib().bh_set_state(self._h, *[_p(a) for a in arrs], stream), "bh_set_state")
+        self.sync(stream)
+
+    def set_accel(self, ax, ay, stream=None):
+        """Accelerations of the state just set (skips the bootstrap pass)."""
+        ax, ay = _f32(ax), _f32(ay)
+        _check(lib().bh_set_accel(self._h, _p(ax), _p(ay), stream), "bh_set_accel")
         self.sync(stream)
 
     def set_state_ptrs(self, x, y, vx, vy, m, stream=None):

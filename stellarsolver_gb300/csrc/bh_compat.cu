@@ -1,0 +1,755 @@
+// The reference's nine launch wrappers (Particle_cuda.cuh:5-13) on the
+// reference's own array layout, implemented with this library's kernels.
+//
+// BuildQuadTree sorts quadrant keys and builds the radix tree of
+// bh_device.cuh, then writes it out in the reference layout: cells numbered
+// from n in node order, a chain of single-child cells above every branching
+// cell (the reference's tree is uncompressed, kernels.cu:197-252), child slots
+// by quadrant digit, cell x/y/mass = sum(m*x), sum(m*y), sum(m) and count.
+// SortParticles fills sorted[]/start[] by a level-by-level pass in one block;
+// CalculateForces is the warp-vote walk over child[] (kernels.cu:340-435).
+// Scratch buffers (keys, sort, tree, frontier queues) are kept per device and
+// grown on demand.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "Particle_cuda.cuh"
+#include "bh_compat.h"
+#include "bh_device.cuh"
+#include "bh_engine.h"
+#include "stellar_bh.h"
+
+using namespace ssg;
+
+namespace {
+
+struct CompatSettings {
+    float theta = 0.5f;   // kernels.cu:9
+    float eps2 = 0.025f;  // kernels.cu:8
+    cudaStream_t stream = nullptr;
+};
+CompatSettings g_set;
+thread_local int t_status = BH_OK;
+
+void record(int st) {
+    if (t_status == BH_OK && st != BH_OK) t_status = st;
+}
+void record_cuda(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) record(cuda_fail(e, what));
+}
+
+// ------------------------------------------------------------------ workspace
+
+struct Workspace {
+    int device = -1;
+    size_t cap = 0;  // bodies
+    size_t mcap = 0;  // nodes (m) for the frontier queues
+    void* base = nullptr;
+    uint64_t *keys, *keys_alt;
+    uint32_t *vals, *vals_alt;
+    uint32_t *hist, *totals;
+    int tiles;
+    int* box_ord;
+    int* seg_off;
+    TreePtrs tree;
+    int* counter;
+    NodeSums sums;
+    float *sx, *sy, *sm;
+    int *ncell, *cbase, *bsum, *total;
+    int *qa, *qb;
+    int* status;
+    // last reference layout seen: lets CalculateForces bound-check child[]
+    const int* child_ptr = nullptr;
+    int child_m = 0;
+};
+std::mutex g_ws_mu;
+std::vector<Workspace> g_ws;
+
+size_t al(size_t b) { return (b + 255) & ~size_t(255); }
+
+Workspace* workspace(size_t n, size_t m) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> lk(g_ws_mu);
+    for (auto& w : g_ws)
+        if (w.device == dev && w.cap >= n && w.mcap >= m) return &w;
+    Workspace* w = nullptr;
+    for (auto& x : g_ws)
+        if (x.device == dev) w = &x;
+    if (!w) {
+        g_ws.emplace_back();
+        w = &g_ws.back();
+        w->device = dev;
+    }
+    if (w->base) cudaFree(w->base);
+    w->base = nullptr;
+    size_t N = std::max(n, w->cap), M = std::max(m, w->mcap);
+    int tiles = (int)((N + kSortTile - 1) / kSortTile);
+    int nb = (int)((N + 1023) / 1024);
+    size_t bytes = 2 * al(8 * N) + 2 * al(4 * N) + al(4 * 256 * (size_t)tiles) + al(4 * 256) +
+                   al(16) + al(8) + 8 * al(4 * N) + 5 * al(4 * N) + al(16 * N) + 3 * al(4 * N) +
+                   2 * al(4 * N) + al(4 * (size_t)nb) + al(4) + 2 * al(4 * M) + al(4);
+    if (cudaMalloc(&w->base, bytes) != cudaSuccess) {
+        w->base = nullptr;
+        w->cap = w->mcap = 0;
+        return nullptr;
+    }
+    char* c = (char*)w->base;
+    auto take = [&](size_t b) {
+        void* p = c;
+        c += al(b);
+        return p;
+    };
+    w->keys = (uint64_t*)take(8 * N);
+    w->keys_alt = (uint64_t*)take(8 * N);
+    w->vals = (uint32_t*)take(4 * N);
+    w->vals_alt = (uint32_t*)take(4 * N);
+    w->hist = (uint32_t*)take(4 * 256 * (size_t)tiles);
+    w->totals = (uint32_t*)take(4 * 256);
+    w->box_ord = (int*)take(16);
+    w->seg_off = (int*)take(8);
+    w->tree.left = (int*)take(4 * N);
+    w->tree.right = (int*)take(4 * N);
+    w->tree.parent = (int*)take(4 * N);
+    w->tree.leaf_parent = (int*)take(4 * N);
+    w->tree.split = (int*)take(4 * N);
+    w->tree.first = (int*)take(4 * N);
+    w->tree.last = (int*)take(4 * N);
+    w->counter = (int*)take(4 * N);
+    w->sums.m = (float*)take(4 * N);
+    w->sums.mx = (float*)take(4 * N);
+    w->sums.my = (float*)take(4 * N);
+    w->sums.cx = (float*)take(4 * N);
+    w->sums.cy = (float*)take(4 * N);
+    w->sums.quad = (float4*)take(16 * N);
+    w->sx = (float*)take(4 * N);
+    w->sy = (float*)take(4 * N);
+    w->sm = (float*)take(4 * N);
+    w->ncell = (int*)take(4 * N);
+    w->cbase = (int*)take(4 * N);
+    w->bsum = (int*)take(4 * (size_t)nb);
+    w->total = (int*)take(4);
+    w->qa = (int*)take(4 * M);
+    w->qb = (int*)take(4 * M);
+    w->status = (int*)take(4);
+    w->tiles = tiles;
+    w->cap = N;
+    w->mcap = M;
+    if (cudaMemset(w->status, 0, 4) != cudaSuccess) return nullptr;
+    return w;
+}
+
+int blocks_for(long long n, int t) { return (int)std::max<long long>(1, (n + t - 1) / t); }
+
+// ------------------------------------------------------------------ simple kernels
+
+__global__ void k_c_setdraw(float* ptr, const float* x, const float* y, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        ptr[2 * i] = x[i];
+        ptr[2 * i + 1] = y[i];
+    }
+}
+
+__global__ void k_c_reset(int* mutex, float* x, float* y, float* mass, int* count, int* start,
+                          int* sorted, int* child, int* index, float* left, float* right,
+                          float* bottom, float* top, int n, int m) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < m) {
+        child[4 * i] = -1;  // caller's pointer: no alignment assumed
+        child[4 * i + 1] = -1;
+        child[4 * i + 2] = -1;
+        child[4 * i + 3] = -1;
+        if (i < n) {
+            count[i] = 1;
+        } else {
+            x[i] = 0.0f;
+            y[i] = 0.0f;
+            mass[i] = 0.0f;
+            count[i] = 0;
+        }
+        start[i] = -1;
+        sorted[i] = 0;
+    }
+    if (i == 0) {
+        *mutex = 0;
+        *index = n;
+        *left = 0.0f;
+        *right = 0.0f;
+        *bottom = 0.0f;
+        *top = 0.0f;
+    }
+}
+
+__device__ __forceinline__ void atomic_min_f(float* a, float v) {
+    if (v >= 0.0f)
+        atomicMin(reinterpret_cast<int*>(a), __float_as_int(v));
+    else
+        atomicMax(reinterpret_cast<unsigned*>(a), __float_as_uint(v));
+}
+__device__ __forceinline__ void atomic_max_f(float* a, float v) {
+    if (v >= 0.0f)
+        atomicMax(reinterpret_cast<int*>(a), __float_as_int(v));
+    else
+        atomicMin(reinterpret_cast<unsigned*>(a), __float_as_uint(v));
+}
+
+__global__ void __launch_bounds__(256) k_c_bbox(const float* x, const float* y, int n, float* left,
+                                                float* right, float* bottom, float* top,
+                                                int* status) {
+    float l = x[0], r = x[0], b = y[0], t = y[0];
+    bool bad = false;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float xv = x[i], yv = y[i];
+        bad |= !isfinite(xv) || !isfinite(yv);
+        l = fminf(l, xv);
+        r = fmaxf(r, xv);
+        b = fminf(b, yv);
+        t = fmaxf(t, yv);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        l = fminf(l, __shfl_xor_sync(kFull, l, o));
+        r = fmaxf(r, __shfl_xor_sync(kFull, r, o));
+        b = fminf(b, __shfl_xor_sync(kFull, b, o));
+        t = fmaxf(t, __shfl_xor_sync(kFull, t, o));
+    }
+    __shared__ float s[4][8];
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+        s[0][w] = l;
+        s[1][w] = r;
+        s[2][w] = b;
+        s[3][w] = t;
+    }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(status, ST_NONFINITE);
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < 8; ++k) {
+            l = fminf(l, s[0][k]);
+            r = fmaxf(r, s[1][k]);
+            b = fminf(b, s[2][k]);
+            t = fmaxf(t, s[3][k]);
+        }
+        l = fminf(l, s[0][0]);
+        r = fmaxf(r, s[1][0]);
+        b = fminf(b, s[2][0]);
+        t = fmaxf(t, s[3][0]);
+        // merged into the caller's values, which ResetArrays set to 0 (kernels.cu:108-111)
+        atomic_min_f(left, l);
+        atomic_max_f(right, r);
+        atomic_min_f(bottom, b);
+        atomic_max_f(top, t);
+    }
+}
+
+__global__ void k_c_box_to_ord(const float* left, const float* right, const float* bottom,
+                               const float* top, int* box_ord, int* seg_off, int n) {
+    box_ord[0] = f2ord(*left);
+    box_ord[1] = f2ord(*right);
+    box_ord[2] = f2ord(*bottom);
+    box_ord[3] = f2ord(*top);
+    seg_off[0] = 0;
+    seg_off[1] = n;
+}
+
+__global__ void k_c_gather3(int n, const uint32_t* perm, const float* x, const float* y,
+                            const float* m, float* sx, float* sy, float* sm) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) {
+        uint32_t i = perm[j];
+        sx[j] = x[i];
+        sy[j] = y[i];
+        sm[j] = m[i];
+    }
+}
+
+// cells of the reference tree owned by each branching node: its chain of
+// single-child cells and itself (the root node owns levels 1..L)
+__global__ void k_c_ncells(int n, const int* split, const int* parent, int* ncell) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    int sp = split[q], c = 0;
+    if (sp >= 0) {
+        int pa = parent[q];
+        if (!(pa >= 0 && merged_into(sp, split[pa]))) {
+            int L = sp >> 1;
+            c = pa >= 0 ? L - (split[pa] >> 1) : L;
+        }
+    }
+    ncell[q] = c;
+}
+
+// exclusive scan of n ints in blocks of 1024
+__global__ void __launch_bounds__(1024) k_c_scan_block(const int* in, int* out, int* bsum, int n) {
+    __shared__ uint32_t tmp[32];
+    int i = blockIdx.x * 1024 + threadIdx.x;
+    uint32_t v = i < n ? (uint32_t)in[i] : 0u;
+    uint32_t tot;
+    uint32_t ex = block_excl_scan<1024>(v, &tot, tmp);
+    if (i < n) out[i] = (int)ex;
+    if (threadIdx.x == 0) bsum[blockIdx.x] = (int)tot;
+}
+
+__global__ void __launch_bounds__(1024) k_c_scan_top(int* bsum, int nb, int* total) {
+    __shared__ uint32_t tmp[32];
+    uint32_t run = 0;
+    for (int base = 0; base < nb; base += 1024) {
+        int i = base + threadIdx.x;
+        uint32_t v = i < nb ? (uint32_t)bsum[i] : 0u;
+        uint32_t tot;
+        uint32_t ex = block_excl_scan<1024>(v, &tot, tmp);
+        if (i < nb) bsum[i] = (int)(run + ex);
+        run += tot;
+    }
+    if (threadIdx.x == 0) *total = (int)run;
+}
+
+__global__ void k_c_scan_add(int* out, const int* bsum, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] += bsum[i / 1024];
+}
+
+__device__ __forceinline__ int digit_at(uint64_t key, int level) {  // level 1..32
+    return (int)((key >> (64 - 2 * level)) & 3ull);
+}
+
+__global__ void k_c_materialize(int n, int m, TreePtrs t, const uint64_t* skeys,
+                                const uint32_t* perm, const int* cbase, const int* total,
+                                NodeSums sums, int* child, int* count, int* start, float* x,
+                                float* y, float* mass, int* index, int* status) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const int tot = *total;
+    if ((long long)n + tot > (long long)m) {
+        if (q == 0) atomicOr(status, ST_CAPACITY);
+        return;
+    }
+    if (q == 0) *index = n + tot;
+    int sp = t.split[q];
+    if (sp < 0) return;
+    int pa = t.parent[q];
+    if (pa >= 0 && merged_into(sp, t.split[pa])) return;
+    int L = sp >> 1;
+    if (L >= 32) {  // equal keys: no 33rd level to place them on
+        atomicOr(status, ST_DUP);
+        return;
+    }
+    int Lp = pa >= 0 ? (t.split[pa] >> 1) : 0;
+    int nc = L - Lp;
+    int b0 = n + cbase[q];
+    uint64_t key = skeys[t.first[q]];
+    int cnt = t.last[q] - t.first[q] + 1;
+    float M = sums.m[q], MX = sums.mx[q], MY = sums.my[q];
+    for (int k = 0; k < nc; ++k) {  // chain cells, then the node's own cell
+        int id = b0 + k;
+        int lev = Lp + 1 + k;
+        if (k + 1 < nc) child[4 * id + digit_at(key, lev + 1)] = id + 1;
+        count[id] = cnt;
+        start[id] = -1;
+        x[id] = MX;
+        y[id] = MY;
+        mass[id] = M;
+    }
+    if (pa < 0 && L >= 1) child[digit_at(key, 1)] = b0;  // root slot -> top of the chain
+    const int own = nc > 0 ? b0 + nc - 1 : 0;
+    int lr[2] = {t.left[q], t.right[q]};
+    for (int s = 0; s < 2; ++s) {
+        int c = lr[s];
+        int cs[2] = {c, kNoChild};
+        if (c >= 0 && merged_into(t.split[c], sp)) {
+            cs[0] = t.left[c];
+            cs[1] = t.right[c];
+        }
+        for (int u = 0; u < 2; ++u) {
+            int cc = cs[u];
+            if (cc == kNoChild) continue;
+            if (cc < 0) {
+                int b = ~cc;
+                child[4 * own + digit_at(skeys[b], L + 1)] = (int)perm[b];
+            } else {
+                child[4 * own + digit_at(skeys[t.first[cc]], L + 1)] = n + cbase[cc];
+            }
+        }
+    }
+}
+
+__global__ void k_c_com(float* x, float* y, const float* mass, const int* index, int n) {
+    int end = *index;
+    for (int i = n + blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
+        x[i] = __fdiv_rn(x[i], mass[i]);  // kernels.cu:283-284
+        y[i] = __fdiv_rn(y[i], mass[i]);
+    }
+}
+
+// sorted[]/start[] by levels from the root slot, one block (kernels.cu:292-336)
+__global__ void __launch_bounds__(1024) k_c_sort(const int* count, int* start, int* sorted,
+                                                 const int* child, int n, int mlimit, int* qa,
+                                                 int* qb, int cap, int* status) {
+    __shared__ int s_in, s_out, s_bad;
+    if (threadIdx.x == 0) {
+        int s = 0, k = 0;
+        s_bad = 0;
+        for (int i = 0; i < 4; ++i) {
+            int node = child[i];
+            if (node >= n) {
+                if (node >= mlimit || k >= cap) {
+                    s_bad = 1;
+                    continue;
+                }
+                start[node] = s;
+                s += count[node];
+                qa[k++] = node;
+            } else if (node >= 0) {
+                if (s < n) sorted[s] = node;
+                ++s;
+            }
+        }
+        s_in = k;
+    }
+    __syncthreads();
+    int* in = qa;
+    int* out = qb;
+    int level = 0;
+    for (; level < 128; ++level) {
+        const int cin = s_in;
+        if (cin == 0) break;
+        if (threadIdx.x == 0) s_out = 0;
+        __syncthreads();
+        for (int tt = threadIdx.x; tt < cin; tt += blockDim.x) {
+            int cell = in[tt];
+            int s = start[cell];
+            for (int i = 0; i < 4; ++i) {
+                int node = child[4 * cell + i];
+                if (node >= n) {
+                    if (node >= mlimit) {
+                        s_bad = 1;
+                        continue;
+                    }
+                    start[node] = s;
+                    s += count[node];
+                    int pos = atomicAdd(&s_out, 1);
+                    if (pos < cap)
+                        out[pos] = node;
+                    else
+                        s_bad = 1;
+                } else if (node >= 0) {
+                    if (s >= 0 && s < n)
+                        sorted[s] = node;
+                    else
+                        s_bad = 1;
+                    ++s;
+                }
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) s_in = min(s_out, cap);
+        int* tmp = in;
+        in = out;
+        out = tmp;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && (s_bad || level == 128)) atomicOr(status, ST_CAPACITY);
+}
+
+// warp-vote walk on the reference layout (kernels.cu:340-435)
+template <int WARPS, int STACK>
+__global__ void __launch_bounds__(WARPS * 32) k_c_forces(
+    const float* __restrict__ x, const float* __restrict__ y, const float* __restrict__ mass,
+    const int* __restrict__ sorted, const int* __restrict__ child, const float* left,
+    const float* right, int n, int mlimit, float theta, float eps2, float* ax, float* ay,
+    int* status) {
+    __shared__ int s_node[WARPS][STACK];
+    __shared__ float s_dp[WARPS][STACK];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const float radius = __fmul_rn(__fsub_rn(*right, *left), 0.5f);  // kernels.cu:349
+    const float dp1 = __fdiv_rn(__fmul_rn(radius, radius), theta);    // :376
+    const int groups = (n + 31) / 32;
+    for (int g = blockIdx.x * WARPS + w; g < groups; g += gridDim.x * WARPS) {
+        const int j = 32 * g + lane;
+        const bool valid = j < n;
+        const int b = valid ? sorted[j] : 0;
+        const float px = valid ? x[b] : 0.0f, py = valid ? y[b] : 0.0f;
+        float acx = 0.0f, acy = 0.0f;
+        int top = 0;
+        bool bad = false;
+        auto interact = [&](int c, float dx, float dy, float r) {
+            float ri = rsqrtf(r);
+            float f = mass[c] * ri * ri * ri;
+            acx = fmaf(f, dx, acx);
+            acy = fmaf(f, dy, acy);
+        };
+        for (int i = 0; i < 4; ++i) {  // root children: cells always opened (:370-388)
+            int c = child[i];
+            if (c >= n && c < mlimit) {
+                if (lane == 0) {
+                    s_node[w][top] = c;
+                    s_dp[w][top] = dp1;
+                }
+                ++top;
+            } else if (c >= 0 && c < n) {
+                float dx, dy;
+                float r = ref_r(x[c], y[c], px, py, eps2, &dx, &dy);
+                interact(c, dx, dy, r);
+            }
+        }
+        while (top > 0 && !bad) {
+            __syncwarp();
+            --top;
+            const int node = s_node[w][top];
+            const float dp = 0.25f * s_dp[w][top];  // :395
+            for (int i = 0; i < 4; ++i) {
+                int c = child[4 * node + i];
+                if (c < 0) continue;
+                if (c >= mlimit) {
+                    bad = true;
+                    continue;
+                }
+                float dx, dy;
+                float r = ref_r(x[c], y[c], px, py, eps2, &dx, &dy);
+                if (c < n || __all_sync(kFull, !valid || dp <= r)) {
+                    interact(c, dx, dy, r);
+                } else if (top < STACK) {
+                    __syncwarp();
+                    if (lane == 0) {
+                        s_node[w][top] = c;
+                        s_dp[w][top] = dp;
+                    }
+                    ++top;
+                } else {
+                    bad = true;
+                }
+            }
+        }
+        if (bad && lane == 0) atomicOr(status, ST_STACK);
+        if (valid) {
+            ax[b] = acx;  // :428-429
+            ay[b] = acy;
+        }
+    }
+}
+
+__global__ void k_c_integrate(float* x, float* y, float* vx, float* vy, const float* ax,
+                              const float* ay, int n, float dt, float ddt) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        float v = __fadd_rn(vx[i], __fmul_rn(dt, ax[i]));  // kernels.cu:529-533
+        float u = __fadd_rn(vy[i], __fmul_rn(dt, ay[i]));
+        vx[i] = v;
+        vy[i] = u;
+        x[i] = __fadd_rn(x[i], __fmul_rn(ddt, v));
+        y[i] = __fadd_rn(y[i], __fmul_rn(ddt, u));
+    }
+}
+
+int fetch_status(Workspace* w) {
+    int bits = 0;
+    if (!w) return BH_OK;
+    if (cudaMemcpy(&bits, w->status, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return BH_ERR_CUDA;
+    cudaMemset(w->status, 0, 4);
+    if (bits & ST_NONFINITE) return BH_ERR_NONFINITE;
+    if (bits & ST_DUP) return BH_ERR_DUPLICATE_KEYS;
+    if (bits & ST_STACK) return BH_ERR_STACK;
+    if (bits & ST_CAPACITY) return BH_ERR_CAPACITY;
+    return BH_OK;
+}
+
+Workspace* g_last_ws = nullptr;
+
+}  // namespace
+
+extern "C" {
+
+void bh_compat_set_constants(float theta, float eps2) {
+    if (theta > 0.0f && eps2 > 0.0f) {
+        g_set.theta = theta;
+        g_set.eps2 = eps2;
+    } else {
+        record(BH_ERR_ARG);
+    }
+}
+
+void bh_compat_set_stream(void* stream) { g_set.stream = (cudaStream_t)stream; }
+
+int bh_compat_status(void) {
+    cudaError_t e = cudaStreamSynchronize(g_set.stream);
+    if (e != cudaSuccess) record(cuda_fail(e, "compat stream"));
+    std::lock_guard<std::mutex> lk(g_ws_mu);
+    for (auto& w : g_ws) {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (w.device == cur && w.base) record(fetch_status(&w));
+    }
+    return t_status;
+}
+
+void bh_compat_clear_status(void) { t_status = BH_OK; }
+
+void bh_compat_release(void) {
+    std::lock_guard<std::mutex> lk(g_ws_mu);
+    for (auto& w : g_ws)
+        if (w.base) cudaFree(w.base);
+    g_ws.clear();
+    g_last_ws = nullptr;
+}
+
+}  // extern "C"
+
+namespace ssg {
+
+void compat_SetDrawArray(float* ptr, float* x, float* y, int n) {
+    if (n <= 0) return;
+    k_c_setdraw<<<blocks_for(n, 256), 256, 0, g_set.stream>>>(ptr, x, y, n);
+    record_cuda(cudaGetLastError(), "SetDrawArray");
+}
+
+void compat_ResetArrays(int* mutex, float* x, float* y, float* mass, int* count, int* start, int* sorted,
+                 int* child, int* index, float* left, float* right, float* bottom, float* top,
+                 int n, int m) {
+    if (n < 1 || m < n) {
+        record(BH_ERR_ARG);
+        return;
+    }
+    k_c_reset<<<blocks_for(m, 256), 256, 0, g_set.stream>>>(mutex, x, y, mass, count, start,
+                                                            sorted, child, index, left, right,
+                                                            bottom, top, n, m);
+    record_cuda(cudaGetLastError(), "ResetArrays");
+}
+
+void compat_ComputeBoundingBox(int* mutex, float* x, float* y, float* left, float* right, float* bottom,
+                        float* top, int n) {
+    (void)mutex;
+    if (n < 1) {
+        record(BH_ERR_ARG);
+        return;
+    }
+    Workspace* w = workspace(1, 1);
+    if (!w) {
+        record(BH_ERR_NOMEM);
+        return;
+    }
+    int blocks = std::min(blocks_for(n, 256), 1024);
+    k_c_bbox<<<blocks, 256, 0, g_set.stream>>>(x, y, n, left, right, bottom, top, w->status);
+    record_cuda(cudaGetLastError(), "ComputeBoundingBox");
+}
+
+void compat_BuildQuadTree(float* x, float* y, float* mass, int* count, int* start, int* child, int* index,
+                   float* left, float* right, float* bottom, float* top, int n, int m) {
+    if (n < 1 || m < n) {
+        record(BH_ERR_ARG);
+        return;
+    }
+    if (n == 1) return;  // a lone body: no cells, *index stays n
+    Workspace* w = workspace((size_t)n, (size_t)m);
+    if (!w) {
+        record(BH_ERR_NOMEM);
+        return;
+    }
+    g_last_ws = w;
+    w->child_ptr = child;
+    w->child_m = m;
+    cudaStream_t st = g_set.stream;
+    const int nb = blocks_for(n, 256);
+    k_c_box_to_ord<<<1, 1, 0, st>>>(left, right, bottom, top, w->box_ord, w->seg_off, n);
+    Segs segs{1, w->seg_off, nullptr};
+    k_keys<<<nb, 256, 0, st>>>(x, y, n, segs, w->box_ord, w->keys, w->vals);
+    uint64_t *ka = w->keys, *kb = w->keys_alt;
+    uint32_t *va = w->vals, *vb = w->vals_alt;
+    const int tiles = (n + kSortTile - 1) / kSortTile;
+    for (int ps = 0; ps < 8; ++ps) {
+        k_radix_hist<<<tiles, kSortThreads, 0, st>>>(ka, va, n, 8 * ps, 0, nullptr, w->hist, tiles);
+        k_radix_scan<<<256, kSortThreads, 0, st>>>(w->hist, tiles, w->totals);
+        k_radix_scatter<<<tiles, kSortThreads, 0, st>>>(ka, va, kb, vb, n, 8 * ps, 0, nullptr,
+                                                        w->hist, w->totals, tiles);
+        std::swap(ka, kb);
+        std::swap(va, vb);
+    }
+    k_c_gather3<<<nb, 256, 0, st>>>(n, va, x, y, mass, w->sx, w->sy, w->sm);
+    k_build<<<nb, 256, 0, st>>>(ka, n, segs, w->tree, w->status);
+    record_cuda(cudaMemsetAsync(w->counter, 0, sizeof(int) * n, st), "BuildQuadTree memset");
+    k_moments<<<nb, 256, 0, st>>>(n, 0, w->sx, w->sy, w->sm, w->tree.left, w->tree.right,
+                                  w->tree.parent, w->tree.leaf_parent, w->counter, w->sums);
+    k_c_ncells<<<nb, 256, 0, st>>>(n, w->tree.split, w->tree.parent, w->ncell);
+    const int sb = blocks_for(n, 1024);
+    k_c_scan_block<<<sb, 1024, 0, st>>>(w->ncell, w->cbase, w->bsum, n);
+    k_c_scan_top<<<1, 1024, 0, st>>>(w->bsum, sb, w->total);
+    k_c_scan_add<<<nb, 256, 0, st>>>(w->cbase, w->bsum, n);
+    k_c_materialize<<<nb, 256, 0, st>>>(n, m, w->tree, ka, va, w->cbase, w->total, w->sums, child,
+                                        count, start, x, y, mass, index, w->status);
+    record_cuda(cudaGetLastError(), "BuildQuadTree");
+}
+
+void compat_ComputeCentreOfMass(float* x, float* y, float* mass, int* index, int n) {
+    k_c_com<<<1024, 256, 0, g_set.stream>>>(x, y, mass, index, n);
+    record_cuda(cudaGetLastError(), "ComputeCentreOfMass");
+}
+
+void compat_SortParticles(int* count, int* start, int* sorted, int* child, int* index, int n) {
+    (void)index;
+    Workspace* w = g_last_ws;
+    int mlimit = (w && w->child_ptr == child) ? w->child_m : 0;
+    if (!w || mlimit == 0) {
+        // layout not produced by BuildQuadTree in this process: size the queues for 2n+12000
+        mlimit = 2 * n + 12000;
+        w = workspace(1, (size_t)mlimit);
+    }
+    if (!w) {
+        record(BH_ERR_NOMEM);
+        return;
+    }
+    k_c_sort<<<1, 1024, 0, g_set.stream>>>(count, start, sorted, child, n, mlimit, w->qa, w->qb,
+                                           (int)w->mcap, w->status);
+    record_cuda(cudaGetLastError(), "SortParticles");
+}
+
+void compat_CalculateForces(float* x, float* y, float* vx, float* vy, float* ax, float* ay, float* mass,
+                     int* sorted, int* child, float* left, float* right, int n, float g) {
+    (void)vx;
+    (void)vy;
+    (void)g;  // unused in the reference too (kernels.cu:340)
+    Workspace* w = g_last_ws;
+    int mlimit = (w && w->child_ptr == child) ? w->child_m : 2 * n + 12000;
+    if (!w) w = workspace(1, 1);
+    if (!w) {
+        record(BH_ERR_NOMEM);
+        return;
+    }
+    constexpr int W = 8, S = 256;
+    int blocks = std::min(blocks_for((n + 31) / 32, W), 152 * 16);
+    k_c_forces<W, S><<<blocks, W * 32, 0, g_set.stream>>>(x, y, mass, sorted, child, left, right, n,
+                                                        mlimit, g_set.theta, g_set.eps2, ax, ay,
+                                                        w->status);
+    record_cuda(cudaGetLastError(), "CalculateForces");
+}
+
+void compat_IntegrateParticles(float* x, float* y, float* vx, float* vy, float* ax, float* ay, int n,
+                        float dt, float d) {
+    if (n <= 0) return;
+    k_c_integrate<<<blocks_for(n, 256), 256, 0, g_set.stream>>>(x, y, vx, vy, ax, ay, n, dt,
+                                                                d * dt);
+    record_cuda(cudaGetLastError(), "IntegrateParticles");
+}
+
+void compat_FillOutputArray(float* x, float* y, float* out, int n) {
+    if (n <= 0) return;
+    k_c_setdraw<<<blocks_for(n, 256), 256, 0, g_set.stream>>>(out, x, y, n);
+    record_cuda(cudaGetLastError(), "FillOutputArray");
+}
+
+}  // namespace ssg
+
+// C-linkage entry points of include/Particle_cuda.cuh
+extern "C" {
+void SetDrawArray(float* ptr, float* x, float* y, int n) { ssg::compat_SetDrawArray(ptr, x, y, n); }
+void ResetArrays(int* mutex, float* x, float* y, float* mass, int* count, int* start, int* sorted, int* child, int* index, float* left, float* right, float* bottom, float* top, int n, int m) { ssg::compat_ResetArrays(mutex, x, y, mass, count, start, sorted, child, index, left, right, bottom, top, n, m); }
+void ComputeBoundingBox(int* mutex, float* x, float* y, float* left, float* right, float* bottom, float* top, int n) { ssg::compat_ComputeBoundingBox(mutex, x, y, left, right, bottom, top, n); }
+void BuildQuadTree(float* x, float* y, float* mass, int* count, int* start, int* child, int* index, float* left, float* right, float* bottom, float* top, int n, int m) { ssg::compat_BuildQuadTree(x, y, mass, count, start, child, index, left, right, bottom, top, n, m); }
+void ComputeCentreOfMass(float* x, float* y, float* mass, int* index, int n) { ssg::compat_ComputeCentreOfMass(x, y, mass, index, n); }
+void SortParticles(int* count, int* start, int* sorted, int* child, int* index, int n) { ssg::compat_SortParticles(count, start, sorted, child, index, n); }
+void CalculateForces(float* x, float* y, float* vx, float* vy, float* ax, float* ay, float* mass, int* sorted, int* child, float* left, float* right, int n, float g) { ssg::compat_CalculateForces(x, y, vx, vy, ax, ay, mass, sorted, child, left, right, n, g); }
+void IntegrateParticles(float* x, float* y, float* vx, float* vy, float* ax, float* ay, int n, float dt, float d) { ssg::compat_IntegrateParticles(x, y, vx, vy, ax, ay, n, dt, d); }
+void FillOutputArray(float* x, float* y, float* out, int n) { ssg::compat_FillOutputArray(x, y, out, n); }
+}  // extern "C"

@@ -100,7 +100,7 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* total,
 // that starts at the origin (the reference resets the box to 0, kernels.cu:54-57),
 // then warp shuffles, shared memory, and one atomicMin/Max per value and block.
 template <int THREADS>
-__global__ void __launch_bounds__(THREADS) k_bbox(const float* __restrict__ x,
+static __global__ void __launch_bounds__(THREADS) k_bbox(const float* __restrict__ x,
                                                   const float* __restrict__ y,
                                                   const int* __restrict__ chunk_seg,
                                                   const int* __restrict__ chunk_begin,
@@ -192,7 +192,7 @@ __device__ __forceinline__ uint64_t quad_key(float px, float py, Box bx) {
     return key;
 }
 
-__global__ void k_keys(const float* __restrict__ x, const float* __restrict__ y, int n, Segs segs,
+static __global__ void k_keys(const float* __restrict__ x, const float* __restrict__ y, int n, Segs segs,
                        const int* __restrict__ box_ord, uint64_t* __restrict__ keys,
                        uint32_t* __restrict__ vals) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -217,7 +217,7 @@ constexpr int kSortItems = 8;
 constexpr int kSortTile = kSortThreads * kSortItems;
 
 // per-tile digit counts, written digit-major: hist[d * tiles + tile]
-__global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint64_t* __restrict__ keys,
+static __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint64_t* __restrict__ keys,
                                                              const uint32_t* __restrict__ vals, int n,
                                                              int shift, int use_seg,
                                                              const int* __restrict__ seg_of_pos,
@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint64_t* __r
 }
 
 // block d turns column d of hist into exclusive offsets; totals[d] = column sum
-__global__ void __launch_bounds__(kSortThreads) k_radix_scan(uint32_t* __restrict__ hist, int tiles,
+static __global__ void __launch_bounds__(kSortThreads) k_radix_scan(uint32_t* __restrict__ hist, int tiles,
                                                              uint32_t* __restrict__ totals) {
     __shared__ uint32_t s_tmp[kSortThreads / 32];
     uint32_t* col = hist + (size_t)blockIdx.x * tiles;
@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scan(uint32_t* __restric
 // (earlier rounds of the warp) + (lower lanes with the same digit); warps are
 // then offset by the counts of lower warps.  Elements are staged in shared
 // memory in digit order and written out as contiguous runs.
-__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(
+static __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(
     const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
     uint32_t* __restrict__ vout, int n, int shift, int use_seg, const int* __restrict__ seg_of_pos,
     const uint32_t* __restrict__ hist, const uint32_t* __restrict__ totals, int tiles) {
@@ -340,9 +340,10 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(
 struct BodyPtrs {
     float *x, *y, *vx, *vy, *m, *xlo, *ylo;  // xlo/ylo may be null
     int* id;
+    float* amag;  // |a| of the previous step (accuracy modes; may be null)
 };
 
-__global__ void k_gather(int n, const uint32_t* __restrict__ perm, BodyPtrs src, BodyPtrs dst) {
+static __global__ void k_gather(int n, const uint32_t* __restrict__ perm, BodyPtrs src, BodyPtrs dst) {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     uint32_t i = perm[j];
@@ -356,6 +357,7 @@ __global__ void k_gather(int n, const uint32_t* __restrict__ perm, BodyPtrs src,
         dst.xlo[j] = src.xlo[i];
         dst.ylo[j] = src.ylo[i];
     }
+    if (src.amag) dst.amag[j] = src.amag[i];
 }
 
 // ------------------------------------------------------------------ (b3) tree
@@ -373,7 +375,7 @@ struct TreePtrs {
 };
 
 // Karras (2012) radix-tree construction, one thread per internal node.
-__global__ void k_build(const uint64_t* __restrict__ k, int n, Segs segs, TreePtrs t,
+static __global__ void k_build(const uint64_t* __restrict__ k, int n, Segs segs, TreePtrs t,
                         int* __restrict__ status) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -478,7 +480,7 @@ __device__ __forceinline__ ChildVals load_child(int c, const float* __restrict__
 // thread arrives last) and continues.  REFERENCE mode keeps the reference's
 // definition com = (sum m*x) / (sum m) (kernels.cu:283-284); accuracy modes
 // combine centres relative to each other and add second moments.
-__global__ void k_moments(int n, int accuracy, const float* __restrict__ sx,
+static __global__ void k_moments(int n, int accuracy, const float* __restrict__ sx,
                           const float* __restrict__ sy, const float* __restrict__ sm,
                           const int* __restrict__ left, const int* __restrict__ right,
                           const int* __restrict__ parent, const int* __restrict__ leaf_parent,
@@ -530,7 +532,7 @@ struct Records {
     float4* A;  // cx, cy, M, criterion (REFERENCE: dp of the node's level; accuracy: ropen^2)
     float4* B;  // accuracy: 3Sxx, 3Sxy, 3Syy, 1.5 (Sxx+Syy)
     int4* C;    // up to four children, kNoChild padded
-    int2* D;    // first body, body count
+    int4* D;    // first body, body count, bits of G*M*l^3 (accuracy), 0
 };
 
 // dp_L = w_L^2/theta with w_L the level-L cell width from the x extent only:
@@ -544,7 +546,7 @@ __device__ __forceinline__ float ref_dp(Box bx, float theta, int level) {
     return ldexpf(dp1, -2 * (level - 1));
 }
 
-__global__ void k_records(int n, Segs segs, int accuracy, float theta,
+static __global__ void k_records(int n, Segs segs, int accuracy, float theta, float G,
                           const int* __restrict__ box_ord, const uint64_t* __restrict__ skeys,
                           const int* __restrict__ left, const int* __restrict__ right,
                           const int* __restrict__ parent, const int* __restrict__ split,
@@ -571,12 +573,12 @@ __global__ void k_records(int n, Segs segs, int accuracy, float theta,
     }
     rec.C[i] = make_int4(ch[0], ch[1], ch[2], ch[3]);
     int f = first[i], cnt = last[i] - f + 1;
-    rec.D[i] = make_int2(f, cnt);
     int level = sp >> 1;
     Box bx = load_box(box_ord, seg_of(segs, i));
     float cx = ns.cx[i], cy = ns.cy[i], M = ns.m[i];
     if (!accuracy) {
         rec.A[i] = make_float4(cx, cy, M, ref_dp(bx, theta, level));
+        rec.D[i] = make_int4(f, cnt, 0, 0);
         return;
     }
     // cell rectangle of the node's level from its key prefix (x bit 1 = left half)
@@ -588,15 +590,16 @@ __global__ void k_records(int n, Segs segs, int accuracy, float theta,
         ix = (ix << 1) | ((dgt & 1u) ? 0ull : 1ull);
         iy = (iy << 1) | ((dgt & 2u) ? 0ull : 1ull);
     }
+    // FP64 for the extent of the cell (the box may be far from the origin)
     double wx = ((double)bx.r - (double)bx.l), wy = ((double)bx.t - (double)bx.b);
     double scale = ldexp(1.0, -L);
-    double x0 = bx.l + wx * scale * (double)ix, x1 = x0 + wx * scale;
-    double y0 = bx.b + wy * scale * (double)iy, y1 = y0 + wy * scale;
-    double ex = fmax(fabs(cx - x0), fabs(x1 - cx));
-    double ey = fmax(fabs(cy - y0), fabs(y1 - cy));
-    double bmax2 = ex * ex + ey * ey;
-    float ropen2 = (float)(bmax2 / ((double)theta * (double)theta));
-    rec.A[i] = make_float4(cx, cy, M, ropen2);
+    double x0 = bx.l + wx * scale * (double)ix, y0 = bx.b + wy * scale * (double)iy;
+    double l = fmax(wx, wy) * scale;
+    double ddx = cx - (x0 + 0.5 * wx * scale), ddy = cy - (y0 + 0.5 * wy * scale);
+    double r = l / (double)theta + sqrt(ddx * ddx + ddy * ddy);  // l/theta + |COM - centre|
+    rec.A[i] = make_float4(cx, cy, M, (float)(r * r));
+    float qerr = (float)((double)G * (double)M * l * l * l);     // G M l^3 (relative rule)
+    rec.D[i] = make_int4(f, cnt, __float_as_int(qerr), 0);
     float4 q = ns.quad[i];  // S about the centre of mass -> T = 3S, h = 1.5 tr S
     rec.B[i] = make_float4(3.0f * q.x, 3.0f * q.y, 3.0f * q.z, 1.5f * (q.x + q.z));
 }

@@ -66,7 +66,10 @@ namespace ssg {
 template <int BUCKET, bool MIXED>
 static cudaError_t set_acc_attr() {
     using Sm = AccSmem<kWalkWarps, kAccStack, BUCKET>;
-    return cudaFuncSetAttribute(k_walk_acc<kWalkWarps, kAccStack, BUCKET, MIXED>,
+    cudaError_t e = cudaFuncSetAttribute(k_walk_acc<kWalkWarps, kAccStack, BUCKET, MIXED, false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Sm));
+    if (e != cudaSuccess || MIXED) return e;
+    return cudaFuncSetAttribute(k_walk_acc<kWalkWarps, kAccStack, BUCKET, false, true>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Sm));
 }
 
@@ -85,12 +88,15 @@ cudaError_t init_walk_attributes() {
 template <int BUCKET, bool MIXED>
 static cudaError_t launch_acc(const StepArgs& a, cudaStream_t st) {
     using Sm = AccSmem<kWalkWarps, kAccStack, BUCKET>;
-    auto kern = k_walk_acc<kWalkWarps, kAccStack, BUCKET, MIXED>;
     int grid = std::min(a.walk_grid_acc, (a.groups.ngroups + kWalkWarps - 1) / kWalkWarps);
     if (grid < 1) grid = 1;
-    kern<<<grid, kWalkWarps * 32, sizeof(Sm), st>>>(a.segs, a.groups, a.in, a.recA, a.recB, a.recC,
-                                                    a.recD, a.eps2, a.G, a.dt, a.ddt, a.out,
-                                                    a.status, a.inter);
+    // bootstrap pass: exits at once unless bh_set_state left the state fresh
+    k_walk_acc<kWalkWarps, kAccStack, BUCKET, false, true><<<grid, kWalkWarps * 32, sizeof(Sm), st>>>(
+        a.segs, a.groups, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt, a.alpha,
+        a.out, a.status, a.inter, a.work + 1, a.fresh);
+    k_walk_acc<kWalkWarps, kAccStack, BUCKET, MIXED, false><<<grid, kWalkWarps * 32, sizeof(Sm), st>>>(
+        a.segs, a.groups, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt, a.alpha,
+        a.out, a.status, a.inter, a.work + 2, a.fresh);
     return cudaGetLastError();
 }
 
@@ -109,7 +115,8 @@ cudaError_t launch_walk(const StepArgs& a, cudaStream_t st) {
         int grid = std::min(a.walk_grid_ref, (a.groups.ngroups + kWalkWarps - 1) / kWalkWarps);
         if (grid < 1) grid = 1;
         k_walk_ref<kWalkWarps, kRefStack><<<grid, kWalkWarps * 32, 0, st>>>(
-            a.segs, a.groups, a.in, a.recA, a.recC, a.eps2, a.dt, a.ddt, a.out, a.status, a.inter);
+            a.segs, a.groups, a.in, a.recA, a.recC, a.eps2, a.dt, a.ddt, a.out, a.status, a.inter,
+            a.work);
         return cudaGetLastError();
     }
     return a.mode == BH_MODE_MIXED ? launch_acc_bucket<true>(a, st)
@@ -158,10 +165,13 @@ struct bh_system {
     float *ax = nullptr, *ay = nullptr;
     int* status = nullptr;
     unsigned long long* inter = nullptr;
+    int* work = nullptr;   // 3 dynamic-scheduling counters, reset every step
+    int* fresh = nullptr;  // 1 after bh_set_state: bootstrap |a_old| in the next step
     int seg_passes = 0;
 
     int walk_grid_ref = 0, walk_grid_acc = 0;
     bool have_state = false;
+    bool caller_order = false;  // true from bh_set_state until the next step
 
     cudaStream_t cap_stream = nullptr;
     cudaGraph_t graph = nullptr;
@@ -193,9 +203,10 @@ ssg::StepArgs step_args(bh_system* s) {
     const BodyPtrs& g = s->st[1];
     const BodyPtrs& c = s->st[0];
     bool mixed = s->p.mode == BH_MODE_MIXED;
-    a.in = WalkIn{g.x, g.y, g.vx, g.vy, g.m, mixed ? g.xlo : nullptr, mixed ? g.ylo : nullptr, g.id};
+    a.in = WalkIn{g.x, g.y, g.vx, g.vy, g.m, mixed ? g.xlo : nullptr, mixed ? g.ylo : nullptr, g.id,
+                  g.amag};
     a.out = WalkOut{c.x, c.y, c.vx, c.vy, c.m, mixed ? c.xlo : nullptr, mixed ? c.ylo : nullptr, c.id,
-                    s->ax, s->ay};
+                    s->ax, s->ay, c.amag};
     a.recA = s->rec.A;
     a.recB = s->rec.B;
     a.recC = s->rec.C;
@@ -204,8 +215,11 @@ ssg::StepArgs step_args(bh_system* s) {
     a.G = s->p.gravity;
     a.dt = s->p.timestep;
     a.ddt = s->p.dampening * s->p.timestep;  // kernels.cu:532: d*dt, in float
+    a.alpha = s->p.alpha;
     a.status = s->status;
     a.inter = s->inter;
+    a.work = s->work;
+    a.fresh = s->fresh;
     a.bucket = normalized_bucket(s->p.leaf_bucket);
     a.walk_grid_ref = s->walk_grid_ref;
     a.walk_grid_acc = s->walk_grid_acc;
@@ -222,6 +236,7 @@ int enqueue_step(bh_system* s, cudaStream_t st, cudaEvent_t* ev = nullptr) {
     CK(cudaMemsetAsync(s->box_ord, 0, sizeof(int) * 4 * s->nseg, st));  // origin box
     CK(cudaMemsetAsync(s->counter, 0, sizeof(int) * n, st));
     CK(cudaMemsetAsync(s->inter, 0, sizeof(unsigned long long), st));
+    CK(cudaMemsetAsync(s->work, 0, 3 * sizeof(int), st));
 
     BodyPtrs cur = s->st[0];
     CK(mark(0));
@@ -258,6 +273,7 @@ int enqueue_step(bh_system* s, cudaStream_t st, cudaEvent_t* ev = nullptr) {
         src.xlo = src.ylo = nullptr;
         dst.xlo = dst.ylo = nullptr;
     }
+    if (!accuracy) src.amag = dst.amag = nullptr;
     k_gather<<<nb, tb, 0, st>>>(n, va, src, dst);
     CK(mark(4));
     k_build<<<nb, tb, 0, st>>>(ka, n, segs, s->tree, s->status);
@@ -266,7 +282,7 @@ int enqueue_step(bh_system* s, cudaStream_t st, cudaEvent_t* ev = nullptr) {
                                  s->tree.right, s->tree.parent, s->tree.leaf_parent, s->counter,
                                  s->sums);
     CK(mark(6));
-    k_records<<<nb, tb, 0, st>>>(n, segs, accuracy ? 1 : 0, s->p.theta, s->box_ord, ka,
+    k_records<<<nb, tb, 0, st>>>(n, segs, accuracy ? 1 : 0, s->p.theta, s->p.gravity, s->box_ord, ka,
                                  s->tree.left, s->tree.right, s->tree.parent, s->tree.split,
                                  s->tree.first, s->tree.last, s->sums, s->rec);
     CK(cudaGetLastError());
@@ -447,15 +463,16 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     s->ngroups = goff[nseg];
 
     size_t bytes = 0;
-    bytes += 2 * (7 * span<float>(N) + span<int>(N));
+    bytes += 2 * (8 * span<float>(N) + span<int>(N));
     bytes += 2 * span<uint64_t>(N) + 2 * span<uint32_t>(N);
     bytes += span<uint32_t>((size_t)256 * s->tiles) + span<uint32_t>(256);
     bytes += span<int>(4 * (size_t)nseg) + 2 * span<int>(nseg + 1) + span<int>(N);
     bytes += 3 * span<int>(s->nchunks);
     bytes += 8 * span<int>(N);
     bytes += 5 * span<float>(N) + span<float4>(N);
-    bytes += 2 * span<float4>(N) + span<int4>(N) + span<int2>(N);
-    bytes += 2 * span<float>(N) + span<int>(1) + span<unsigned long long>(1);
+    bytes += 2 * span<float4>(N) + 2 * span<int4>(N);
+    bytes += 2 * span<float>(N) + span<int>(1) + span<unsigned long long>(1) + span<int>(3) +
+             span<int>(1);
     cudaError_t e = cudaMalloc(&s->arena, bytes);
     if (e != cudaSuccess) {
         cuda_fail(e, "cudaMalloc(arena)");
@@ -474,6 +491,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
         b.xlo = carve<float>(c, N);
         b.ylo = carve<float>(c, N);
         b.id = carve<int>(c, N);
+        b.amag = carve<float>(c, N);
     }
     s->keys = carve<uint64_t>(c, N);
     s->keys_alt = carve<uint64_t>(c, N);
@@ -505,11 +523,13 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     s->rec.A = carve<float4>(c, N);
     s->rec.B = carve<float4>(c, N);
     s->rec.C = carve<int4>(c, N);
-    s->rec.D = carve<int2>(c, N);
+    s->rec.D = carve<int4>(c, N);
     s->ax = carve<float>(c, N);
     s->ay = carve<float>(c, N);
     s->status = carve<int>(c, 1);
     s->inter = carve<unsigned long long>(c, 1);
+    s->work = carve<int>(c, 3);
+    s->fresh = carve<int>(c, 1);
 
     std::vector<int> sop;
     if (nseg > 1) {
@@ -531,6 +551,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     up(s->chunk_begin, cbeg.data(), sizeof(int) * s->nchunks);
     up(s->chunk_end, cend.data(), sizeof(int) * s->nchunks);
     if (rc == BH_OK && cudaMemset(s->status, 0, sizeof(int)) != cudaSuccess) rc = BH_ERR_CUDA;
+    if (rc == BH_OK && cudaMemset(s->fresh, 0, sizeof(int)) != cudaSuccess) rc = BH_ERR_CUDA;
     if (rc == BH_OK) {
         cudaError_t ea = init_walk_attributes();
         if (ea != cudaSuccess) rc = cuda_fail(ea, "cudaFuncSetAttribute(walk)");
@@ -541,7 +562,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
             &bref, k_walk_ref<kWalkWarps, kRefStack>, kWalkWarps * 32, 0);
         using Sm = AccSmem<kWalkWarps, kAccStack, 16>;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &bacc, k_walk_acc<kWalkWarps, kAccStack, 16, true>, kWalkWarps * 32, sizeof(Sm));
+            &bacc, k_walk_acc<kWalkWarps, kAccStack, 16, true, false>, kWalkWarps * 32, sizeof(Sm));
         s->walk_grid_ref = walk_grid_cap(s->sms, bref) * 4;
         s->walk_grid_acc = walk_grid_cap(s->sms, bacc) * 4;
         cudaGetLastError();
@@ -574,6 +595,7 @@ void bh_default_params(bh_params* p) {
     p->block_size = 0;
     p->stack_depth = 0;
     p->use_graph = 0;
+    p->alpha = 0.01f;
 }
 
 int bh_create(const bh_params* p, int n, int device, bh_system** out) {
@@ -629,9 +651,39 @@ int bh_set_state(bh_system* s, const float* x, const float* y, const float* vx, 
     CK(cudaMemsetAsync(s->ax, 0, b, st));
     CK(cudaMemsetAsync(s->ay, 0, b, st));
     CK(cudaMemsetAsync(s->status, 0, sizeof(int), st));
+    CK(cudaMemsetAsync(c.amag, 0, b, st));
+    const int one = 1;
+    CK(cudaMemcpyAsync(s->fresh, &one, sizeof(int), cudaMemcpyHostToDevice, st));
     k_iota<<<(s->n + 255) / 256, 256, 0, st>>>(c.id, s->n);
     CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));  // `one` lives on this stack frame
     s->have_state = true;
+    s->caller_order = true;
+    return BH_OK;
+}
+
+__global__ void k_amag(int n, const float* ax, const float* ay, float* amag, float* sax, float* say) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        float a = ax[i], b = ay[i];
+        amag[i] = sqrtf(a * a + b * b);
+        sax[i] = a;
+        say[i] = b;
+    }
+}
+
+int bh_set_accel(bh_system* s, const float* ax, const float* ay, void* stream) {
+    if (!s || !ax || !ay) return BH_ERR_ARG;
+    if (!s->have_state || !s->caller_order) return BH_ERR_STATE;  // only right after bh_set_state
+    CK(cudaSetDevice(s->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t b = sizeof(float) * s->n;
+    BodyPtrs& t = s->st[1];
+    CK(cudaMemcpyAsync(t.x, ax, b, cudaMemcpyDefault, st));
+    CK(cudaMemcpyAsync(t.y, ay, b, cudaMemcpyDefault, st));
+    k_amag<<<(s->n + 255) / 256, 256, 0, st>>>(s->n, t.x, t.y, s->st[0].amag, s->ax, s->ay);
+    CK(cudaGetLastError());
+    CK(cudaMemsetAsync(s->fresh, 0, sizeof(int), st));
     return BH_OK;
 }
 
@@ -700,11 +752,13 @@ int bh_step(bh_system* s, int steps, void* stream) {
             if (rc != BH_OK) return rc;
         }
         for (int k = 0; k < steps; ++k) CK(cudaGraphLaunch(s->graph_exec, st));
+        if (steps > 0) s->caller_order = false;
         return BH_OK;
     }
     for (int k = 0; k < steps; ++k) {
         int rc = enqueue_step(s, st);
         if (rc != BH_OK) return rc;
+        s->caller_order = false;
     }
     return BH_OK;
 }
@@ -814,6 +868,7 @@ int bh_step_profiled(bh_system* s, void* stream, float* phase_ms) {
     cudaEvent_t ev[BH_NUM_PHASES + 1];
     for (auto& e : ev) CK(cudaEventCreate(&e));
     int rc = enqueue_step(s, st, ev);
+    s->caller_order = false;
     if (rc == BH_OK) {
         CK(cudaEventSynchronize(ev[BH_NUM_PHASES]));
         for (int k = 0; k < BH_NUM_PHASES; ++k) {

@@ -23,10 +23,12 @@ struct StepArgs {
     const float4* recA;
     const float4* recB;
     const int4* recC;
-    const int2* recD;
-    float eps2, G, dt, ddt;
+    const int4* recD;
+    float eps2, G, dt, ddt, alpha;
     int* status;
     unsigned long long* inter;
+    int* work;   // [0] reference walk, [1] bootstrap pass, [2] accuracy walk
+    int* fresh;  // set by bh_set_state: the next step bootstraps |a_old|
     int bucket;
     int walk_grid_ref, walk_grid_acc;
 };

@@ -25,12 +25,21 @@ namespace ssg {
 struct WalkIn {
     const float *x, *y, *vx, *vy, *m, *xlo, *ylo;
     const int* id;
+    float* amag;  // |a| of the previous step; written by the bootstrap pass
 };
 struct WalkOut {
     float *x, *y, *vx, *vy, *m, *xlo, *ylo;
     int* id;
     float *ax, *ay;
+    float* amag;  // |a| of this step, for the next step's relative rule
 };
+
+// Next group for this warp: dynamic scheduling, groups differ ~10x in cost.
+__device__ __forceinline__ int next_group(int* work) {
+    int g = 0;
+    if ((threadIdx.x & 31) == 0) g = atomicAdd(work, 1);
+    return __shfl_sync(kFull, g, 0);
+}
 
 struct Groups {
     int ngroups;
@@ -72,12 +81,13 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk_ref(Segs segs, Groups gr, W
                                                          const int4* __restrict__ recC, float eps2,
                                                          float dt, float ddt, WalkOut out,
                                                          int* __restrict__ status,
-                                                         unsigned long long* __restrict__ inter_total) {
+                                                         unsigned long long* __restrict__ inter_total,
+                                                         int* __restrict__ work) {
     __shared__ int s_stack[WARPS][STACK];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int* stack = s_stack[warp];
     unsigned long long my_inter = 0;
-    for (int g = blockIdx.x * WARPS + warp; g < gr.ngroups; g += gridDim.x * WARPS) {
+    for (int g = next_group(work); g < gr.ngroups; g = next_group(work)) {
         int lo, hi, gstart;
         group_range(segs, gr, g, &lo, &hi, &gstart);
         const int j = gstart + lane;
@@ -220,17 +230,30 @@ struct AccSmem {
     float4 cA[WARPS][32];
     float4 cB[WARPS][32];
     float4 bP[WARPS][32];
+    float2 gp[WARPS][32];  // the group's body positions, for the exact distance test
 };
 
-template <int WARPS, int STACK, int BUCKET, bool MIXED>
+// PLAIN / MIXED walk.  ESTIMATE = the bootstrap pass after bh_set_state: the
+// geometric rule only, writes |G a| into in.amag and nothing else (skipped
+// unless *fresh is set).  The main pass also applies the relative rule
+//   G M l^3 <= alpha * a_g * d^5,  a_g = max(min |a_old|, 0.1 mean |a_old|) over the group,
+// d = min over the group's bodies of |COM - p|; the geometric rule is d > l/theta + delta.
+template <int WARPS, int STACK, int BUCKET, bool MIXED, bool ESTIMATE>
 __global__ void __launch_bounds__(WARPS * 32) k_walk_acc(Segs segs, Groups gr, WalkIn in,
                                                          const float4* __restrict__ recA,
                                                          const float4* __restrict__ recB,
                                                          const int4* __restrict__ recC,
-                                                         const int2* __restrict__ recD, float eps2,
-                                                         float G, float dt, float ddt, WalkOut out,
-                                                         int* __restrict__ status,
-                                                         unsigned long long* __restrict__ inter_total) {
+                                                         const int4* __restrict__ recD, float eps2,
+                                                         float G, float dt, float ddt, float alpha,
+                                                         WalkOut out, int* __restrict__ status,
+                                                         unsigned long long* __restrict__ inter_total,
+                                                         int* __restrict__ work,
+                                                         int* __restrict__ fresh) {
+    if (ESTIMATE) {
+        if (*(volatile int*)fresh == 0) return;
+    } else if (blockIdx.x == 0 && threadIdx.x == 0) {
+        *fresh = 0;  // the bootstrap pass of this step (if any) has completed
+    }
     using Sm = AccSmem<WARPS, STACK, BUCKET>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Sm& sm = *reinterpret_cast<Sm*>(smem_raw);
@@ -242,23 +265,30 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk_acc(Segs segs, Groups gr, W
     float4* cA = sm.cA[warp];
     float4* cB = sm.cB[warp];
     float4* bP = sm.bP[warp];
+    float2* gp = sm.gp[warp];
     unsigned long long my_inter = 0;
 
-    for (int g = blockIdx.x * WARPS + warp; g < gr.ngroups; g += gridDim.x * WARPS) {
+    for (int g = next_group(work); g < gr.ngroups; g = next_group(work)) {
         int lo, hi, gstart;
         group_range(segs, gr, g, &lo, &hi, &gstart);
         const int j = gstart + lane;
         const bool valid = j < hi;
         const int cnt = min(32, hi - gstart);
-        const int jj = valid ? j : gstart;  // invalid lanes mirror lane 0's body
+        const int jj = valid ? j : gstart;  // invalid lanes mirror the group's first body
         const float px = in.x[jj], py = in.y[jj];
-        float gx0 = px, gx1 = px, gy0 = py, gy1 = py;
+        __syncwarp();
+        gp[lane] = make_float2(px, py);
+        // relative-rule scale of the group
+        float aa = __int_as_float(0x7f800000);
+        if (!ESTIMATE && alpha > 0.0f) {
+            float a = in.amag[jj];
+            float amin = a, asum = valid ? a : 0.0f;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            gx0 = fminf(gx0, __shfl_xor_sync(kFull, gx0, o));
-            gx1 = fmaxf(gx1, __shfl_xor_sync(kFull, gx1, o));
-            gy0 = fminf(gy0, __shfl_xor_sync(kFull, gy0, o));
-            gy1 = fmaxf(gy1, __shfl_xor_sync(kFull, gy1, o));
+            for (int o = 16; o > 0; o >>= 1) {
+                amin = fminf(amin, __shfl_xor_sync(kFull, amin, o));
+                asum += __shfl_xor_sync(kFull, asum, o);
+            }
+            aa = alpha * fmaxf(amin, 0.1f * asum / (float)cnt);
         }
         float ax = 0.0f, ay = 0.0f;     // running sums
         float cax = 0.0f, cay = 0.0f;   // Kahan compensation (MIXED)
@@ -269,7 +299,6 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk_acc(Segs segs, Groups gr, W
             if (lane == 0) stack[0] = lo;
             top = 1;
         }
-        // flush helpers ---------------------------------------------------
         auto add_batch = [&](float bx, float by) {
             if (MIXED) {
                 float yx = bx - cax, tx = ax + yx;
@@ -313,7 +342,6 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk_acc(Segs segs, Groups gr, W
             bcnt -= k;
             entries += k;
         };
-        // traversal -------------------------------------------------------
         while (top > 0) {
             int k = min(32, top);
             int room = (STACK - top) / 3;  // pop k, push <= 4k: keep top+3k <= STACK
@@ -325,22 +353,25 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk_acc(Segs segs, Groups gr, W
             __syncwarp();
             const int node = lane < k ? stack[top - 1 - lane] : -1;
             top -= k;
-            int cat = -1;  // 0 accept cell, 1 leaf bodies, 2 open
-            float4 A;
-            int2 D = make_int2(0, 0);
+            int cat = -1;  // 0 approximate, 1 leaf bodies, 2 open
+            int4 D = make_int4(0, 0, 0, 0);
             if (node >= 0) {
-                A = recA[node];
+                const float4 A = recA[node];
                 D = recD[node];
-                float ddx = fmaxf(fmaxf(gx0 - A.x, A.x - gx1), 0.0f);
-                float ddy = fmaxf(fmaxf(gy0 - A.y, A.y - gy1), 0.0f);
-                float d2 = fmaf(ddx, ddx, ddy * ddy);
-                cat = d2 > A.w ? 0 : (D.y <= BUCKET ? 1 : 2);
+                float d2 = __int_as_float(0x7f800000);
+#pragma unroll 8
+                for (int e = 0; e < 32; ++e) {
+                    float2 q = gp[e];
+                    float dx = q.x - A.x, dy = q.y - A.y;
+                    d2 = fminf(d2, fmaf(dx, dx, dy * dy));
+                }
+                bool acc = d2 > A.w;
+                if (acc && !ESTIMATE) acc = __int_as_float(D.z) <= aa * d2 * d2 * sqrtf(d2);
+                cat = acc ? 0 : (D.y <= BUCKET ? 1 : 2);
             }
-            // accepted cells
             unsigned mc = __ballot_sync(kFull, cat == 0);
             if (cat == 0) clist[ccnt + __popc(mc & lt)] = node;
             ccnt += __popc(mc);
-            // opened nodes: children
             int4 C = make_int4(kNoChild, kNoChild, kNoChild, kNoChild);
             if (cat == 2) C = recC[node];
             const int cs[4] = {C.x, C.y, C.z, C.w};
@@ -377,10 +408,14 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk_acc(Segs segs, Groups gr, W
         if (ccnt > 0) flush_cells(ccnt);
         if (bcnt > 0) flush_bodies(bcnt);
         if (overflow && lane == 0) atomicOr(status, ST_STACK);
+        const float gax = G * (MIXED ? ax - cax : ax);
+        const float gay = G * (MIXED ? ay - cay : ay);
+        if (ESTIMATE) {
+            if (valid) in.amag[j] = sqrtf(gax * gax + gay * gay);
+            continue;
+        }
         my_inter += (unsigned long long)(entries * cnt);
         if (valid) {
-            float gax = G * (MIXED ? ax - cax : ax);
-            float gay = G * (MIXED ? ay - cay : ay);
             float vx = fmaf(dt, gax, in.vx[j]);
             float vy = fmaf(dt, gay, in.vy[j]);
             if (MIXED) {
@@ -409,9 +444,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk_acc(Segs segs, Groups gr, W
             out.id[j] = in.id[j];
             out.ax[j] = gax;
             out.ay[j] = gay;
+            out.amag[j] = sqrtf(gax * gax + gay * gay);
         }
     }
-    if (lane == 0 && my_inter) atomicAdd(inter_total, my_inter);
+    if (!ESTIMATE && lane == 0 && my_inter) atomicAdd(inter_total, my_inter);
 }
 
 }  // namespace ssg

@@ -1,0 +1,42 @@
+"""Small fixed workload for profiler captures (ncu launch lists and kernel captures).
+
+    python -m stellarsolver_gb300.profile_step --n 1048576 --mode mixed --steps 3
+
+Creates one system on the 2D Plummer input, runs `--warmup` steps, then
+`--steps` steps, synchronising after each, and prints the per-step status.
+Kernel order per step: k_bbox, k_keys, (k_radix_hist, k_radix_scan,
+k_radix_scatter) x 8, k_gather, k_build, k_moments, k_records, then the walk
+(REFERENCE: k_walk_ref; PLAIN/MIXED: the bootstrap k_walk_acc, which exits at
+once unless the state was just set, and the main k_walk_acc).
+"""
+import argparse
+
+from . import bh, models
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=1 << 20)
+    ap.add_argument("--mode", default="mixed", choices=list(bh.MODES))
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=1)
+    ap.add_argument("--bucket", type=int, default=0)
+    ap.add_argument("--graph", action="store_true")
+    a = ap.parse_args()
+    x, y, vx, vy, m = models.plummer(a.n, models.SEED_BASE + 1)
+    with bh.BarnesHutSystem(a.n, mode=a.mode, theta=0.5, eps2=1e-4, timestep=1e-4,
+                            leaf_bucket=a.bucket, use_graph=a.graph) as s:
+        s.set_state(x, y, vx, vy, m)
+        for _ in range(a.warmup):
+            s.step(1)
+            s.sync()
+        for k in range(a.steps):
+            s.step(1)
+            s.sync()
+        st = s.stats()
+    print(f"profile_step n={a.n} mode={a.mode} steps={a.steps} interactions={st['interactions']} "
+          f"status={st['status']}")
+
+
+if __name__ == "__main__":
+    main()

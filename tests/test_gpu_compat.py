@@ -1,0 +1,176 @@
+"""The drop-in wrappers (include/Particle_cuda.cuh) on the reference's layout.
+
+Runs the reference's update() sequence (BarnesHutParticleSystem.cpp:308-315)
+through the nine wrappers on device arrays of length m = 2n+12000, phase by
+phase, and compares every phase with the golden fixtures made by the
+reference's own kernels: box, tree (canonical form), counts, sorted[] and
+start[] bit-exact; centres of mass, forces and the integrated state within the
+tolerances of test_oracle_golden.py.  debug.cpp's invariants must hold too.
+"""
+import numpy as np
+import pytest
+
+import golden_cases as gc
+from test_oracle_golden import FORCE_TOL, TRAJ_TOL
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def L():
+    import compat_lib
+
+    lib = compat_lib.load()
+    lib.bh_compat_set_constants(0.5, 0.025)
+    return lib
+
+
+def P(t):
+    return t.data_ptr()
+
+
+class RefArrays:
+    """Device arrays laid out like BarnesHutParticleSystem.cpp:54-83."""
+
+    def __init__(self, g):
+        n = int(g["n"])
+        m = 2 * n + 12000
+        self.n, self.m = n, m
+        dev = "cuda"
+        f = lambda: torch.zeros(m, dtype=torch.float32, device=dev)  # noqa: E731
+        self.x, self.y, self.vx, self.vy, self.mass, self.ax, self.ay = (f() for _ in range(7))
+        for t, k in ((self.x, "x"), (self.y, "y"), (self.vx, "vx"), (self.vy, "vy"),
+                     (self.mass, "m")):
+            t[:n] = torch.from_numpy(g[k])
+        i = lambda k=1: torch.zeros(k * m, dtype=torch.int32, device=dev)  # noqa: E731
+        self.count, self.start, self.sorted, self.child = i(), i(), i(), i(4)
+        self.index = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.mutex = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.box = [torch.zeros(1, dtype=torch.float32, device=dev) for _ in range(4)]
+        self.out = torch.zeros(2 * m, dtype=torch.float32, device=dev)
+
+
+def update(L, a, dt, damp, rec):
+    n, m = a.n, a.m
+    bx = [P(b) for b in a.box]
+    L.ResetArrays(P(a.mutex), P(a.x), P(a.y), P(a.mass), P(a.count), P(a.start), P(a.sorted),
+                  P(a.child), P(a.index), *bx, n, m)
+    L.ComputeBoundingBox(P(a.mutex), P(a.x), P(a.y), *bx, n)
+    torch.cuda.synchronize()
+    rec["box"] = np.array([float(b.item()) for b in a.box], np.float32)
+    L.BuildQuadTree(P(a.x), P(a.y), P(a.mass), P(a.count), P(a.start), P(a.child), P(a.index),
+                    *bx, n, m)
+    torch.cuda.synchronize()
+    rec["sums"] = (a.x.cpu().numpy(), a.y.cpu().numpy(), a.mass.cpu().numpy())
+    L.ComputeCentreOfMass(P(a.x), P(a.y), P(a.mass), P(a.index), n)
+    L.SortParticles(P(a.count), P(a.start), P(a.sorted), P(a.child), P(a.index), n)
+    L.CalculateForces(P(a.x), P(a.y), P(a.vx), P(a.vy), P(a.ax), P(a.ay), P(a.mass), P(a.sorted),
+                      P(a.child), bx[0], bx[1], n, 1.0)
+    torch.cuda.synchronize()
+    rec["child"] = a.child.cpu().numpy()
+    rec["count"] = a.count.cpu().numpy()
+    rec["start"] = a.start.cpu().numpy()
+    rec["index"] = int(a.index.item())
+    rec["com"] = (a.x.cpu().numpy(), a.y.cpu().numpy(), a.mass.cpu().numpy())
+    rec["sorted"] = a.sorted.cpu().numpy()
+    rec["ax"] = a.ax[:n].cpu().numpy()
+    rec["ay"] = a.ay[:n].cpu().numpy()
+    L.IntegrateParticles(P(a.x), P(a.y), P(a.vx), P(a.vy), P(a.ax), P(a.ay), n, dt, damp)
+    L.FillOutputArray(P(a.x), P(a.y), P(a.out), m)
+    torch.cuda.synchronize()
+    rec["out"] = a.out.cpu().numpy()
+    rec["state"] = tuple(t[:n].cpu().numpy() for t in (a.x, a.y, a.vx, a.vy))
+
+
+@pytest.fixture(scope="module", params=gc.CASES)
+def run(request, L):
+    g = gc.load(request.param)
+    g["name"] = request.param
+    a = RefArrays(g)
+    L.bh_compat_clear_status()
+    rec = {}
+    update(L, a, float(g["dt"]), float(g["damp"]), rec)
+    rec["status1"] = L.bh_compat_status()
+    for _ in range(int(g["steps"]) - 1):
+        update(L, a, float(g["dt"]), float(g["damp"]), {})
+    rec["state3"] = tuple(t[: a.n].cpu().numpy() for t in (a.x, a.y, a.vx, a.vy))
+    rec["status3"] = L.bh_compat_status()
+    return g, rec
+
+
+def test_status_ok(run):
+    _, rec = run
+    assert rec["status1"] == 0 and rec["status3"] == 0
+
+
+def test_box_bit_exact(run):
+    g, rec = run
+    assert np.array_equal(rec["box"].view(np.uint32), g["box"].view(np.uint32))
+
+
+def test_tree_bit_exact(run, oracle):
+    g, rec = run
+    n = int(g["n"])
+    bd, bp, cells, vals = oracle.canonical_from_child(rec["child"], rec["count"], n, rec["com"])
+    assert np.array_equal(bd, g["body_depth"])
+    assert np.array_equal(bp, g["body_path"])
+    assert np.array_equal(cells["level"], g["cell_level"])
+    assert np.array_equal(cells["prefix"], g["cell_prefix"])
+    assert np.array_equal(cells["count"], g["cell_count"])
+    assert rec["index"] - n == int(g["ncells"])
+    box = g["box"]
+    ext = float(max(box[1] - box[0], box[3] - box[2]))
+    tol = 64 * np.finfo(np.float32).eps * ext
+    assert np.max(np.abs(vals[0] - g["cell_cx"])) <= tol
+    assert np.max(np.abs(vals[1] - g["cell_cy"])) <= tol
+    assert np.allclose(vals[2], g["cell_m"], rtol=2e-6, atol=0)
+
+
+def test_sorted_bit_exact(run):
+    g, rec = run
+    n = int(g["n"])
+    assert np.array_equal(rec["sorted"][:n], g["sorted"])
+
+
+def test_forces_and_integration(run):
+    g, rec = run
+    rms = np.sqrt(np.mean(g["ax"].astype(np.float64) ** 2 + g["ay"].astype(np.float64) ** 2))
+    err = np.hypot(rec["ax"] - g["ax"], rec["ay"] - g["ay"]).max() / rms
+    assert err <= FORCE_TOL[g["name"]], err
+    tol = TRAJ_TOL[g["name"]]
+    for a, ref in zip(rec["state"], ("x1", "y1", "vx1", "vy1")):
+        assert np.max(np.abs(a - g[ref])) <= tol * np.abs(g[ref]).max(), ref
+    for a, ref in zip(rec["state3"], ("x3", "y3", "vx3", "vy3")):
+        assert np.max(np.abs(a - g[ref])) <= 3 * tol * np.abs(g[ref]).max(), ref
+
+
+def test_output_buffer(run):
+    _, rec = run
+    x, y = rec["state"][0], rec["state"][1]
+    n = len(x)
+    assert np.array_equal(rec["out"][0:2 * n:2], x)
+    assert np.array_equal(rec["out"][1:2 * n:2], y)
+
+
+def test_debug_invariants(run):
+    """debug.cpp:23-174 on the wrappers' own output."""
+    g, rec = run
+    n = int(g["n"])
+    m = 2 * n + 12000
+    child = rec["child"].astype(np.int64)
+    count = rec["count"]
+    ch = child.reshape(m, 4)
+    kids = np.where(ch[n:] >= 0, count[np.clip(ch[n:], 0, m - 1)], 0).sum(1)
+    assert np.array_equal(kids, count[n:])                                  # COUNT 1
+    assert child[(child >= 0) & (child < n)].sum() == n * (n - 1) // 2     # CHILD 1
+    assert (child < m).all()                                                # CHILD 2
+    assert (child >= -1).all()                                              # CHILD 3
+    s = rec["sorted"][:n]
+    assert np.array_equal(np.sort(s), np.arange(n))                          # SORTED 1, 2
+    assert rec["box"][0] <= rec["box"][1] and rec["box"][2] <= rec["box"][3]  # BOX 1
+    # start[] of every cell is the first sorted position of its bodies
+    st = rec["start"]
+    cells = np.arange(n, rec["index"])
+    assert (st[cells] >= 0).all()
