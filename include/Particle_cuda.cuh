@@ -84,6 +84,27 @@ void bh_compat_clear_status(void);
  * buffers grown on demand on the current device). */
 void bh_compat_release(void);
 
+/* BuildQuadTree for callers that cannot allocate device memory.  No
+ * counterpart in the reference.  Such callers include a host that owns the
+ * whole device-memory budget, a real-time loop that cannot afford an
+ * allocation stall, and code whose allocator the library cannot call.
+ * BuildQuadTree grows a cached workspace with cudaMalloc; this variant calls
+ * no cudaMalloc/cudaFree and no allocating library routine.  Its scratch is
+ * one static device array sized for at most 65536 bodies (about 6 MiB), which
+ * every GPU that loads the library holds until the process exits.
+ *   - Same arguments and outputs as BuildQuadTree.  Returns a BH_* status:
+ *     BH_ERR_CAPACITY for n > 65536 (see bh_last_error), else the build's
+ *     device status.
+ *   - Synchronous: waits on the compat stream before it returns.
+ *   - The first call on a device resolves the array's device address
+ *     (cudaGetSymbolAddress).  Make that first call before any stream capture.
+ *   - All calls share the one array and it keeps the last call's contents.
+ *     Calls that overlap on the GPU (other host threads, other streams) race;
+ *     serialise them. */
+int BuildQuadTreeNoAlloc(float *x, float *y, float *mass, int *count, int *start, int *child,
+                         int *index, float *left, float *right, float *bottom, float *top, int n,
+                         int m);
+
 #ifdef __cplusplus
 }
 #endif

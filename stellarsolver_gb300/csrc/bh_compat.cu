@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cstring>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "Particle_cuda.cuh"
@@ -753,3 +754,174 @@ void CalculateForces(float* x, float* y, float* vx, float* vy, float* ax, float*
 void IntegrateParticles(float* x, float* y, float* vx, float* vy, float* ax, float* ay, int n, float dt, float d) { ssg::compat_IntegrateParticles(x, y, vx, vy, ax, ay, n, dt, d); }
 void FillOutputArray(float* x, float* y, float* out, int n) { ssg::compat_FillOutputArray(x, y, out, n); }
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// BuildQuadTreeNoAlloc: BuildQuadTree for callers that cannot allocate device
+// memory.  Examples: a host that hands the GPU a fixed memory budget and owns
+// every allocation itself, a real-time loop in which a cudaMalloc stall is not
+// acceptable, or code whose allocator is a pool the library cannot reach.
+// The existing wrapper grows a cached workspace with cudaMalloc.  This variant
+// takes its scratch from one file-scope __device__ array instead, sized for at
+// most kNoAllocMaxBodies bodies.  Every GPU that loads the library holds that
+// array (about 6 MiB) until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kNoAllocMaxBodies = 1 << 16;
+
+constexpr size_t na_al(size_t b) { return (b + 255) & ~size_t(255); }
+
+// scratch bytes for n bodies, in the carve order of noalloc_layout()
+constexpr size_t noalloc_bytes(size_t n) {
+    return 2 * na_al(8 * n) + 2 * na_al(4 * n)                    // keys, values (ping-pong)
+           + na_al(4 * 256 * ((n + kSortTile - 1) / kSortTile))  // digit histograms
+           + na_al(4 * 256) + na_al(16) + na_al(8)                // totals, box, system offsets
+           + 8 * na_al(4 * n)                                     // tree arrays + counter
+           + 5 * na_al(4 * n)                                     // node sums
+           + 3 * na_al(4 * n)                                     // gathered x, y, m
+           + 2 * na_al(4 * n)                                     // cells per node, cell base
+           + na_al(4 * ((n + 1023) / 1024)) + na_al(4) + na_al(4);  // block sums, total, status
+}
+
+constexpr size_t kNoAllocBytes = noalloc_bytes(kNoAllocMaxBodies);
+
+}  // namespace
+
+// The scratch itself.  In host code this name is only a stand-in for the
+// device array: its device address comes from cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device, resolved once per
+// device (the first call on a device does this set-up).
+unsigned char* noalloc_scratch(int dev, int* status) {
+    if (dev < 0 || dev >= kNoAllocMaxDevices) {
+        *status = BH_ERR_NO_DEVICE;
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            *status = cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+            return nullptr;
+        }
+        g_noalloc_addr[dev] = static_cast<unsigned char*>(p);
+    }
+    return g_noalloc_addr[dev];
+}
+
+void noalloc_layout(unsigned char* base, size_t n, Workspace* w) {
+    unsigned char* c = base;
+    auto take = [&](size_t b) {
+        void* p = c;
+        c += na_al(b);
+        return p;
+    };
+    const int tiles = (int)((n + kSortTile - 1) / kSortTile);
+    const int nb = (int)((n + 1023) / 1024);
+    w->keys = (uint64_t*)take(8 * n);
+    w->keys_alt = (uint64_t*)take(8 * n);
+    w->vals = (uint32_t*)take(4 * n);
+    w->vals_alt = (uint32_t*)take(4 * n);
+    w->hist = (uint32_t*)take(4 * 256 * (size_t)tiles);
+    w->totals = (uint32_t*)take(4 * 256);
+    w->box_ord = (int*)take(16);
+    w->seg_off = (int*)take(8);
+    w->tree.left = (int*)take(4 * n);
+    w->tree.right = (int*)take(4 * n);
+    w->tree.parent = (int*)take(4 * n);
+    w->tree.leaf_parent = (int*)take(4 * n);
+    w->tree.split = (int*)take(4 * n);
+    w->tree.first = (int*)take(4 * n);
+    w->tree.last = (int*)take(4 * n);
+    w->counter = (int*)take(4 * n);
+    w->sums.m = (float*)take(4 * n);
+    w->sums.mx = (float*)take(4 * n);
+    w->sums.my = (float*)take(4 * n);
+    w->sums.cx = (float*)take(4 * n);
+    w->sums.cy = (float*)take(4 * n);
+    w->sums.quad = nullptr;  // only written in the accuracy modes, never here
+    w->sx = (float*)take(4 * n);
+    w->sy = (float*)take(4 * n);
+    w->sm = (float*)take(4 * n);
+    w->ncell = (int*)take(4 * n);
+    w->cbase = (int*)take(4 * n);
+    w->bsum = (int*)take(4 * (size_t)nb);
+    w->total = (int*)take(4);
+    w->status = (int*)take(4);
+    w->tiles = tiles;
+}
+
+}  // namespace
+
+extern "C" int BuildQuadTreeNoAlloc(float* x, float* y, float* mass, int* count, int* start,
+                                    int* child, int* index, float* left, float* right,
+                                    float* bottom, float* top, int n, int m) {
+    if (n < 1 || m < n) return BH_ERR_ARG;
+    if (n > kNoAllocMaxBodies) {
+        g_last_error = "BuildQuadTreeNoAlloc: n = " + std::to_string(n) +
+                       " exceeds the static scratch limit of " +
+                       std::to_string(kNoAllocMaxBodies) + " bodies";
+        return BH_ERR_CAPACITY;
+    }
+    if (n == 1) return BH_OK;  // a lone body: no cells, *index stays n
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    int st_code = BH_OK;
+    unsigned char* base = noalloc_scratch(dev, &st_code);
+    if (!base) return st_code;
+    Workspace w;
+    noalloc_layout(base, (size_t)n, &w);
+    cudaStream_t st = g_set.stream;
+    // the array keeps the previous call's contents: clear what must start at zero
+    e = cudaMemsetAsync(w.status, 0, sizeof(int), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(w.counter, 0, sizeof(int) * n, st);
+    if (e != cudaSuccess) return cuda_fail(e, "BuildQuadTreeNoAlloc memset");
+    const int nb = blocks_for(n, 256);
+    k_c_box_to_ord<<<1, 1, 0, st>>>(left, right, bottom, top, w.box_ord, w.seg_off, n);
+    Segs segs{1, w.seg_off, nullptr};
+    k_keys<<<nb, 256, 0, st>>>(x, y, n, segs, w.box_ord, w.keys, w.vals);
+    uint64_t *ka = w.keys, *kb = w.keys_alt;
+    uint32_t *va = w.vals, *vb = w.vals_alt;
+    const int tiles = w.tiles;
+    for (int ps = 0; ps < 8; ++ps) {
+        k_radix_hist<<<tiles, kSortThreads, 0, st>>>(ka, va, n, 8 * ps, 0, nullptr, w.hist, tiles);
+        k_radix_scan<<<256, kSortThreads, 0, st>>>(w.hist, tiles, w.totals);
+        k_radix_scatter<<<tiles, kSortThreads, 0, st>>>(ka, va, kb, vb, n, 8 * ps, 0, nullptr,
+                                                        w.hist, w.totals, tiles);
+        std::swap(ka, kb);
+        std::swap(va, vb);
+    }
+    k_c_gather3<<<nb, 256, 0, st>>>(n, va, x, y, mass, w.sx, w.sy, w.sm);
+    k_build<<<nb, 256, 0, st>>>(ka, n, segs, w.tree, w.status);
+    k_moments<<<nb, 256, 0, st>>>(n, 0, w.sx, w.sy, w.sm, w.tree.left, w.tree.right,
+                                  w.tree.parent, w.tree.leaf_parent, w.counter, w.sums);
+    k_c_ncells<<<nb, 256, 0, st>>>(n, w.tree.split, w.tree.parent, w.ncell);
+    const int sb = blocks_for(n, 1024);
+    k_c_scan_block<<<sb, 1024, 0, st>>>(w.ncell, w.cbase, w.bsum, n);
+    k_c_scan_top<<<1, 1024, 0, st>>>(w.bsum, sb, w.total);
+    k_c_scan_add<<<nb, 256, 0, st>>>(w.cbase, w.bsum, n);
+    k_c_materialize<<<nb, 256, 0, st>>>(n, m, w.tree, ka, va, w.cbase, w.total, w.sums, child,
+                                        count, start, x, y, mass, index, w.status);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "BuildQuadTreeNoAlloc launch");
+    // wait for this build and return its device status (the scratch is shared:
+    // the next call may overwrite it as soon as this one returns)
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "BuildQuadTreeNoAlloc sync");
+    int bits = 0;
+    e = cudaMemcpy(&bits, w.status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "BuildQuadTreeNoAlloc status");
+    if (bits & ST_DUP) return BH_ERR_DUPLICATE_KEYS;
+    if (bits & ST_CAPACITY) return BH_ERR_CAPACITY;
+    if (bits & ST_NONFINITE) return BH_ERR_NONFINITE;
+    return BH_OK;
+}

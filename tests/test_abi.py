@@ -13,11 +13,14 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def declared_functions():
     names = set()
-    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+    for h in sorted(glob.glob(os.path.join(ROOT, "include", "*.h")) +
+                    glob.glob(os.path.join(ROOT, "include", "*.cuh"))):
         text = open(h).read()
         text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
         text = re.sub(r"//[^\n]*", "", text)
-        for m in re.finditer(r"\b(bh_[a-z0-9_]+)\s*\(", text):
+        # every function declared at file scope: "<type> [*]name(" at a line start
+        for m in re.finditer(r"^(?:const\s+)?(?:void|int|char|float|double)\s*\**\s*([A-Za-z_]\w*)\s*\(",
+                             text, flags=re.M):
             names.add(m.group(1))
     return sorted(names)
 
@@ -34,7 +37,10 @@ def lib():
 def test_header_declares_the_boundary():
     names = declared_functions()
     for required in ("bh_create", "bh_destroy", "bh_set_state", "bh_get_state", "bh_step",
-                     "bh_sync", "bh_get_accel", "bh_default_params"):
+                     "bh_sync", "bh_get_accel", "bh_default_params", "ResetArrays",
+                     "ComputeBoundingBox", "BuildQuadTree", "ComputeCentreOfMass",
+                     "SortParticles", "CalculateForces", "IntegrateParticles", "FillOutputArray",
+                     "SetDrawArray"):
         assert required in names
 
 
