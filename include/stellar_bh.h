@@ -165,6 +165,17 @@ int bh_direct_sum_f64(bh_system* s, int ns, const int* idx, double* ax, double* 
  * walk.  device -1 = current.  No reference counterpart. */
 int bh_measure_fp32_peak(int device, double* tflops);
 
+/* The reference's initial conditions, number for number: the Model enum of
+ * SimulationParameters.h:8-13 and the generators of
+ * BarnesHutParticleSystem.cpp:390-560 (std::default_random_engine, default
+ * seed).  Host arrays of n floats; accelerations start at zero.  gravity
+ * enters the disk velocities only, as in the reference. */
+#define BH_MODEL_DISK 0
+#define BH_MODEL_COLLIDING_DISKS 1
+#define BH_MODEL_PLUMMER 2
+int bh_initial_conditions(int model, int n, float gravity, float* mass, float* x, float* y,
+                          float* vx, float* vy);
+
 /* Human-readable text for a status code, and the last CUDA error seen by the
  * library in this thread. */
 const char* bh_status_string(int status);

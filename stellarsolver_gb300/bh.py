@@ -85,6 +85,7 @@ def lib() -> ctypes.CDLL:
     L.bh_step_profiled.argtypes = [vp, vp, vp]
     L.bh_direct_sum_f64.argtypes = [vp, i32, vp, vp, vp]
     L.bh_measure_fp32_peak.argtypes = [i32, P(ctypes.c_double)]
+    L.bh_initial_conditions.argtypes = [i32, i32, ctypes.c_float] + [vp] * 5
     L.bh_status_string.argtypes = [i32]
     L.bh_status_string.restype = ctypes.c_char_p
     L.bh_last_error.restype = ctypes.c_char_p
@@ -115,6 +116,19 @@ def _f32(a):
 
 def _p(a):
     return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+REFERENCE_MODELS = {"disk": 0, "colliding-disks": 1, "plummer": 2}
+
+
+def reference_initial_conditions(model: str, n: int, gravity: float = 1.0):
+    """The reference's -disk/-plummer/-colliding-disks initial conditions
+    (host arrays x, y, vx, vy, m), generated by the library."""
+    out = [np.empty(n, np.float32) for _ in range(5)]  # m, x, y, vx, vy
+    _check(lib().bh_initial_conditions(REFERENCE_MODELS[model], n, gravity, *[_p(a) for a in out]),
+           "bh_initial_conditions")
+    m, x, y, vx, vy = out
+    return x, y, vx, vy, m
 
 
 def measure_fp32_peak(device: int = -1) -> float:

@@ -23,8 +23,10 @@ APP = os.path.join(LIB_DIR, "stellar_app")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# -ffp-contract=off applies to host code only (device contraction is nvcc's --fmad):
+# the reference's initial conditions must round the same on x86 and Arm hosts.
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
-              "-I" + INCLUDE, "-I" + CSRC]
+              "-Xcompiler", "-ffp-contract=off", "-I" + INCLUDE, "-I" + CSRC]
 
 
 def nvcc() -> str:
@@ -62,7 +64,8 @@ def build(verbose: bool = False) -> str:
     _run([nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs)
     host_srcs = _sources(HOST, (".cpp",))
     if host_srcs:
-        _run([nvcc()] + ARCH + ["-O2", "-std=c++17", "-I" + INCLUDE, "-I" + HOST, "-o", APP]
+        _run([nvcc()] + ARCH + ["-O2", "-std=c++17", "-Xcompiler", "-ffp-contract=off",
+                                "-I" + INCLUDE, "-I" + HOST, "-o", APP]
              + host_srcs + ["-L" + LIB_DIR, "-lstellar_bh", "-Xlinker", "-rpath=$ORIGIN"])
     if verbose:
         print(f"built {LIB}")
