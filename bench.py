@@ -41,7 +41,7 @@ EPS = 0.01
 DT = 1e-4
 THETA = 0.5
 FLOPS_PER_INTERACTION = 14  # dx,dy 2; r^2 4; rsqrt 1; r^-3 2; m*r^-3 1; two FMAs 4
-LAUNCHES_PER_STEP = 31       # bbox 1, keys 1, sort 8x3, reorder 1, build 1, moments 1, records 1, walk 1
+LAUNCHES_PER_STEP = 32       # bbox, keys, sort 8 x (hist, scan, scatter), reorder, build, moments, records, walk x2
 
 
 def peaks():
@@ -59,11 +59,10 @@ def phase_bytes(n, mixed, passes=8):
     return {
         "bbox": 8 * n,
         "keys": 20 * n,
-        "sort": 24 * n * passes,
+        "sort": 24 * n * passes,  # one read + one write of (key, index) per pass
         "reorder": 52 * n + lo,
         "build": 36 * n,
-        "moments": 68 * n,
-        "records": 108 * n,
+        "moments": 68 * n + 108 * n,  # sums, then walk records (two kernels)
     }
 
 

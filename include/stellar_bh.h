@@ -81,6 +81,9 @@ typedef struct bh_stats {
     int32_t max_depth;     /* deepest leaf level */
     int32_t status;        /* sticky device status (BH_* code) */
     float box[4];          /* left, right, bottom, top of the last step */
+    int32_t max_stack;     /* deepest walk stack of the last step (PLAIN/MIXED) */
+    int32_t walk_rounds;   /* warp rounds of node tests in the last step (PLAIN/MIXED) */
+    int32_t nodes_tested;  /* nodes tested by the walk in the last step (PLAIN/MIXED) */
 } bh_stats;
 
 /* Fill p with the reference's defaults: mode REFERENCE, theta 0.5, eps2 0.025,
@@ -146,7 +149,8 @@ int bh_get_stats(bh_system* s, bh_stats* out, void* stream);
 int bh_get_debug(bh_system* s, const char* name, void* host_out, size_t bytes, void* stream);
 
 /* Phases timed by bh_step_profiled, in order. */
-#define BH_NUM_PHASES 8 /* bbox, keys, sort, reorder, build, moments, records, walk */
+#define BH_NUM_PHASES 8 /* bbox, keys, sort, reorder, build, moments and walk records,
+                          bootstrap (accuracy modes, first step after bh_set_state), walk */
 
 /* One step (never graph-replayed) with CUDA events at the phase boundaries;
  * synchronises, then ADDS each phase's milliseconds to phase_ms[0..7].

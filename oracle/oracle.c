@@ -507,9 +507,11 @@ void orc_energy_f64(int n, const float* x, const float* y, const float* vx, cons
  * the reference has one monopole walk).  Checks the GPU walk and its opening
  * rule against the FP64 direct sum.  Per group of 32 consecutive sorted
  * bodies, a node is approximated by its quadrupole expansion iff
- *   geometric: min_j |COM - p_j| > l/theta + |COM - cell centre|
- *              (l = larger side of the node's cell), and
- *   relative : G M l^3 <= alpha * a_g * d^5, d = that minimum distance,
+ *   geometric: d > l/theta + |COM - cell centre|, where d is the distance
+ *              from the COM to the group's box when that already decides
+ *              (box distance > r, or box distance + box diagonal <= r), else
+ *              min_j |COM - p_j| (l = larger side of the node's cell), and
+ *   relative : G M l^3 <= alpha * a_g * d^5 with the same d,
  *              a_g = max(min_j |a_old_j|, 0.1 * mean_j |a_old_j|)
  *              (skipped when aold == NULL or alpha <= 0);
  * otherwise a node of <= bucket bodies interacts body by body and a larger
@@ -610,22 +612,37 @@ int64_t orc_walk_acc(int n, const float* sx, const float* sy, const float* sm,
                 amean /= (float)cnt;
                 aa = alpha * fmaxf(amin, 0.1f * amean);
             }
+            float gx0 = sx[g0], gx1 = sx[g0], gy0 = sy[g0], gy1 = sy[g0];
             for (int k = 0; k < cnt; ++k) {
                 px[k] = sx[g0 + k];
                 py[k] = sy[g0 + k];
                 ax[k] = ay[k] = 0.0f;
+                gx0 = fminf(gx0, px[k]);
+                gx1 = fmaxf(gx1, px[k]);
+                gy0 = fminf(gy0, py[k]);
+                gy1 = fmaxf(gy1, py[k]);
             }
+            const float gdiag = sqrtf((gx1 - gx0) * (gx1 - gx0) + (gy1 - gy0) * (gy1 - gy0));
             int64_t entries = 0;
             int top = 0;
             stack[top++] = 0;
             while (top > 0) {
                 int32_t node = stack[--top];
                 float cx = mom[node].cx, cy = mom[node].cy;
-                float d2 = INFINITY;
-                for (int k = 0; k < cnt; ++k) {
-                    float dx = px[k] - cx, dy = py[k] - cy;
-                    float q = dx * dx + dy * dy;
-                    d2 = q < d2 ? q : d2;
+                /* group-box lower bound; exact minimum only when inconclusive */
+                float ddx = fmaxf(fmaxf(gx0 - cx, cx - gx1), 0.0f);
+                float ddy = fmaxf(fmaxf(gy0 - cy, cy - gy1), 0.0f);
+                float d2 = ddx * ddx + ddy * ddy;
+                if (d2 <= ropen2[node]) {
+                    float reach = sqrtf(d2) + gdiag;
+                    if (reach * reach > ropen2[node]) {
+                        d2 = INFINITY;
+                        for (int k = 0; k < cnt; ++k) {
+                            float dx = px[k] - cx, dy = py[k] - cy;
+                            float q = dx * dx + dy * dy;
+                            d2 = q < d2 ? q : d2;
+                        }
+                    }
                 }
                 int accept = d2 > ropen2[node];
                 if (accept && relative) accept = qerr[node] <= aa * d2 * d2 * sqrtf(d2);

@@ -16,7 +16,7 @@ import numpy as np
 from . import build as _build
 
 MODES = {"reference": 0, "plain": 1, "mixed": 2}
-PHASES = ("bbox", "keys", "sort", "reorder", "build", "moments", "records", "walk")
+PHASES = ("bbox", "keys", "sort", "reorder", "build", "moments", "bootstrap", "walk")
 PHASES_N = len(PHASES)
 
 BH_OK = 0
@@ -45,7 +45,9 @@ class Params(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [("interactions", ctypes.c_int64), ("cells", ctypes.c_int32),
                 ("nodes", ctypes.c_int32), ("max_depth", ctypes.c_int32),
-                ("status", ctypes.c_int32), ("box", ctypes.c_float * 4)]
+                ("status", ctypes.c_int32), ("box", ctypes.c_float * 4),
+                ("max_stack", ctypes.c_int32), ("walk_rounds", ctypes.c_int32),
+                ("nodes_tested", ctypes.c_int32)]
 
 
 _lib = None
@@ -237,7 +239,7 @@ class BarnesHutSystem:
     def step_profiled(self, phase_ms: np.ndarray, stream=None):
         """One non-graph step with events at the phase boundaries; adds each
         phase's milliseconds to phase_ms (float32[8]: bbox, keys, sort,
-        reorder, build, moments, records, walk)."""
+        reorder, build, moments with the walk records, bootstrap, walk)."""
         assert phase_ms.dtype == np.float32 and phase_ms.shape == (PHASES_N,)
         _check(lib().bh_step_profiled(self._h, stream, _p(phase_ms)), "bh_step_profiled")
 
@@ -257,7 +259,9 @@ class BarnesHutSystem:
         s = Stats()
         _check(lib().bh_get_stats(self._h, ctypes.byref(s), stream), "bh_get_stats")
         return dict(interactions=int(s.interactions), cells=int(s.cells), nodes=int(s.nodes),
-                    max_depth=int(s.max_depth), status=int(s.status), box=np.array(s.box[:]))
+                    max_depth=int(s.max_depth), status=int(s.status), box=np.array(s.box[:]),
+                    max_stack=int(s.max_stack), walk_rounds=int(s.walk_rounds),
+                    nodes_tested=int(s.nodes_tested))
 
     def debug(self, name: str):
         n = self.n

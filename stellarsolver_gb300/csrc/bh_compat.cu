@@ -671,8 +671,9 @@ void compat_BuildQuadTree(float* x, float* y, float* mass, int* count, int* star
     k_c_gather3<<<nb, 256, 0, st>>>(n, va, x, y, mass, w->sx, w->sy, w->sm);
     k_build<<<nb, 256, 0, st>>>(ka, n, segs, w->tree, w->status);
     record_cuda(cudaMemsetAsync(w->counter, 0, sizeof(int) * n, st), "BuildQuadTree memset");
-    k_moments<<<nb, 256, 0, st>>>(n, 0, w->sx, w->sy, w->sm, w->tree.left, w->tree.right,
-                                  w->tree.parent, w->tree.leaf_parent, w->counter, w->sums);
+    k_moments<256><<<nb, 256, 0, st>>>(n, 0, w->sx, w->sy, w->sm, w->tree.left, w->tree.right,
+                                       w->tree.parent, w->tree.leaf_parent, w->tree.first,
+                                       w->tree.last, w->counter, w->sums);
     k_c_ncells<<<nb, 256, 0, st>>>(n, w->tree.split, w->tree.parent, w->ncell);
     const int sb = blocks_for(n, 1024);
     k_c_scan_block<<<sb, 1024, 0, st>>>(w->ncell, w->cbase, w->bsum, n);
@@ -902,8 +903,9 @@ extern "C" int BuildQuadTreeNoAlloc(float* x, float* y, float* mass, int* count,
     }
     k_c_gather3<<<nb, 256, 0, st>>>(n, va, x, y, mass, w.sx, w.sy, w.sm);
     k_build<<<nb, 256, 0, st>>>(ka, n, segs, w.tree, w.status);
-    k_moments<<<nb, 256, 0, st>>>(n, 0, w.sx, w.sy, w.sm, w.tree.left, w.tree.right,
-                                  w.tree.parent, w.tree.leaf_parent, w.counter, w.sums);
+    k_moments<256><<<nb, 256, 0, st>>>(n, 0, w.sx, w.sy, w.sm, w.tree.left, w.tree.right,
+                                       w.tree.parent, w.tree.leaf_parent, w.tree.first,
+                                       w.tree.last, w.counter, w.sums);
     k_c_ncells<<<nb, 256, 0, st>>>(n, w.tree.split, w.tree.parent, w.ncell);
     const int sb = blocks_for(n, 1024);
     k_c_scan_block<<<sb, 1024, 0, st>>>(w.ncell, w.cbase, w.bsum, n);

@@ -475,47 +475,79 @@ __device__ __forceinline__ ChildVals load_child(int c, const float* __restrict__
     return v;
 }
 
+__device__ __forceinline__ void combine_node(int p, int accuracy, const float* __restrict__ sx,
+                                             const float* __restrict__ sy,
+                                             const float* __restrict__ sm,
+                                             const int* __restrict__ left,
+                                             const int* __restrict__ right, const NodeSums& ns) {
+    ChildVals a = load_child(left[p], sx, sy, sm, ns, accuracy);
+    ChildVals b = load_child(right[p], sx, sy, sm, ns, accuracy);
+    float M = __fadd_rn(a.m, b.m);
+    float MX = __fadd_rn(a.mx, b.mx);
+    float MY = __fadd_rn(a.my, b.my);
+    float cx, cy;
+    if (!accuracy) {
+        cx = __fdiv_rn(MX, M);
+        cy = __fdiv_rn(MY, M);
+    } else {
+        float w = M > 0.0f ? b.m / M : 0.5f;
+        cx = fmaf(w, b.cx - a.cx, a.cx);
+        cy = fmaf(w, b.cy - a.cy, a.cy);
+        float ax = a.cx - cx, ay = a.cy - cy, bx = b.cx - cx, by = b.cy - cy;
+        float sxx = a.sxx + b.sxx + a.m * ax * ax + b.m * bx * bx;
+        float sxy = a.sxy + b.sxy + a.m * ax * ay + b.m * bx * by;
+        float syy = a.syy + b.syy + a.m * ay * ay + b.m * by * by;
+        ns.quad[p] = make_float4(sxx, sxy, syy, 0.0f);
+    }
+    ns.m[p] = M;
+    ns.mx[p] = MX;
+    ns.my[p] = MY;
+    ns.cx[p] = cx;
+    ns.cy[p] = cy;
+}
+
 // Bottom-up: each body climbs from its leaf; the second thread to reach a node
 // combines both children (left + right, so the sums do not depend on which
 // thread arrives last) and continues.  REFERENCE mode keeps the reference's
 // definition com = (sum m*x) / (sum m) (kernels.cu:283-284); accuracy modes
 // combine centres relative to each other and add second moments.
-static __global__ void k_moments(int n, int accuracy, const float* __restrict__ sx,
-                          const float* __restrict__ sy, const float* __restrict__ sm,
-                          const int* __restrict__ left, const int* __restrict__ right,
-                          const int* __restrict__ parent, const int* __restrict__ leaf_parent,
-                          int* __restrict__ counter, NodeSums ns) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
+//
+// A warp owns 32 consecutive leaves.  A node whose body range lies inside its
+// warp's 32 leaves is reached only by lanes of that warp: its arrival counter
+// lives in shared memory and block-scope fences order the child data.  Only
+// nodes that span two warps' leaves use a global counter and device-scope
+// fences.
+template <int THREADS>
+static __global__ void __launch_bounds__(THREADS) k_moments(int n, int accuracy, const float* __restrict__ sx,
+                                                     const float* __restrict__ sy,
+                                                     const float* __restrict__ sm,
+                                                     const int* __restrict__ left,
+                                                     const int* __restrict__ right,
+                                                     const int* __restrict__ parent,
+                                                     const int* __restrict__ leaf_parent,
+                                                     const int* __restrict__ first,
+                                                     const int* __restrict__ last,
+                                                     int* __restrict__ counter, NodeSums ns) {
+    __shared__ int s_cnt[THREADS];
+    const int j = blockIdx.x * THREADS + threadIdx.x;
+    s_cnt[threadIdx.x] = 0;
+    __syncwarp();
     if (j >= n) return;
+    const int c0 = j & ~31;  // this warp's leaves: [c0, c0 + 32)
+    int* wcnt = s_cnt + (threadIdx.x & ~31);
     int p = leaf_parent[j];
     while (p >= 0) {
-        __threadfence();
-        if (atomicAdd(counter + p, 1) == 0) return;
-        __threadfence();
-        ChildVals a = load_child(left[p], sx, sy, sm, ns, accuracy);
-        ChildVals b = load_child(right[p], sx, sy, sm, ns, accuracy);
-        float M = __fadd_rn(a.m, b.m);
-        float MX = __fadd_rn(a.mx, b.mx);
-        float MY = __fadd_rn(a.my, b.my);
-        float cx, cy;
-        if (!accuracy) {
-            cx = __fdiv_rn(MX, M);
-            cy = __fdiv_rn(MY, M);
+        const bool local = first[p] >= c0 && last[p] < c0 + 32;
+        if (local) {
+            __threadfence_block();
+            if (atomicAdd(wcnt + (p - c0), 1) == 0) return;
+            __threadfence_block();
         } else {
-            float w = M > 0.0f ? b.m / M : 0.5f;
-            cx = fmaf(w, b.cx - a.cx, a.cx);
-            cy = fmaf(w, b.cy - a.cy, a.cy);
-            float ax = a.cx - cx, ay = a.cy - cy, bx = b.cx - cx, by = b.cy - cy;
-            float sxx = a.sxx + b.sxx + a.m * ax * ax + b.m * bx * bx;
-            float sxy = a.sxy + b.sxy + a.m * ax * ay + b.m * bx * by;
-            float syy = a.syy + b.syy + a.m * ay * ay + b.m * by * by;
-            ns.quad[p] = make_float4(sxx, sxy, syy, 0.0f);
+            __threadfence();
+            if (atomicAdd(counter + p, 1) == 0) return;
+            __threadfence();
         }
-        ns.m[p] = M;
-        ns.mx[p] = MX;
-        ns.my[p] = MY;
-        ns.cx[p] = cx;
-        ns.cy[p] = cy;
+        combine_node(p, accuracy, sx, sy, sm, left, right, ns);
         p = parent[p];
     }
 }
@@ -535,6 +567,17 @@ struct Records {
     int4* D;    // first body, body count, bits of G*M*l^3 (accuracy), 0
 };
 
+// Every other bit of x (bits 0, 2, 4, ...) packed into the low 32 bits.
+__device__ __forceinline__ uint64_t compact_even_bits(uint64_t x) {
+    x &= 0x5555555555555555ull;
+    x = (x | (x >> 1)) & 0x3333333333333333ull;
+    x = (x | (x >> 2)) & 0x0f0f0f0f0f0f0f0full;
+    x = (x | (x >> 4)) & 0x00ff00ff00ff00ffull;
+    x = (x | (x >> 8)) & 0x0000ffff0000ffffull;
+    x = (x | (x >> 16)) & 0x00000000ffffffffull;
+    return x;
+}
+
 // dp_L = w_L^2/theta with w_L the level-L cell width from the x extent only:
 // radius = (right-left)*0.5 (kernels.cu:349), root children pushed with
 // radius^2/theta (:376), times 0.25 per level (:395).  Cells at level <= 1 are
@@ -546,62 +589,67 @@ __device__ __forceinline__ float ref_dp(Box bx, float theta, int level) {
     return ldexpf(dp1, -2 * (level - 1));
 }
 
-static __global__ void k_records(int n, Segs segs, int accuracy, float theta, float G,
-                          const int* __restrict__ box_ord, const uint64_t* __restrict__ skeys,
-                          const int* __restrict__ left, const int* __restrict__ right,
-                          const int* __restrict__ parent, const int* __restrict__ split,
-                          const int* __restrict__ first, const int* __restrict__ last,
-                          NodeSums ns, Records rec) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int sp = split[i];
-    if (sp < 0) return;  // unused slot
-    int pa = parent[i];
-    if (pa >= 0 && merged_into(sp, split[pa])) return;  // folded into its parent
+
+// Walk record of branching node i, from its sums and the tree (the body of
+// k_records).
+__device__ __forceinline__ void emit_record(int i, int sp, int accuracy, float theta, float G,
+                                            const int* __restrict__ box_ord, int seg,
+                                            const uint64_t* __restrict__ skeys,
+                                            const TreePtrs& t, float M, float cx, float cy,
+                                            float4 quad, Records rec) {
     int ch[4] = {kNoChild, kNoChild, kNoChild, kNoChild};
     int nc = 0;
-    int lr[2] = {left[i], right[i]};
+    const int lr[2] = {t.left[i], t.right[i]};
 #pragma unroll
-    for (int s = 0; s < 2; ++s) {
-        int c = lr[s];
-        if (c >= 0 && merged_into(split[c], sp)) {
-            ch[nc++] = left[c];
-            ch[nc++] = right[c];
+    for (int s2 = 0; s2 < 2; ++s2) {
+        const int c = lr[s2];
+        if (c >= 0 && merged_into(t.split[c], sp)) {
+            ch[nc++] = t.left[c];
+            ch[nc++] = t.right[c];
         } else {
             ch[nc++] = c;
         }
     }
     rec.C[i] = make_int4(ch[0], ch[1], ch[2], ch[3]);
-    int f = first[i], cnt = last[i] - f + 1;
-    int level = sp >> 1;
-    Box bx = load_box(box_ord, seg_of(segs, i));
-    float cx = ns.cx[i], cy = ns.cy[i], M = ns.m[i];
+    const int f = t.first[i], cnt = t.last[i] - f + 1;
+    const int level = sp >> 1;
+    const Box bx = load_box(box_ord, seg);
     if (!accuracy) {
         rec.A[i] = make_float4(cx, cy, M, ref_dp(bx, theta, level));
         rec.D[i] = make_int4(f, cnt, 0, 0);
         return;
     }
-    // cell rectangle of the node's level from its key prefix (x bit 1 = left half)
-    int L = level < 32 ? level : 32;
-    uint64_t pre = L > 0 ? skeys[f] >> (64 - 2 * L) : 0ull;
-    unsigned long long ix = 0, iy = 0;
-    for (int q = L - 1; q >= 0; --q) {
-        unsigned dgt = (unsigned)(pre >> (2 * q)) & 3u;
-        ix = (ix << 1) | ((dgt & 1u) ? 0ull : 1ull);
-        iy = (iy << 1) | ((dgt & 2u) ? 0ull : 1ull);
-    }
-    // FP64 for the extent of the cell (the box may be far from the origin)
-    double wx = ((double)bx.r - (double)bx.l), wy = ((double)bx.t - (double)bx.b);
-    double scale = ldexp(1.0, -L);
-    double x0 = bx.l + wx * scale * (double)ix, y0 = bx.b + wy * scale * (double)iy;
-    double l = fmax(wx, wy) * scale;
-    double ddx = cx - (x0 + 0.5 * wx * scale), ddy = cy - (y0 + 0.5 * wy * scale);
-    double r = l / (double)theta + sqrt(ddx * ddx + ddy * ddy);  // l/theta + |COM - centre|
-    rec.A[i] = make_float4(cx, cy, M, (float)(r * r));
-    float qerr = (float)((double)G * (double)M * l * l * l);     // G M l^3 (relative rule)
+    const int L = level < 32 ? level : 32;
+    const uint64_t pre = L > 0 ? skeys[f] >> (64 - 2 * L) : 0ull;
+    const uint64_t mask = L > 0 ? (~0ull >> (64 - L)) : 0ull;
+    const uint64_t ix = ~compact_even_bits(pre) & mask;
+    const uint64_t iy = ~compact_even_bits(pre >> 1) & mask;
+    const float scale = ldexpf(1.0f, -L);
+    const float wx = bx.r - bx.l, wy = bx.t - bx.b;
+    const float l = fmaxf(wx, wy) * scale;
+    const double hs = 0.5 * (double)scale;
+    const double ddx = (double)cx - ((double)bx.l + (double)wx * ((double)ix * (double)scale + hs));
+    const double ddy = (double)cy - ((double)bx.b + (double)wy * ((double)iy * (double)scale + hs));
+    const float delta = sqrtf((float)(ddx * ddx + ddy * ddy));
+    const float r = l / theta + delta;
+    rec.A[i] = make_float4(cx, cy, M, r * r);
+    const float qerr = G * M * l * l * l;
     rec.D[i] = make_int4(f, cnt, __float_as_int(qerr), 0);
-    float4 q = ns.quad[i];  // S about the centre of mass -> T = 3S, h = 1.5 tr S
-    rec.B[i] = make_float4(3.0f * q.x, 3.0f * q.y, 3.0f * q.z, 1.5f * (q.x + q.z));
+    rec.B[i] = make_float4(3.0f * quad.x, 3.0f * quad.y, 3.0f * quad.z, 1.5f * (quad.x + quad.z));
+}
+
+static __global__ void k_records(int n, Segs segs, int accuracy, float theta, float G,
+                                 const int* __restrict__ box_ord, const uint64_t* __restrict__ skeys,
+                                 TreePtrs t, NodeSums ns, Records rec) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int sp = t.split[i];
+    if (sp < 0) return;  // unused slot
+    const int pa = t.parent[i];
+    if (pa >= 0 && merged_into(sp, t.split[pa])) return;  // folded into its parent
+    const float4 q = accuracy ? ns.quad[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    emit_record(i, sp, accuracy, theta, G, box_ord, seg_of(segs, i), skeys, t, ns.m[i], ns.cx[i],
+                ns.cy[i], q, rec);
 }
 
 }  // namespace ssg

@@ -38,7 +38,7 @@ namespace {
 
 constexpr int kWalkWarps = 8;
 constexpr int kRefStack = 256;
-constexpr int kAccStack = 1024;
+constexpr int kAccStack = 768;  // deepest measured: 670 (2D Plummer, N = 2^24)
 constexpr int kBboxThreads = 256;
 constexpr int kBboxChunk = 8192;
 
@@ -86,32 +86,40 @@ cudaError_t init_walk_attributes() {
 }
 
 template <int BUCKET, bool MIXED>
-static cudaError_t launch_acc(const StepArgs& a, cudaStream_t st) {
+static cudaError_t launch_acc(const StepArgs& a, cudaStream_t st, int part) {
     using Sm = AccSmem<kWalkWarps, kAccStack, BUCKET>;
     int grid = std::min(a.walk_grid_acc, (a.groups.ngroups + kWalkWarps - 1) / kWalkWarps);
     if (grid < 1) grid = 1;
-    // bootstrap pass: exits at once unless bh_set_state left the state fresh
-    k_walk_acc<kWalkWarps, kAccStack, BUCKET, false, true><<<grid, kWalkWarps * 32, sizeof(Sm), st>>>(
-        a.segs, a.groups, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt, a.alpha,
-        a.out, a.status, a.inter, a.work + 1, a.fresh);
-    k_walk_acc<kWalkWarps, kAccStack, BUCKET, MIXED, false><<<grid, kWalkWarps * 32, sizeof(Sm), st>>>(
-        a.segs, a.groups, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt, a.alpha,
-        a.out, a.status, a.inter, a.work + 2, a.fresh);
+    if (part == 0) {
+        // bootstrap pass: exits at once unless bh_set_state left the state fresh
+        k_walk_acc<kWalkWarps, kAccStack, BUCKET, false, true>
+            <<<grid, kWalkWarps * 32, sizeof(Sm), st>>>(
+                a.segs, a.groups, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt,
+                a.alpha, a.out, a.status, a.inter, a.work + 1, a.fresh, a.max_stack);
+    } else {
+        k_walk_acc<kWalkWarps, kAccStack, BUCKET, MIXED, false>
+            <<<grid, kWalkWarps * 32, sizeof(Sm), st>>>(
+                a.segs, a.groups, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt,
+                a.alpha, a.out, a.status, a.inter, a.work + 2, a.fresh, a.max_stack);
+    }
     return cudaGetLastError();
 }
 
 template <bool MIXED>
-static cudaError_t launch_acc_bucket(const StepArgs& a, cudaStream_t st) {
+static cudaError_t launch_acc_bucket(const StepArgs& a, cudaStream_t st, int part) {
     switch (a.bucket) {
-        case 1: return launch_acc<1, MIXED>(a, st);
-        case 4: return launch_acc<4, MIXED>(a, st);
-        case 16: return launch_acc<16, MIXED>(a, st);
-        default: return launch_acc<8, MIXED>(a, st);
+        case 1: return launch_acc<1, MIXED>(a, st, part);
+        case 4: return launch_acc<4, MIXED>(a, st, part);
+        case 16: return launch_acc<16, MIXED>(a, st, part);
+        default: return launch_acc<8, MIXED>(a, st, part);
     }
 }
 
-cudaError_t launch_walk(const StepArgs& a, cudaStream_t st) {
+// part 0: the accuracy modes' bootstrap pass (nothing in REFERENCE mode);
+// part 1: the walk.
+cudaError_t launch_walk(const StepArgs& a, cudaStream_t st, int part) {
     if (a.mode == BH_MODE_REFERENCE) {
+        if (part == 0) return cudaSuccess;
         int grid = std::min(a.walk_grid_ref, (a.groups.ngroups + kWalkWarps - 1) / kWalkWarps);
         if (grid < 1) grid = 1;
         k_walk_ref<kWalkWarps, kRefStack><<<grid, kWalkWarps * 32, 0, st>>>(
@@ -119,8 +127,8 @@ cudaError_t launch_walk(const StepArgs& a, cudaStream_t st) {
             a.work);
         return cudaGetLastError();
     }
-    return a.mode == BH_MODE_MIXED ? launch_acc_bucket<true>(a, st)
-                                   : launch_acc_bucket<false>(a, st);
+    return a.mode == BH_MODE_MIXED ? launch_acc_bucket<true>(a, st, part)
+                                   : launch_acc_bucket<false>(a, st, part);
 }
 
 int normalized_bucket(int b) {
@@ -165,7 +173,7 @@ struct bh_system {
     float *ax = nullptr, *ay = nullptr;
     int* status = nullptr;
     unsigned long long* inter = nullptr;
-    int* work = nullptr;   // 3 dynamic-scheduling counters, reset every step
+    int* work = nullptr;   // 3 scheduling counters, walk stack peak, rounds, tests; reset every step
     int* fresh = nullptr;  // 1 after bh_set_state: bootstrap |a_old| in the next step
     int seg_passes = 0;
 
@@ -220,6 +228,7 @@ ssg::StepArgs step_args(bh_system* s) {
     a.inter = s->inter;
     a.work = s->work;
     a.fresh = s->fresh;
+    a.max_stack = s->work + 3;
     a.bucket = normalized_bucket(s->p.leaf_bucket);
     a.walk_grid_ref = s->walk_grid_ref;
     a.walk_grid_acc = s->walk_grid_acc;
@@ -236,7 +245,7 @@ int enqueue_step(bh_system* s, cudaStream_t st, cudaEvent_t* ev = nullptr) {
     CK(cudaMemsetAsync(s->box_ord, 0, sizeof(int) * 4 * s->nseg, st));  // origin box
     CK(cudaMemsetAsync(s->counter, 0, sizeof(int) * n, st));
     CK(cudaMemsetAsync(s->inter, 0, sizeof(unsigned long long), st));
-    CK(cudaMemsetAsync(s->work, 0, 3 * sizeof(int), st));
+    CK(cudaMemsetAsync(s->work, 0, 6 * sizeof(int), st));
 
     BodyPtrs cur = s->st[0];
     CK(mark(0));
@@ -278,17 +287,17 @@ int enqueue_step(bh_system* s, cudaStream_t st, cudaEvent_t* ev = nullptr) {
     CK(mark(4));
     k_build<<<nb, tb, 0, st>>>(ka, n, segs, s->tree, s->status);
     CK(mark(5));
-    k_moments<<<nb, tb, 0, st>>>(n, accuracy ? 1 : 0, dst.x, dst.y, dst.m, s->tree.left,
-                                 s->tree.right, s->tree.parent, s->tree.leaf_parent, s->counter,
-                                 s->sums);
-    CK(mark(6));
-    k_records<<<nb, tb, 0, st>>>(n, segs, accuracy ? 1 : 0, s->p.theta, s->p.gravity, s->box_ord, ka,
-                                 s->tree.left, s->tree.right, s->tree.parent, s->tree.split,
-                                 s->tree.first, s->tree.last, s->sums, s->rec);
+    k_moments<256><<<nb, 256, 0, st>>>(n, accuracy ? 1 : 0, dst.x, dst.y, dst.m, s->tree.left,
+                                       s->tree.right, s->tree.parent, s->tree.leaf_parent,
+                                       s->tree.first, s->tree.last, s->counter, s->sums);
+    k_records<<<nb, tb, 0, st>>>(n, segs, accuracy ? 1 : 0, s->p.theta, s->p.gravity, s->box_ord,
+                                 ka, s->tree, s->sums, s->rec);
     CK(cudaGetLastError());
-    CK(mark(7));
+    CK(mark(6));
     StepArgs a = step_args(s);
-    CK(launch_walk(a, st));
+    CK(launch_walk(a, st, 0));
+    CK(mark(7));
+    CK(launch_walk(a, st, 1));
     CK(mark(8));
     return BH_OK;
 }
@@ -471,7 +480,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     bytes += 8 * span<int>(N);
     bytes += 5 * span<float>(N) + span<float4>(N);
     bytes += 2 * span<float4>(N) + 2 * span<int4>(N);
-    bytes += 2 * span<float>(N) + span<int>(1) + span<unsigned long long>(1) + span<int>(3) +
+    bytes += 2 * span<float>(N) + span<int>(1) + span<unsigned long long>(1) + span<int>(6) +
              span<int>(1);
     cudaError_t e = cudaMalloc(&s->arena, bytes);
     if (e != cudaSuccess) {
@@ -528,7 +537,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     s->ay = carve<float>(c, N);
     s->status = carve<int>(c, 1);
     s->inter = carve<unsigned long long>(c, 1);
-    s->work = carve<int>(c, 3);
+    s->work = carve<int>(c, 6);
     s->fresh = carve<int>(c, 1);
 
     std::vector<int> sop;
@@ -780,6 +789,11 @@ int bh_get_stats(bh_system* s, bh_stats* out, void* stream) {
     int bits = 0;
     unsigned long long inter = 0;
     int box[4] = {0, 0, 0, 0};
+    int wst[3] = {0, 0, 0};
+    CK(cudaMemcpy(wst, s->work + 3, sizeof(wst), cudaMemcpyDeviceToHost));
+    out->max_stack = wst[0];
+    out->walk_rounds = wst[1];
+    out->nodes_tested = wst[2];
     CK(cudaMemcpy(&bits, s->status, sizeof(int), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(&inter, s->inter, sizeof(inter), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(box, s->box_ord, sizeof(box), cudaMemcpyDeviceToHost));

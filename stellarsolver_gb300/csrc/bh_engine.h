@@ -29,11 +29,12 @@ struct StepArgs {
     unsigned long long* inter;
     int* work;   // [0] reference walk, [1] bootstrap pass, [2] accuracy walk
     int* fresh;  // set by bh_set_state: the next step bootstraps |a_old|
+    int* max_stack;  // deepest accuracy-walk stack of the step
     int bucket;
     int walk_grid_ref, walk_grid_acc;
 };
 
-cudaError_t launch_walk(const StepArgs& a, cudaStream_t st);
+cudaError_t launch_walk(const StepArgs& a, cudaStream_t st, int part);
 cudaError_t init_walk_attributes();
 int normalized_bucket(int b);
 

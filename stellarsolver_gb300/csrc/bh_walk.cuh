@@ -188,12 +188,15 @@ __device__ __forceinline__ int warp_excl_scan(int v, int* total) {
     return x - v;
 }
 
-// a += m * d * u^-3/2 (softened body-body / monopole term)
+// a += m * d * u^-3/2 (softened body-body / monopole term).  With eps2 > 0,
+// u > 0 always; with eps2 == 0 the guard drops the self-interaction.
+template <bool GUARD>
 __device__ __forceinline__ void p2p(float bx, float by, float bm, float px, float py, float eps2,
                                     float& ax, float& ay) {
     float dx = bx - px, dy = by - py;
     float u = fmaf(dx, dx, fmaf(dy, dy, eps2));
-    float ri = u > 0.0f ? rsqrtf(u) : 0.0f;
+    float ri = rsqrtf(u);
+    if (GUARD) ri = u > 0.0f ? ri : 0.0f;
     float f = bm * ri * ri * ri;
     ax = fmaf(f, dx, ax);
     ay = fmaf(f, dy, ay);
@@ -239,7 +242,7 @@ struct AccSmem {
 //   G M l^3 <= alpha * a_g * d^5,  a_g = max(min |a_old|, 0.1 mean |a_old|) over the group,
 // d = min over the group's bodies of |COM - p|; the geometric rule is d > l/theta + delta.
 template <int WARPS, int STACK, int BUCKET, bool MIXED, bool ESTIMATE>
-__global__ void __launch_bounds__(WARPS * 32) k_walk_acc(Segs segs, Groups gr, WalkIn in,
+__global__ void __launch_bounds__(WARPS * 32, 4) k_walk_acc(Segs segs, Groups gr, WalkIn in,
                                                          const float4* __restrict__ recA,
                                                          const float4* __restrict__ recB,
                                                          const int4* __restrict__ recC,
@@ -248,7 +251,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk_acc(Segs segs, Groups gr, W
                                                          WalkOut out, int* __restrict__ status,
                                                          unsigned long long* __restrict__ inter_total,
                                                          int* __restrict__ work,
-                                                         int* __restrict__ fresh) {
+                                                         int* __restrict__ fresh,
+                                                         int* __restrict__ max_stack) {
     if (ESTIMATE) {
         if (*(volatile int*)fresh == 0) return;
     } else if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -278,6 +282,15 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk_acc(Segs segs, Groups gr, W
         const float px = in.x[jj], py = in.y[jj];
         __syncwarp();
         gp[lane] = make_float2(px, py);
+        float gx0 = px, gx1 = px, gy0 = py, gy1 = py;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            gx0 = fminf(gx0, __shfl_xor_sync(kFull, gx0, o));
+            gx1 = fmaxf(gx1, __shfl_xor_sync(kFull, gx1, o));
+            gy0 = fminf(gy0, __shfl_xor_sync(kFull, gy0, o));
+            gy1 = fmaxf(gy1, __shfl_xor_sync(kFull, gy1, o));
+        }
+        const float gdiag = sqrtf((gx1 - gx0) * (gx1 - gx0) + (gy1 - gy0) * (gy1 - gy0));
         // relative-rule scale of the group
         float aa = __int_as_float(0x7f800000);
         if (!ESTIMATE && alpha > 0.0f) {
@@ -294,7 +307,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk_acc(Segs segs, Groups gr, W
         float cax = 0.0f, cay = 0.0f;   // Kahan compensation (MIXED)
         long long entries = 0;
         bool overflow = false;
-        int top = 0, ccnt = 0, bcnt = 0;
+        int top = 0, ccnt = 0, bcnt = 0, peak = 0, rounds = 0, tested = 0;
         if (hi - lo >= 2) {
             if (lane == 0) stack[0] = lo;
             top = 1;
@@ -321,7 +334,12 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk_acc(Segs segs, Groups gr, W
             }
             __syncwarp();
             float bx = 0.0f, by = 0.0f;
-            for (int e = 0; e < k; ++e) p2m(cA[e], cB[e], px, py, eps2, bx, by);
+            if (k == 32) {
+#pragma unroll 4
+                for (int e = 0; e < 32; ++e) p2m(cA[e], cB[e], px, py, eps2, bx, by);
+            } else {
+                for (int e = 0; e < k; ++e) p2m(cA[e], cB[e], px, py, eps2, bx, by);
+            }
             add_batch(bx, by);
             ccnt -= k;
             entries += k;
@@ -334,9 +352,22 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk_acc(Segs segs, Groups gr, W
             }
             __syncwarp();
             float bx = 0.0f, by = 0.0f;
-            for (int e = 0; e < k; ++e) {
-                float4 P = bP[e];
-                p2p(P.x, P.y, P.z, px, py, eps2, bx, by);
+            if (eps2 > 0.0f && k == 32) {
+#pragma unroll 4
+                for (int e = 0; e < 32; ++e) {
+                    float4 P = bP[e];
+                    p2p<false>(P.x, P.y, P.z, px, py, eps2, bx, by);
+                }
+            } else if (eps2 > 0.0f) {
+                for (int e = 0; e < k; ++e) {
+                    float4 P = bP[e];
+                    p2p<false>(P.x, P.y, P.z, px, py, eps2, bx, by);
+                }
+            } else {
+                for (int e = 0; e < k; ++e) {
+                    float4 P = bP[e];
+                    p2p<true>(P.x, P.y, P.z, px, py, eps2, bx, by);
+                }
             }
             add_batch(bx, by);
             bcnt -= k;
@@ -353,18 +384,39 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk_acc(Segs segs, Groups gr, W
             __syncwarp();
             const int node = lane < k ? stack[top - 1 - lane] : -1;
             top -= k;
+            ++rounds;
+            tested += k;
             int cat = -1;  // 0 approximate, 1 leaf bodies, 2 open
             int4 D = make_int4(0, 0, 0, 0);
+            // Distance from the node's centre of mass to the group's bodies:
+            // the group box gives a lower bound; the exact minimum over the 32
+            // bodies is needed only when the box test is inconclusive, i.e.
+            // d_box <= ropen < d_box + box diagonal, for some lane.
+            float4 A = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            float d2 = 0.0f;
+            bool need = false;
             if (node >= 0) {
-                const float4 A = recA[node];
+                A = recA[node];
                 D = recD[node];
-                float d2 = __int_as_float(0x7f800000);
+                const float ddx = fmaxf(fmaxf(gx0 - A.x, A.x - gx1), 0.0f);
+                const float ddy = fmaxf(fmaxf(gy0 - A.y, A.y - gy1), 0.0f);
+                d2 = fmaf(ddx, ddx, ddy * ddy);
+                if (d2 <= A.w) {
+                    const float reach = sqrtf(d2) + gdiag;
+                    need = reach * reach > A.w;
+                }
+            }
+            if (__any_sync(kFull, need)) {
+                float e2 = __int_as_float(0x7f800000);
 #pragma unroll 8
                 for (int e = 0; e < 32; ++e) {
                     float2 q = gp[e];
                     float dx = q.x - A.x, dy = q.y - A.y;
-                    d2 = fminf(d2, fmaf(dx, dx, dy * dy));
+                    e2 = fminf(e2, fmaf(dx, dx, dy * dy));
                 }
+                if (need) d2 = e2;
+            }
+            if (node >= 0) {
                 bool acc = d2 > A.w;
                 if (acc && !ESTIMATE) acc = __int_as_float(D.z) <= aa * d2 * d2 * sqrtf(d2);
                 cat = acc ? 0 : (D.y <= BUCKET ? 1 : 2);
@@ -381,9 +433,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk_acc(Segs segs, Groups gr, W
                 nb += (cs[q] != kNoChild && cs[q] < 0);
                 nn += (cs[q] >= 0);
             }
-            int btot, ntot;
-            int boff = warp_excl_scan(nb, &btot);
-            int noff = warp_excl_scan(nn, &ntot);
+            int tot;
+            const int off = warp_excl_scan(nb | (nn << 16), &tot);
+            const int boff = off & 0xffff, noff = off >> 16;
+            const int btot = tot & 0xffff, ntot = tot >> 16;
             int* bw = blist + bcnt + boff;
             __syncwarp();  // every lane has read its stack slot before children overwrite it
             if (cat == 1) {
@@ -401,13 +454,21 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk_acc(Segs segs, Groups gr, W
             }
             bcnt += btot;
             top += ntot;
+            peak = max(peak, top);
             __syncwarp();
             while (ccnt >= 32) flush_cells(32);
             while (bcnt >= 32) flush_bodies(32);
         }
         if (ccnt > 0) flush_cells(ccnt);
         if (bcnt > 0) flush_bodies(bcnt);
-        if (overflow && lane == 0) atomicOr(status, ST_STACK);
+        if (lane == 0) {
+            if (overflow) atomicOr(status, ST_STACK);
+            atomicMax(max_stack, peak);
+            if (!ESTIMATE) {
+                atomicAdd(max_stack + 1, rounds);
+                atomicAdd(max_stack + 2, tested);
+            }
+        }
         const float gax = G * (MIXED ? ax - cax : ax);
         const float gay = G * (MIXED ? ay - cay : ay);
         if (ESTIMATE) {

@@ -22,8 +22,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=1)
     ap.add_argument("--bucket", type=int, default=0)
     ap.add_argument("--graph", action="store_true")
+    ap.add_argument("--model", default="plummer", choices=["plummer", "disk", "colliding"])
     a = ap.parse_args()
-    x, y, vx, vy, m = models.plummer(a.n, models.SEED_BASE + 1)
+    if a.model == "plummer":
+        x, y, vx, vy, m = models.plummer(a.n, models.SEED_BASE + 1)
+    elif a.model == "disk":
+        x, y, vx, vy, m = models.disk(a.n, models.SEED_BASE)
+    else:
+        x, y, vx, vy, m = models.colliding_disks(a.n, models.SEED_BASE + 2)
     with bh.BarnesHutSystem(a.n, mode=a.mode, theta=0.5, eps2=1e-4, timestep=1e-4,
                             leaf_bucket=a.bucket, use_graph=a.graph) as s:
         s.set_state(x, y, vx, vy, m)
@@ -35,7 +41,8 @@ def main():
             s.sync()
         st = s.stats()
     print(f"profile_step n={a.n} mode={a.mode} steps={a.steps} interactions={st['interactions']} "
-          f"status={st['status']}")
+          f"status={st['status']} max_stack={st['max_stack']} nodes={st['nodes']} "
+          f"rounds={st['walk_rounds']} tested={st['nodes_tested']}")
 
 
 if __name__ == "__main__":
