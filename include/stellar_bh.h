@@ -95,6 +95,16 @@ void bh_default_params(bh_params* p);
  * device ordinal (-1 = current). */
 int bh_create(const bh_params* p, int n, int device, bh_system** out);
 
+/* A batch of nsys independent systems in one handle (no reference
+ * counterpart: the reference runs one system).  System k's bodies occupy
+ * [bh_system_offset(s, k), + sizes[k]) of every body array passed to or from
+ * the handle; each system has its own box, tree and walk, and every phase is
+ * one launch over the whole batch.  bh_step advances all systems. */
+int bh_ensemble_create(const bh_params* p, int nsys, const int* sizes, int device,
+                       bh_system** out);
+int bh_num_systems(const bh_system* s);
+int bh_system_offset(const bh_system* s, int k);
+
 /* ~BarnesHutParticleSystem (BarnesHutParticleSystem.cpp:249-292). */
 int bh_destroy(bh_system* s);
 
@@ -164,6 +174,14 @@ int bh_step_profiled(bh_system* s, void* stream, float* phase_ms);
  * reference counterpart.  Synchronous. */
 int bh_direct_sum_f64(bh_system* s, int ns, const int* idx, double* ax, double* ay);
 
+/* FP64 energy and momentum of every system of the handle at the current
+ * positions: out[4k+0] kinetic 0.5 sum m v^2, out[4k+1] potential
+ * 0.5 sum m phi with phi from a tree walk over a tree of the current
+ * positions (geometric opening rule, quadrupole cells, softened like the
+ * forces, per-body sums in FP64), out[4k+2..3] momentum.  The state is not
+ * changed.  Synchronous.  No reference counterpart. */
+int bh_energy(bh_system* s, void* stream, double* out);
+
 /* Measure the device's FP32 FMA throughput (TFLOP/s, 2 flops per FMA) with a
  * register-only kernel on every SM; the roofline denominator of the force
  * walk.  device -1 = current.  No reference counterpart. */
@@ -179,6 +197,16 @@ int bh_measure_fp32_peak(int device, double* tflops);
 #define BH_MODEL_PLUMMER 2
 int bh_initial_conditions(int model, int n, float gravity, float* mass, float* x, float* y,
                           float* vx, float* vy);
+
+/* Choose the accuracy walk's shape for the current state: the stack depth
+ * from the deepest stack of one step (x1.5), then the fastest of block sizes
+ * {128, 256} x leaf buckets {4, 8, 16}, each timed over two steps from the
+ * same saved state.  The state is restored afterwards, and the chosen values
+ * are stored in the system's parameters (and copied to *chosen if not NULL).
+ * REFERENCE mode has nothing to tune.  Replaces the reference's hand-matched
+ * blockSize/gridSize constants (Particle_cuda.cu:5-6, README.md:59).
+ * Allocates a temporary state backup; synchronous. */
+int bh_autotune(bh_system* s, void* stream, bh_params* chosen);
 
 /* Human-readable text for a status code, and the last CUDA error seen by the
  * library in this thread. */

@@ -71,6 +71,9 @@ def lib() -> ctypes.CDLL:
     L.bh_default_params.argtypes = [P(Params)]
     L.bh_default_params.restype = None
     L.bh_create.argtypes = [P(Params), i32, i32, P(vp)]
+    L.bh_ensemble_create.argtypes = [P(Params), i32, vp, i32, P(vp)]
+    L.bh_num_systems.argtypes = [vp]
+    L.bh_system_offset.argtypes = [vp, i32]
     L.bh_destroy.argtypes = [vp]
     L.bh_set_params.argtypes = [vp, P(Params)]
     L.bh_get_params.argtypes = [vp, P(Params)]
@@ -87,6 +90,8 @@ def lib() -> ctypes.CDLL:
     L.bh_step_profiled.argtypes = [vp, vp, vp]
     L.bh_direct_sum_f64.argtypes = [vp, i32, vp, vp, vp]
     L.bh_measure_fp32_peak.argtypes = [i32, P(ctypes.c_double)]
+    L.bh_autotune.argtypes = [vp, vp, P(Params)]
+    L.bh_energy.argtypes = [vp, vp, vp]
     L.bh_initial_conditions.argtypes = [i32, i32, ctypes.c_float] + [vp] * 5
     L.bh_status_string.argtypes = [i32]
     L.bh_status_string.restype = ctypes.c_char_p
@@ -155,14 +160,22 @@ def make_params(mode="reference", theta=0.5, eps2=0.025, gravity=1.0, timestep=1
 
 
 class BarnesHutSystem:
-    """One system of n bodies on one GPU (BarnesHutParticleSystem.cpp:28-84)."""
+    """One system of n bodies on one GPU (BarnesHutParticleSystem.cpp:28-84), or,
+    with `sizes`, a batch of independent systems stepped together
+    (bh_ensemble_create); body arrays then hold the systems back to back."""
 
-    def __init__(self, n: int, device: int = 0, **params):
-        self.n = int(n)
+    def __init__(self, n: int = 0, device: int = 0, sizes=None, **params):
         self.params = make_params(**params)
         h = ctypes.c_void_p()
-        _check(lib().bh_create(ctypes.byref(self.params), self.n, device, ctypes.byref(h)),
-               "bh_create")
+        if sizes is None:
+            self.n = int(n)
+            _check(lib().bh_create(ctypes.byref(self.params), self.n, device, ctypes.byref(h)),
+                   "bh_create")
+        else:
+            sz = np.ascontiguousarray(sizes, dtype=np.int32)
+            self.n = int(sz.sum())
+            _check(lib().bh_ensemble_create(ctypes.byref(self.params), len(sz), _p(sz), device,
+                                            ctypes.byref(h)), "bh_ensemble_create")
         self._h = h
 
     # lifecycle -----------------------------------------------------------
@@ -186,6 +199,14 @@ class BarnesHutSystem:
     @property
     def handle(self):
         return self._h
+
+    @property
+    def num_systems(self) -> int:
+        return int(lib().bh_num_systems(self._h))
+
+    def offsets(self) -> np.ndarray:
+        k = self.num_systems
+        return np.array([lib().bh_system_offset(self._h, i) for i in range(k + 1)], np.int64)
 
     # state ----------------------------------------------------------------
     def set_params(self, **params):
@@ -235,6 +256,20 @@ class BarnesHutSystem:
     # stepping ---------------------------------------------------------------
     def step(self, steps: int = 1, stream=None):
         _check(lib().bh_step(self._h, int(steps), stream), "bh_step")
+
+    def energy(self, stream=None) -> np.ndarray:
+        """FP64 (kinetic, potential, px, py) per system, shape (systems, 4)."""
+        out = np.zeros(4 * self.num_systems, np.float64)
+        _check(lib().bh_energy(self._h, stream, _p(out)), "bh_energy")
+        return out.reshape(-1, 4)
+
+    def autotune(self, stream=None) -> dict:
+        """Pick the walk's block size, leaf bucket and stack depth (bh_autotune)."""
+        p = Params()
+        _check(lib().bh_autotune(self._h, stream, ctypes.byref(p)), "bh_autotune")
+        self.params = p
+        return {"block_size": p.block_size, "leaf_bucket": p.leaf_bucket,
+                "stack_depth": p.stack_depth}
 
     def step_profiled(self, phase_ms: np.ndarray, stream=None):
         """One non-graph step with events at the phase boundaries; adds each

@@ -38,7 +38,12 @@ namespace {
 
 constexpr int kWalkWarps = 8;
 constexpr int kRefStack = 256;
-constexpr int kAccStack = 768;  // deepest measured: 670 (2D Plummer, N = 2^24)
+constexpr int kDefaultStack = 768;  // deepest measured: 670 (2D Plummer, N = 2^24)
+constexpr int kMaxStack = 2048;
+constexpr int kDefaultBucket = 8;
+constexpr int kMaxBucket = 32;
+// worst case: 8 warps x (staging + 2048-entry stack + 32-body buckets)
+constexpr int kMaxWalkSmem = 8 * (3 * 32 * 16 + 32 * 8 + 64 * 4 + kMaxStack * 4 + (32 + 32 * kMaxBucket) * 4);
 constexpr int kBboxThreads = 256;
 constexpr int kBboxChunk = 8192;
 
@@ -63,56 +68,42 @@ size_t span(size_t count) {
 
 namespace ssg {
 
-template <int BUCKET, bool MIXED>
-static cudaError_t set_acc_attr() {
-    using Sm = AccSmem<kWalkWarps, kAccStack, BUCKET>;
-    cudaError_t e = cudaFuncSetAttribute(k_walk_acc<kWalkWarps, kAccStack, BUCKET, MIXED, false>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Sm));
-    if (e != cudaSuccess || MIXED) return e;
-    return cudaFuncSetAttribute(k_walk_acc<kWalkWarps, kAccStack, BUCKET, false, true>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Sm));
-}
-
-// Opt every accuracy-walk instantiation into its shared-memory size once, at
-// creation (never while a graph is being captured).
+// Opt the accuracy walk into the largest shared-memory size it may use, once,
+// at creation (never while a graph is being captured).
 cudaError_t init_walk_attributes() {
-    cudaError_t e = cudaSuccess;
-    cudaError_t r[8] = {set_acc_attr<1, false>(), set_acc_attr<4, false>(), set_acc_attr<8, false>(),
-                        set_acc_attr<16, false>(), set_acc_attr<1, true>(), set_acc_attr<4, true>(),
-                        set_acc_attr<8, true>(), set_acc_attr<16, true>()};
-    for (cudaError_t x : r)
-        if (x != cudaSuccess) e = x;
+    const int bytes = kMaxWalkSmem;
+    cudaError_t e = cudaFuncSetAttribute(k_walk_acc<false, false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_walk_acc<false, false, true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_walk_acc<true, false>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_walk_acc<false, true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     return e;
 }
 
-template <int BUCKET, bool MIXED>
+template <bool MIXED>
 static cudaError_t launch_acc(const StepArgs& a, cudaStream_t st, int part) {
-    using Sm = AccSmem<kWalkWarps, kAccStack, BUCKET>;
-    int grid = std::min(a.walk_grid_acc, (a.groups.ngroups + kWalkWarps - 1) / kWalkWarps);
+    const AccShape sh{a.stack, a.bucket};
+    const int warps = a.warps;
+    const size_t smem = (size_t)warps * acc_warp_bytes(sh);
+    int grid = std::min(a.walk_grid_acc, (a.groups.ngroups + warps - 1) / warps);
     if (grid < 1) grid = 1;
     if (part == 0) {
         // bootstrap pass: exits at once unless bh_set_state left the state fresh
-        k_walk_acc<kWalkWarps, kAccStack, BUCKET, false, true>
-            <<<grid, kWalkWarps * 32, sizeof(Sm), st>>>(
-                a.segs, a.groups, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt,
-                a.alpha, a.out, a.status, a.inter, a.work + 1, a.fresh, a.max_stack);
+        k_walk_acc<false, true><<<grid, warps * 32, smem, st>>>(
+            sh, a.segs, a.groups, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt,
+            a.alpha, a.out, a.status, a.inter, a.work + 1, a.fresh, a.max_stack);
     } else {
-        k_walk_acc<kWalkWarps, kAccStack, BUCKET, MIXED, false>
-            <<<grid, kWalkWarps * 32, sizeof(Sm), st>>>(
-                a.segs, a.groups, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt,
-                a.alpha, a.out, a.status, a.inter, a.work + 2, a.fresh, a.max_stack);
+        k_walk_acc<MIXED, false><<<grid, warps * 32, smem, st>>>(
+            sh, a.segs, a.groups, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt,
+            a.alpha, a.out, a.status, a.inter, a.work + 2, a.fresh, a.max_stack);
     }
     return cudaGetLastError();
-}
-
-template <bool MIXED>
-static cudaError_t launch_acc_bucket(const StepArgs& a, cudaStream_t st, int part) {
-    switch (a.bucket) {
-        case 1: return launch_acc<1, MIXED>(a, st, part);
-        case 4: return launch_acc<4, MIXED>(a, st, part);
-        case 16: return launch_acc<16, MIXED>(a, st, part);
-        default: return launch_acc<8, MIXED>(a, st, part);
-    }
 }
 
 // part 0: the accuracy modes' bootstrap pass (nothing in REFERENCE mode);
@@ -127,15 +118,14 @@ cudaError_t launch_walk(const StepArgs& a, cudaStream_t st, int part) {
             a.work);
         return cudaGetLastError();
     }
-    return a.mode == BH_MODE_MIXED ? launch_acc_bucket<true>(a, st, part)
-                                   : launch_acc_bucket<false>(a, st, part);
+    return a.mode == BH_MODE_MIXED ? launch_acc<true>(a, st, part) : launch_acc<false>(a, st, part);
 }
 
-int normalized_bucket(int b) {
-    if (b <= 1) return b <= 0 ? 8 : 1;
-    if (b <= 4) return 4;
-    if (b <= 8) return 8;
-    return 16;
+int normalized_bucket(int b) { return b <= 0 ? kDefaultBucket : std::min(b, kMaxBucket); }
+int normalized_stack(int s) { return s <= 0 ? kDefaultStack : std::max(64, std::min(s, kMaxStack)); }
+int normalized_warps(int block) {
+    int w = block <= 0 ? kWalkWarps : block / 32;
+    return std::max(1, std::min(w, 8));
 }
 
 }  // namespace ssg
@@ -174,6 +164,8 @@ struct bh_system {
     int* status = nullptr;
     unsigned long long* inter = nullptr;
     int* work = nullptr;   // 3 scheduling counters, walk stack peak, rounds, tests; reset every step
+                           // [6..8]: scratch of bh_energy
+    double* diag = nullptr;  // bh_energy: 4 sums per system
     int* fresh = nullptr;  // 1 after bh_set_state: bootstrap |a_old| in the next step
     int seg_passes = 0;
 
@@ -230,16 +222,19 @@ ssg::StepArgs step_args(bh_system* s) {
     a.fresh = s->fresh;
     a.max_stack = s->work + 3;
     a.bucket = normalized_bucket(s->p.leaf_bucket);
+    a.stack = normalized_stack(s->p.stack_depth);
+    a.warps = normalized_warps(s->p.block_size);
     a.walk_grid_ref = s->walk_grid_ref;
     a.walk_grid_acc = s->walk_grid_acc;
     return a;
 }
 
-// ev (optional): kPhases+1 events recorded at the phase boundaries
-int enqueue_step(bh_system* s, cudaStream_t st, cudaEvent_t* ev = nullptr) {
+// Box, keys, sort, reorder, tree, moments and walk records of the current
+// state (phases 0-5; the walk records in the accuracy layout when `accuracy`).
+// ev (optional): events recorded at the phase boundaries.
+int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev) {
     const int n = s->n;
     auto mark = [&](int k) -> cudaError_t { return ev ? cudaEventRecord(ev[k], st) : cudaSuccess; };
-    const bool accuracy = s->p.mode != BH_MODE_REFERENCE;
     const bool mixed = s->p.mode == BH_MODE_MIXED;
     Segs segs{s->nseg, s->seg_off, s->nseg > 1 ? s->seg_of_pos : nullptr};
     CK(cudaMemsetAsync(s->box_ord, 0, sizeof(int) * 4 * s->nseg, st));  // origin box
@@ -294,6 +289,15 @@ int enqueue_step(bh_system* s, cudaStream_t st, cudaEvent_t* ev = nullptr) {
                                  ka, s->tree, s->sums, s->rec);
     CK(cudaGetLastError());
     CK(mark(6));
+    return BH_OK;
+}
+
+// One step: the front half, then the bootstrap pass (accuracy modes, fresh
+// state only) and the walk fused with the integration (phases 6-7).
+int enqueue_step(bh_system* s, cudaStream_t st, cudaEvent_t* ev = nullptr) {
+    auto mark = [&](int k) -> cudaError_t { return ev ? cudaEventRecord(ev[k], st) : cudaSuccess; };
+    int rc = enqueue_front(s, st, s->p.mode != BH_MODE_REFERENCE, ev);
+    if (rc != BH_OK) return rc;
     StepArgs a = step_args(s);
     CK(launch_walk(a, st, 0));
     CK(mark(7));
@@ -480,7 +484,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     bytes += 8 * span<int>(N);
     bytes += 5 * span<float>(N) + span<float4>(N);
     bytes += 2 * span<float4>(N) + 2 * span<int4>(N);
-    bytes += 2 * span<float>(N) + span<int>(1) + span<unsigned long long>(1) + span<int>(6) +
+    bytes += 2 * span<float>(N) + span<int>(1) + span<unsigned long long>(1) + span<int>(9) + span<double>(4 * (size_t)nseg) +
              span<int>(1);
     cudaError_t e = cudaMalloc(&s->arena, bytes);
     if (e != cudaSuccess) {
@@ -537,7 +541,8 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     s->ay = carve<float>(c, N);
     s->status = carve<int>(c, 1);
     s->inter = carve<unsigned long long>(c, 1);
-    s->work = carve<int>(c, 6);
+    s->work = carve<int>(c, 9);
+    s->diag = carve<double>(c, 4 * (size_t)nseg);
     s->fresh = carve<int>(c, 1);
 
     std::vector<int> sop;
@@ -569,9 +574,11 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
         int bref = 0, bacc = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(
             &bref, k_walk_ref<kWalkWarps, kRefStack>, kWalkWarps * 32, 0);
-        using Sm = AccSmem<kWalkWarps, kAccStack, 16>;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &bacc, k_walk_acc<kWalkWarps, kAccStack, 16, true, false>, kWalkWarps * 32, sizeof(Sm));
+        // grid cap from the worst-case shape; the walks fetch groups dynamically
+        const AccShape sh{kDefaultStack, kDefaultBucket};
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bacc, k_walk_acc<true, false>,
+                                                      kWalkWarps * 32,
+                                                      (size_t)kWalkWarps * acc_warp_bytes(sh));
         s->walk_grid_ref = walk_grid_cap(s->sms, bref) * 4;
         s->walk_grid_acc = walk_grid_cap(s->sms, bacc) * 4;
         cudaGetLastError();
@@ -609,6 +616,19 @@ void bh_default_params(bh_params* p) {
 
 int bh_create(const bh_params* p, int n, int device, bh_system** out) {
     return ssg::system_create(p, &n, 1, device, out);
+}
+
+int bh_ensemble_create(const bh_params* p, int nsys, const int* sizes, int device,
+                       bh_system** out) {
+    if (nsys < 1 || nsys > 65536 || !sizes) return BH_ERR_ARG;
+    return ssg::system_create(p, sizes, nsys, device, out);
+}
+
+int bh_num_systems(const bh_system* s) { return s ? s->nseg : -1; }
+
+int bh_system_offset(const bh_system* s, int k) {
+    if (!s || k < 0 || k > s->nseg) return -1;
+    return s->h_off[k];
 }
 
 int bh_destroy(bh_system* s) {
@@ -968,6 +988,143 @@ int bh_measure_fp32_peak(int device, double* tflops) {
     double flops = 2.0 * 8.0 * 16.0 * iters * (double)blocks * threads;
     *tflops = flops / (best * 1e-3) / 1e12;
     return BH_OK;
+}
+
+// Per-system FP64 sums: out[4k..4k+3] += kinetic, potential (0.5 m phi), px, py.
+__global__ void k_energy_reduce(int n, Segs segs, const float* __restrict__ m,
+                                const float* __restrict__ vx, const float* __restrict__ vy,
+                                const double* __restrict__ pot, double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double mi = m[i], u = vx[i], v = vy[i];
+    double* o = out + 4 * seg_of(segs, i);
+    atomicAdd(o + 0, 0.5 * mi * (u * u + v * v));
+    atomicAdd(o + 1, 0.5 * mi * pot[i]);
+    atomicAdd(o + 2, mi * u);
+    atomicAdd(o + 3, mi * v);
+}
+
+int bh_energy(bh_system* s, void* stream, double* out) {
+    if (!s || !out) return BH_ERR_ARG;
+    if (!s->have_state) return BH_ERR_STATE;
+    CK(cudaSetDevice(s->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = enqueue_front(s, st, true, nullptr);  // tree of the current positions
+    if (rc != BH_OK) return rc;
+    StepArgs a = step_args(s);
+    a.alpha = 0.0f;
+    const AccShape sh{a.stack, a.bucket};
+    const size_t smem = (size_t)a.warps * acc_warp_bytes(sh);
+    int grid = std::min(a.walk_grid_acc, (a.groups.ngroups + a.warps - 1) / a.warps);
+    if (grid < 1) grid = 1;
+    // the sort's spare key buffer holds the per-body potential (8 bytes per body)
+    double* pot = reinterpret_cast<double*>(s->kfinal == s->keys ? s->keys_alt : s->keys);
+    int* counter = s->work + 6;  // dynamic scheduling of this pass; work[7]: its stack peak
+    CK(cudaMemsetAsync(counter, 0, 2 * sizeof(int), st));
+    k_walk_acc<false, false, true><<<grid, a.warps * 32, smem, st>>>(
+        sh, a.segs, a.groups, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt, 0.0f,
+        a.out, a.status, a.inter, counter, a.fresh, s->work + 7, pot);
+    CK(cudaGetLastError());
+    CK(cudaMemsetAsync(s->diag, 0, sizeof(double) * 4 * s->nseg, st));
+    Segs segs{s->nseg, s->seg_off, s->nseg > 1 ? s->seg_of_pos : nullptr};
+    const BodyPtrs& g = s->st[1];
+    k_energy_reduce<<<(s->n + 255) / 256, 256, 0, st>>>(s->n, segs, g.m, g.vx, g.vy, pot, s->diag);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, s->diag, sizeof(double) * 4 * s->nseg, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    int bits = 0;
+    CK(cudaMemcpy(&bits, s->status, sizeof(int), cudaMemcpyDeviceToHost));
+    return status_code(bits, BH_MODE_PLAIN);
+}
+
+int bh_autotune(bh_system* s, void* stream, bh_params* chosen) {
+    if (!s) return BH_ERR_ARG;
+    if (!s->have_state) return BH_ERR_STATE;
+    CK(cudaSetDevice(s->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t N = (size_t)s->n;
+    // back up the state the candidates will all start from
+    float* bk = nullptr;
+    CK(cudaMalloc(&bk, N * 9 * sizeof(float) + sizeof(int)));
+    BodyPtrs& c = s->st[0];
+    float* arrs[8] = {c.x, c.y, c.vx, c.vy, c.m, c.xlo, c.ylo, c.amag};
+    auto save = [&]() -> int {
+        for (int k = 0; k < 8; ++k)
+            CK(cudaMemcpyAsync(bk + k * N, arrs[k], N * sizeof(float), cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(bk + 8 * N, c.id, N * sizeof(int), cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(bk + 9 * N, s->fresh, sizeof(int), cudaMemcpyDeviceToDevice, st));
+        return BH_OK;
+    };
+    auto restore = [&]() -> int {
+        for (int k = 0; k < 8; ++k)
+            CK(cudaMemcpyAsync(arrs[k], bk + k * N, N * sizeof(float), cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(c.id, bk + 8 * N, N * sizeof(int), cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(s->fresh, bk + 9 * N, sizeof(int), cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemsetAsync(s->status, 0, sizeof(int), st));
+        return BH_OK;
+    };
+    const bh_params orig = s->p;
+    const bool orig_caller = s->caller_order;
+    int rc = save();
+    float best_ms = 1e30f;
+    bh_params best = orig;
+    if (rc == BH_OK && orig.mode != BH_MODE_REFERENCE) {
+        // stack depth: 1.5x the deepest stack of one step with a generous stack
+        s->p.stack_depth = kMaxStack;
+        drop_graph(s);
+        rc = enqueue_step(s, st);
+        int peak = 0;
+        if (rc == BH_OK) {
+            cudaError_t e = cudaMemcpyAsync(&peak, s->work + 3, sizeof(int), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) rc = cuda_fail(e, "bh_autotune");
+        }
+        const int stack = std::min(kMaxStack, std::max(256, ((peak * 3 / 2) + 127) / 128 * 128));
+        const int blocks[2] = {128, 256};
+        const int buckets[3] = {4, 8, 16};
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (rc == BH_OK) {
+            CK(cudaEventCreate(&e0));
+            CK(cudaEventCreate(&e1));
+        }
+        for (int bi = 0; bi < 2 && rc == BH_OK; ++bi) {
+            for (int ki = 0; ki < 3 && rc == BH_OK; ++ki) {
+                bh_params cand = orig;
+                cand.block_size = blocks[bi];
+                cand.leaf_bucket = buckets[ki];
+                cand.stack_depth = stack;
+                cand.use_graph = 0;
+                s->p = cand;
+                drop_graph(s);
+                rc = restore();
+                if (rc == BH_OK) rc = enqueue_step(s, st);  // warm-up (and bootstrap if fresh)
+                if (rc != BH_OK) break;
+                CK(cudaEventRecord(e0, st));
+                for (int k = 0; k < 2 && rc == BH_OK; ++k) rc = enqueue_step(s, st);
+                CK(cudaEventRecord(e1, st));
+                CK(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                CK(cudaEventElapsedTime(&ms, e0, e1));
+                int bits = 0;
+                CK(cudaMemcpy(&bits, s->status, sizeof(int), cudaMemcpyDeviceToHost));
+                if (status_code(bits, cand.mode) == BH_OK && ms < best_ms) {
+                    best_ms = ms;
+                    best = cand;
+                }
+            }
+        }
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+    }
+    if (rc == BH_OK) rc = restore();
+    if (rc == BH_OK) CK(cudaStreamSynchronize(st));
+    cudaFree(bk);
+    best.use_graph = orig.use_graph;
+    s->p = rc == BH_OK ? best : orig;
+    s->caller_order = orig_caller;
+    drop_graph(s);
+    if (chosen) *chosen = s->p;
+    return rc;
 }
 
 const char* bh_status_string(int st) {

@@ -30,13 +30,15 @@ struct StepArgs {
     int* work;   // [0] reference walk, [1] bootstrap pass, [2] accuracy walk
     int* fresh;  // set by bh_set_state: the next step bootstraps |a_old|
     int* max_stack;  // deepest accuracy-walk stack of the step
-    int bucket;
+    int bucket, stack, warps;  // accuracy-walk shape: leaf bucket, stack entries, warps/block
     int walk_grid_ref, walk_grid_acc;
 };
 
 cudaError_t launch_walk(const StepArgs& a, cudaStream_t st, int part);
 cudaError_t init_walk_attributes();
 int normalized_bucket(int b);
+int normalized_stack(int s);
+int normalized_warps(int block);
 
 // Create a batch of independent systems of the given sizes (bh_create is the
 // single-system case).

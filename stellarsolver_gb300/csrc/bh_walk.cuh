@@ -190,6 +190,18 @@ __device__ __forceinline__ int warp_excl_scan(int v, int* total) {
 
 // a += m * d * u^-3/2 (softened body-body / monopole term).  With eps2 > 0,
 // u > 0 always; with eps2 == 0 the guard drops the self-interaction.
+// Potential at p of a cell (monopole + quadrupole about its COM c):
+//   phi = -[M u^-1/2 + 0.5 d.T.d u^-5/2 - (h/3) u^-3/2],  d = c - p, T = 3S, h = 1.5 tr S
+// (G applied by the caller).
+__device__ __forceinline__ float pot_cell(float4 A, float4 B, float px, float py, float eps2) {
+    const float dx = A.x - px, dy = A.y - py;
+    const float u = fmaf(dx, dx, fmaf(dy, dy, eps2));
+    const float ri = rsqrtf(u), r2 = ri * ri, r3 = ri * r2;
+    const float tdx = fmaf(B.x, dx, B.y * dy), tdy = fmaf(B.y, dx, B.z * dy);
+    const float dtd = fmaf(dx, tdx, dy * tdy);
+    return -(A.z * ri + 0.5f * dtd * r3 * r2 - (B.w * (1.0f / 3.0f)) * r3);
+}
+
 template <bool GUARD>
 __device__ __forceinline__ void p2p(float bx, float by, float bm, float px, float py, float eps2,
                                     float& ax, float& ay) {
@@ -224,25 +236,33 @@ __device__ __forceinline__ void p2m(float4 A, float4 B, float px, float py, floa
     ay = fmaf(r3, fy, ay);
 }
 
-template <int WARPS, int STACK, int BUCKET>
-struct AccSmem {
-    static constexpr int kBodyCap = 32 + 32 * (BUCKET > 4 ? BUCKET : 4);
-    int stack[WARPS][STACK];
-    int clist[WARPS][64];
-    int blist[WARPS][kBodyCap];
-    float4 cA[WARPS][32];
-    float4 cB[WARPS][32];
-    float4 bP[WARPS][32];
-    float2 gp[WARPS][32];  // the group's body positions, for the exact distance test
+// Launch-time shape of the accuracy walk (chosen by bh_autotune or the defaults).
+struct AccShape {
+    int stack;   // stack entries per warp
+    int bucket;  // a node of <= bucket bodies is a leaf: its bodies interact directly
 };
+
+// Per-warp shared memory of the accuracy walk (bytes, 16-byte aligned pieces):
+// staged cell records, staged bodies, the group's positions, the cell list,
+// the node stack and the body list.
+__host__ __device__ __forceinline__ int acc_body_cap(int bucket) {
+    return 32 + 32 * (bucket > 4 ? bucket : 4);
+}
+__host__ __device__ __forceinline__ int acc_warp_bytes(AccShape sh) {
+    return 3 * 32 * 16 + 32 * 8 + 64 * 4 + ((sh.stack * 4 + 15) & ~15) +
+           ((acc_body_cap(sh.bucket) * 4 + 15) & ~15);
+}
 
 // PLAIN / MIXED walk.  ESTIMATE = the bootstrap pass after bh_set_state: the
 // geometric rule only, writes |G a| into in.amag and nothing else (skipped
 // unless *fresh is set).  The main pass also applies the relative rule
 //   G M l^3 <= alpha * a_g * d^5,  a_g = max(min |a_old|, 0.1 mean |a_old|) over the group,
 // d = min over the group's bodies of |COM - p|; the geometric rule is d > l/theta + delta.
-template <int WARPS, int STACK, int BUCKET, bool MIXED, bool ESTIMATE>
-__global__ void __launch_bounds__(WARPS * 32, 4) k_walk_acc(Segs segs, Groups gr, WalkIn in,
+// DIAG = diagnostics pass: the main rule, but each body's potential (FP64
+// accumulation of float batches, own body excluded) goes to pot[] and nothing
+// is integrated.
+template <bool MIXED, bool ESTIMATE, bool DIAG = false>
+__global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, Groups gr, WalkIn in,
                                                          const float4* __restrict__ recA,
                                                          const float4* __restrict__ recB,
                                                          const int4* __restrict__ recC,
@@ -252,26 +272,29 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_walk_acc(Segs segs, Groups gr
                                                          unsigned long long* __restrict__ inter_total,
                                                          int* __restrict__ work,
                                                          int* __restrict__ fresh,
-                                                         int* __restrict__ max_stack) {
+                                                         int* __restrict__ max_stack,
+                                                         double* __restrict__ pot = nullptr) {
     if (ESTIMATE) {
         if (*(volatile int*)fresh == 0) return;
-    } else if (blockIdx.x == 0 && threadIdx.x == 0) {
+    } else if (!DIAG && blockIdx.x == 0 && threadIdx.x == 0) {
         *fresh = 0;  // the bootstrap pass of this step (if any) has completed
     }
-    using Sm = AccSmem<WARPS, STACK, BUCKET>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    Sm& sm = *reinterpret_cast<Sm*>(smem_raw);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned lt = lanemask_lt();
-    int* stack = sm.stack[warp];
-    int* clist = sm.clist[warp];
-    int* blist = sm.blist[warp];
-    float4* cA = sm.cA[warp];
-    float4* cB = sm.cB[warp];
-    float4* bP = sm.bP[warp];
-    float2* gp = sm.gp[warp];
+    const int STACK = shape.stack, BUCKET = shape.bucket;
+    unsigned char* wbase = smem_raw + (size_t)warp * acc_warp_bytes(shape);
+    float4* cA = reinterpret_cast<float4*>(wbase);
+    float4* cB = cA + 32;
+    float4* bP = cB + 32;
+    float2* gp = reinterpret_cast<float2*>(bP + 32);
+    int* clist = reinterpret_cast<int*>(gp + 32);
+    int* stack = clist + 64;
+    int* blist = stack + ((STACK + 3) & ~3);
     unsigned long long my_inter = 0;
 
+    const int WARPS = blockDim.x >> 5;
+    (void)WARPS;
     for (int g = next_group(work); g < gr.ngroups; g = next_group(work)) {
         int lo, hi, gstart;
         group_range(segs, gr, g, &lo, &hi, &gstart);
@@ -293,7 +316,7 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_walk_acc(Segs segs, Groups gr
         const float gdiag = sqrtf((gx1 - gx0) * (gx1 - gx0) + (gy1 - gy0) * (gy1 - gy0));
         // relative-rule scale of the group
         float aa = __int_as_float(0x7f800000);
-        if (!ESTIMATE && alpha > 0.0f) {
+        if (!ESTIMATE && !DIAG && alpha > 0.0f) {
             float a = in.amag[jj];
             float amin = a, asum = valid ? a : 0.0f;
 #pragma unroll
@@ -305,6 +328,7 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_walk_acc(Segs segs, Groups gr
         }
         float ax = 0.0f, ay = 0.0f;     // running sums
         float cax = 0.0f, cay = 0.0f;   // Kahan compensation (MIXED)
+        double phi = 0.0;               // DIAG: potential
         long long entries = 0;
         bool overflow = false;
         int top = 0, ccnt = 0, bcnt = 0, peak = 0, rounds = 0, tested = 0;
@@ -334,7 +358,11 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_walk_acc(Segs segs, Groups gr
             }
             __syncwarp();
             float bx = 0.0f, by = 0.0f;
-            if (k == 32) {
+            if (DIAG) {
+                float f = 0.0f;
+                for (int e = 0; e < k; ++e) f += pot_cell(cA[e], cB[e], px, py, eps2);
+                phi += (double)f;
+            } else if (k == 32) {
 #pragma unroll 4
                 for (int e = 0; e < 32; ++e) p2m(cA[e], cB[e], px, py, eps2, bx, by);
             } else {
@@ -348,11 +376,20 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_walk_acc(Segs segs, Groups gr
             __syncwarp();
             if (lane < k) {
                 int b = blist[bcnt - k + lane];
-                bP[lane] = make_float4(in.x[b], in.y[b], in.m[b], 0.0f);
+                bP[lane] = make_float4(in.x[b], in.y[b], in.m[b], __int_as_float(b));
             }
             __syncwarp();
             float bx = 0.0f, by = 0.0f;
-            if (eps2 > 0.0f && k == 32) {
+            if (DIAG) {
+                float f = 0.0f;
+                for (int e = 0; e < k; ++e) {
+                    const float4 P = bP[e];
+                    if (__float_as_int(P.w) == j) continue;  // own body
+                    const float dx = P.x - px, dy = P.y - py;
+                    f -= P.z * rsqrtf(fmaf(dx, dx, fmaf(dy, dy, eps2)));
+                }
+                phi += (double)f;
+            } else if (eps2 > 0.0f && k == 32) {
 #pragma unroll 4
                 for (int e = 0; e < 32; ++e) {
                     float4 P = bP[e];
@@ -418,7 +455,7 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_walk_acc(Segs segs, Groups gr
             }
             if (node >= 0) {
                 bool acc = d2 > A.w;
-                if (acc && !ESTIMATE) acc = __int_as_float(D.z) <= aa * d2 * d2 * sqrtf(d2);
+                if (acc && !ESTIMATE && !DIAG) acc = __int_as_float(D.z) <= aa * d2 * d2 * sqrtf(d2);
                 cat = acc ? 0 : (D.y <= BUCKET ? 1 : 2);
             }
             unsigned mc = __ballot_sync(kFull, cat == 0);
@@ -464,13 +501,17 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_walk_acc(Segs segs, Groups gr
         if (lane == 0) {
             if (overflow) atomicOr(status, ST_STACK);
             atomicMax(max_stack, peak);
-            if (!ESTIMATE) {
+            if (!ESTIMATE && !DIAG) {
                 atomicAdd(max_stack + 1, rounds);
                 atomicAdd(max_stack + 2, tested);
             }
         }
         const float gax = G * (MIXED ? ax - cax : ax);
         const float gay = G * (MIXED ? ay - cay : ay);
+        if (DIAG) {
+            if (valid) pot[j] = (double)G * phi;
+            continue;
+        }
         if (ESTIMATE) {
             if (valid) in.amag[j] = sqrtf(gax * gax + gay * gay);
             continue;
@@ -508,7 +549,7 @@ __global__ void __launch_bounds__(WARPS * 32, 4) k_walk_acc(Segs segs, Groups gr
             out.amag[j] = sqrtf(gax * gax + gay * gay);
         }
     }
-    if (!ESTIMATE && lane == 0 && my_inter) atomicAdd(inter_total, my_inter);
+    if (!ESTIMATE && !DIAG && lane == 0 && my_inter) atomicAdd(inter_total, my_inter);
 }
 
 }  // namespace ssg

@@ -173,3 +173,56 @@ def test_set_accel_skips_bootstrap(bh):
         st2b = s.get_state()
     for k in ("x", "y", "vx", "vy"):
         assert np.allclose(st2[k], st2b[k], rtol=0, atol=1e-6 * np.abs(st2[k]).max()), k
+
+
+def test_energy_and_momentum_fp64(bh, oracle):
+    """bh_energy against the exact FP64 O(N^2) sums: kinetic energy and momentum
+    to 1e-12 (same float inputs, FP64 sums), potential to 1e-3 (tree walk,
+    geometric rule, quadrupole cells)."""
+    from stellarsolver_gb300 import models
+
+    x, y, vx, vy, m = models.plummer(1 << 14, 0x5EED4000)
+    eps2 = 1e-4
+    with bh.BarnesHutSystem(len(x), mode="plain", eps2=eps2, timestep=1e-4) as s:
+        s.set_state(x, y, vx, vy, m)
+        e = s.energy()[0]
+        st = s.get_state()
+    ke, pe, px, py = oracle.energy_f64(st["x"], st["y"], st["vx"], st["vy"], st["m"], eps2)
+    assert abs(e[0] - ke) <= 1e-12 * abs(ke)
+    assert abs(e[2] - px) <= 1e-12 * abs(ke) and abs(e[3] - py) <= 1e-12 * abs(ke)
+    assert abs(e[1] - pe) <= 1e-3 * abs(pe), (e[1], pe)
+
+
+def test_energy_drift_small_over_steps(bh):
+    """MIXED mode, 2D Plummer 2^14, dt = 1e-4, 50 steps: |dE/E| small."""
+    from stellarsolver_gb300 import models
+
+    x, y, vx, vy, m = models.plummer(1 << 14, 0x5EED4001)
+    with bh.BarnesHutSystem(len(x), mode="mixed", eps2=1e-4, timestep=1e-4) as s:
+        s.set_state(x, y, vx, vy, m)
+        e0 = s.energy()[0]
+        s.step(50)
+        s.sync()
+        e1 = s.energy()[0]
+    E0, E1 = e0[0] + e0[1], e1[0] + e1[1]
+    assert abs(E1 - E0) <= 2e-3 * abs(E0), (E0, E1)
+
+
+def test_autotune_keeps_results_and_accuracy(bh, oracle):
+    from stellarsolver_gb300 import models
+
+    x, y, vx, vy, m = models.plummer(1 << 16, 0x5EED4002)
+    with bh.BarnesHutSystem(len(x), mode="mixed", eps2=1e-4, timestep=0.0) as s:
+        s.set_state(x, y, vx, vy, m)
+        before = s.get_state()
+        chosen = s.autotune()
+        after = s.get_state()
+        for k in ("x", "y", "vx", "vy"):
+            assert np.array_equal(before[k], after[k]), k  # state restored
+        assert chosen["leaf_bucket"] in (4, 8, 16) and chosen["block_size"] in (128, 256)
+        assert 256 <= chosen["stack_depth"] <= 2048
+        s.step(1)
+        s.sync()
+        ax, ay = s.get_accel()
+    rms, mx = force_error(oracle, x, y, m, ax, ay, 1e-4)
+    assert rms <= 1e-3, (rms, mx)
