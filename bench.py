@@ -187,6 +187,9 @@ def run_engine(args):
     # ---------------------------------------------------------------- steps/s
     sysm = bh.BarnesHutSystem(n, device=local, mode=args.mode, use_graph=True, **common)
     sysm.set_state(x, y, vx, vy, m)
+    tuned = None
+    if not args.no_autotune and args.mode != "reference":
+        tuned = sysm.autotune(sp)
     for _ in range(args.warmup):
         sysm.step(1, sp)
     sysm.sync(sp)
@@ -249,8 +252,11 @@ def run_engine(args):
         phases[name] = entry
 
     # ---------------------------------------------------------------- e2e through the C ABI
-    e2e = run_e2e(bh, torch, stream, sp, n, x, y, vx, vy, m, common, local, args)
+    e2e = run_e2e(bh, torch, stream, sp, n, x, y, vx, vy, m, sysm.params, local, args)
     sysm.close()
+    ens = None
+    if not args.no_ensemble:
+        ens = run_ensemble(bh, torch, stream, sp, local, world, rank, args)
 
     result = {
         "metric": METRIC,
@@ -266,7 +272,7 @@ def run_engine(args):
         "dtype": "f32",
         "data": "synthetic (seeded 2D Plummer, models.plummer)",
         "config": {"workload": WORKLOAD, "n_bodies": n, "theta": THETA, "eps": EPS, "dt": DT,
-                   "mode": args.mode, "leaf_bucket": args.bucket or "default", "cuda_graph": True,
+                   "mode": args.mode, "walk_shape": tuned or "defaults", "cuda_graph": True,
                    "l2": "flushed (256 MB write) before every timed step",
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "timed_wall_s_incl_flush": round(t_wall, 3)},
@@ -287,6 +293,7 @@ def run_engine(args):
                      "traffic": traffic, "phases": phases,
                      "hbm_peak_gbs": hbm_peak, "hbm_peak_source": hbm_kind},
         "e2e": e2e,
+        "ensemble": ens,
         "gpu_launches": LAUNCHES_PER_STEP * args.steps,
         "clocks": clocks,
     }
@@ -315,14 +322,18 @@ def recorded_traffic(kernel):
         return None
 
 
-def run_e2e(bh, torch, stream, sp, n, x, y, vx, vy, m, common, local, args):
+def run_e2e(bh, torch, stream, sp, n, x, y, vx, vy, m, params, local, args):
     pin = {k: torch.from_numpy(v.copy()).pin_memory() for k, v in
            (("x", x), ("y", y), ("vx", vx), ("vy", vy), ("m", m))}
     outx = torch.empty(n, dtype=torch.float32).pin_memory()
     outy = torch.empty(n, dtype=torch.float32).pin_memory()
     ptr = {k: v.data_ptr() for k, v in pin.items()}
     lib = bh.lib()
-    with bh.BarnesHutSystem(n, device=local, mode=args.mode, use_graph=True, **common) as s:
+    with bh.BarnesHutSystem(n, device=local, mode=args.mode, use_graph=True,
+                            theta=params.theta, eps2=params.eps2, gravity=params.gravity,
+                            timestep=params.timestep, dampening=params.dampening,
+                            leaf_bucket=params.leaf_bucket, block_size=params.block_size,
+                            stack_depth=params.stack_depth, alpha=params.alpha) as s:
         def one():
             rc = lib.bh_set_state(s.handle, ptr["x"], ptr["y"], ptr["vx"], ptr["vy"], ptr["m"], sp)
             rc |= lib.bh_step(s.handle, 1, sp)
@@ -345,6 +356,68 @@ def run_e2e(bh, torch, stream, sp, n, x, y, vx, vy, m, common, local, args):
     return {"value": round(args.steps / secs, 3), "unit": "steps/s",
             "h2d_bytes_per_step": 20 * n, "d2h_bytes_per_step": 8 * n,
             "path": "bh_set_state(pinned host) + bh_step + bh_get_state(x, y -> pinned host)"}
+
+
+def run_ensemble(bh, torch, stream, sp, local, world, rank, args):
+    """256 independent systems, N log-uniform in [2^10, 2^17], half disks and half
+    Plummer spheres (eps = 0.01, dt = 1e-4, theta = 0.5).  The batched MIXED engine
+    (one launch per phase, CUDA graph) against one handle per system in PLAIN FP32
+    without a graph.  With several GPUs each rank steps its own systems."""
+    from stellarsolver_gb300 import models, sharding
+
+    sizes = models.ensemble_sizes(256)
+    mine = sharding.shard_of(sizes, world, rank)
+    systems = models.ensemble(sizes, indices=mine)
+    my_sizes = [int(sizes[i]) for i in mine]
+    cat = [np.concatenate([sy[k] for sy in systems]) for k in range(5)]
+    common = dict(theta=THETA, eps2=EPS * EPS, gravity=1.0, timestep=DT, dampening=1.0)
+    k = max(3, min(args.steps, 10))
+
+    def timed(step_fn):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(k):
+            step_fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3 / k
+
+    with bh.BarnesHutSystem(sizes=my_sizes, device=local, mode="mixed", use_graph=True,
+                            **common) as b:
+        b.set_state(*cat)
+        b.autotune(sp)
+        for _ in range(2):
+            b.step(1, sp)
+        t_batch = timed(lambda: b.step(1, sp))
+        inter = b.stats(sp)["interactions"]
+    handles = []
+    try:
+        for sy in systems:
+            h = bh.BarnesHutSystem(len(sy[0]), device=local, mode="plain", use_graph=False,
+                                   **common)
+            h.set_state(*sy)
+            handles.append(h)
+
+        def one_each():
+            for h in handles:
+                h.step(1, sp)
+
+        one_each()
+        t_each = timed(one_each)
+    finally:
+        for h in handles:
+            h.close()
+    if world > 1:
+        t = torch.tensor([t_batch, t_each], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_batch, t_each = float(t[0]), float(t[1])
+    return {"workload": "ensemble of 256 systems, N log-uniform in [2^10, 2^17]",
+            "bodies": int(np.sum(sizes)), "steps_timed": k,
+            "batched_mixed_graph_steps_per_s": round(1.0 / t_batch, 3),
+            "one_handle_per_system_plain_steps_per_s": round(1.0 / t_each, 3),
+            "batched_over_per_system": round(t_each / t_batch, 2),
+            "interactions_per_s": round(inter / t_batch, 1)}
 
 
 def cpu_baseline(x, y, vx, vy, m):
@@ -423,6 +496,8 @@ def main():
     ap.add_argument("--mode", choices=["mixed", "plain", "reference"], default="mixed")
     ap.add_argument("--bucket", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "engine":
         args.warmup = 3

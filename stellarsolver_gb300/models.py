@@ -82,13 +82,16 @@ def ensemble_sizes(count: int = 256, lo: int = 1 << 10, hi: int = 1 << 17, seed:
     return np.rint(np.exp(rng.uniform(np.log(lo), np.log(hi), count))).astype(np.int64).clip(lo, hi)
 
 
-def ensemble(sizes, seed_base: int = SEED_BASE + 3):
+def ensemble_system(i: int, n: int, seed_base: int = SEED_BASE + 3):
+    """System i of an ensemble: a disk for even i, a Plummer sphere for odd i."""
+    sd = seed_base + (i << 16)
+    return disk(int(n), sd) if i % 2 == 0 else plummer(int(n), sd)
+
+
+def ensemble(sizes, seed_base: int = SEED_BASE + 3, indices=None):
     """Alternating disk (even index) and Plummer (odd) systems, each with its own seed."""
-    out = []
-    for i, n in enumerate(sizes):
-        sd = seed_base + (i << 16)
-        out.append(disk(int(n), sd) if i % 2 == 0 else plummer(int(n), sd))
-    return out
+    idx = range(len(sizes)) if indices is None else indices
+    return [ensemble_system(i, sizes[i], seed_base) for i in idx]
 
 
 # Benchmark workloads with their integration parameters.
