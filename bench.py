@@ -40,7 +40,12 @@ N_BODIES = 1 << 20
 EPS = 0.01
 DT = 1e-4
 THETA = 0.5
-FLOPS_PER_INTERACTION = 14  # dx,dy 2; r^2 4; rsqrt 1; r^-3 2; m*r^-3 1; two FMAs 4
+# FP32 flops per interaction (an FMA counts 2, rsqrt 1), from the kernels' arithmetic:
+#   body-body  (p2p): dx,dy 2; u 4; rsqrt 1; r^-3 2; m*r^-3 1; two FMAs 4           = 14
+#   body-cell  (p2m): dx,dy 2; u 4; rsqrt 1; r^-2,r^-3 2; T.d 6; d.T.d 3; t 3;
+#                     coef 2; fx,fy 6; two FMAs 4                                    = 33
+FLOPS_P2P = 14
+FLOPS_P2M = 33
 LAUNCHES_PER_STEP = 32       # bbox, keys, sort 8 x (hist, scan, scatter), reorder, build, moments, records, walk x2
 
 
@@ -237,7 +242,8 @@ def run_engine(args):
     sysm.sync(sp)
     walk_ms = float(phase_ms[bh.PHASES.index("walk")])
     fp32_peak = bh.measure_fp32_peak(local)
-    walk_flops = FLOPS_PER_INTERACTION * stats["interactions"]
+    cell_inter = stats["cell_interactions"]
+    walk_flops = FLOPS_P2P * (stats["interactions"] - cell_inter) + FLOPS_P2M * cell_inter
     achieved = walk_flops / (walk_ms * 1e-3) / 1e12
     traffic = recorded_traffic("walk")
     pb = phase_bytes(n, args.mode == "mixed")
@@ -277,6 +283,8 @@ def run_engine(args):
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "timed_wall_s_incl_flush": round(t_wall, 3)},
         "interactions_per_step": stats["interactions"],
+        "cell_interactions_per_step": stats["cell_interactions"],
+        "walk_flops_per_step": walk_flops,
         "interactions_per_s": round(stats["interactions"] * value / world, 1) * world,
         "force_error_vs_fp64": errors,
         "plain_fp32": {"steps_per_s_graph": round(sides["plain_graph"], 3),

@@ -46,7 +46,8 @@ extern "C" {
  *   iff min over the group's bodies |COM - p| > l/theta + |COM - cell centre|
  *   (l = larger cell side) and G M l^3 / d^5 <= alpha |a_old| (previous
  *   step's |a|; the first step after bh_set_state bootstraps it with a
- *   geometric-only pass); leaf buckets; G applied.
+ *   geometric-only pass at opening angle max(theta, 1)); leaf buckets; G
+ *   applied.
  * MIXED: PLAIN plus compensated (Kahan) force sums and positions kept as
  *   hi + lo float pairs. */
 #define BH_MODE_REFERENCE 0
@@ -84,6 +85,7 @@ typedef struct bh_stats {
     int32_t max_stack;     /* deepest walk stack of the last step (PLAIN/MIXED) */
     int32_t walk_rounds;   /* warp rounds of node tests in the last step (PLAIN/MIXED) */
     int32_t nodes_tested;  /* nodes tested by the walk in the last step (PLAIN/MIXED) */
+    int64_t cell_interactions; /* of `interactions`, body-cell (quadrupole) ones (PLAIN/MIXED) */
 } bh_stats;
 
 /* Fill p with the reference's defaults: mode REFERENCE, theta 0.5, eps2 0.025,
@@ -114,7 +116,9 @@ int bh_num_bodies(const bh_system* s); /* getNumParticles() (BarnesHutParticleSy
 
 /* reset()'s host-to-device copy (BarnesHutParticleSystem.cpp:364-371).  Any
  * pointer may be host or device memory (cudaMemcpyDefault).  Accelerations
- * start at zero. */
+ * start at zero.  Asynchronous on `stream`, like cudaMemcpyAsync: pinned host
+ * or device sources must stay unchanged until the stream has passed the call
+ * (pageable host memory is staged before the call returns). */
 int bh_set_state(bh_system* s, const float* x, const float* y, const float* vx,
                  const float* vy, const float* mass, void* stream);
 

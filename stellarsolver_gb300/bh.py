@@ -47,7 +47,7 @@ class Stats(ctypes.Structure):
                 ("nodes", ctypes.c_int32), ("max_depth", ctypes.c_int32),
                 ("status", ctypes.c_int32), ("box", ctypes.c_float * 4),
                 ("max_stack", ctypes.c_int32), ("walk_rounds", ctypes.c_int32),
-                ("nodes_tested", ctypes.c_int32)]
+                ("nodes_tested", ctypes.c_int32), ("cell_interactions", ctypes.c_int64)]
 
 
 _lib = None
@@ -296,7 +296,8 @@ class BarnesHutSystem:
         return dict(interactions=int(s.interactions), cells=int(s.cells), nodes=int(s.nodes),
                     max_depth=int(s.max_depth), status=int(s.status), box=np.array(s.box[:]),
                     max_stack=int(s.max_stack), walk_rounds=int(s.walk_rounds),
-                    nodes_tested=int(s.nodes_tested))
+                    nodes_tested=int(s.nodes_tested),
+                    cell_interactions=int(s.cell_interactions))
 
     def debug(self, name: str):
         n = self.n

@@ -92,7 +92,7 @@ Workspace* workspace(size_t n, size_t m) {
     int tiles = (int)((N + kSortTile - 1) / kSortTile);
     int nb = (int)((N + 1023) / 1024);
     size_t bytes = 2 * al(8 * N) + 2 * al(4 * N) + al(4 * 256 * (size_t)tiles) + al(4 * 256) +
-                   al(16) + al(8) + 8 * al(4 * N) + 5 * al(4 * N) + al(16 * N) + 3 * al(4 * N) +
+                   al(16) + al(8) + 8 * al(4 * N) + al(16 * N) + 2 * al(16 * N) + 3 * al(4 * N) +
                    2 * al(4 * N) + al(4 * (size_t)nb) + al(4) + 2 * al(4 * M) + al(4);
     if (cudaMalloc(&w->base, bytes) != cudaSuccess) {
         w->base = nullptr;
@@ -121,12 +121,9 @@ Workspace* workspace(size_t n, size_t m) {
     w->tree.first = (int*)take(4 * N);
     w->tree.last = (int*)take(4 * N);
     w->counter = (int*)take(4 * N);
-    w->sums.m = (float*)take(4 * N);
-    w->sums.mx = (float*)take(4 * N);
-    w->sums.my = (float*)take(4 * N);
-    w->sums.cx = (float*)take(4 * N);
-    w->sums.cy = (float*)take(4 * N);
-    w->sums.quad = (float4*)take(16 * N);
+    w->tree.climb = (int4*)take(16 * N);
+    w->sums.s0 = (float4*)take(16 * N);
+    w->sums.s1 = (float4*)take(16 * N);
     w->sx = (float*)take(4 * N);
     w->sy = (float*)take(4 * N);
     w->sm = (float*)take(4 * N);
@@ -344,7 +341,8 @@ __global__ void k_c_materialize(int n, int m, TreePtrs t, const uint64_t* skeys,
     int b0 = n + cbase[q];
     uint64_t key = skeys[t.first[q]];
     int cnt = t.last[q] - t.first[q] + 1;
-    float M = sums.m[q], MX = sums.mx[q], MY = sums.my[q];
+    const float4 s0 = sums.s0[q];
+    const float M = s0.x, MX = s0.y, MY = s0.z;
     for (int k = 0; k < nc; ++k) {  // chain cells, then the node's own cell
         int id = b0 + k;
         int lev = Lp + 1 + k;
@@ -671,9 +669,8 @@ void compat_BuildQuadTree(float* x, float* y, float* mass, int* count, int* star
     k_c_gather3<<<nb, 256, 0, st>>>(n, va, x, y, mass, w->sx, w->sy, w->sm);
     k_build<<<nb, 256, 0, st>>>(ka, n, segs, w->tree, w->status);
     record_cuda(cudaMemsetAsync(w->counter, 0, sizeof(int) * n, st), "BuildQuadTree memset");
-    k_moments<256><<<nb, 256, 0, st>>>(n, 0, w->sx, w->sy, w->sm, w->tree.left, w->tree.right,
-                                       w->tree.parent, w->tree.leaf_parent, w->tree.first,
-                                       w->tree.last, w->counter, w->sums);
+    k_moments<<<(n + kMomentsThreads - 1) / kMomentsThreads, kMomentsThreads, 0, st>>>(
+        n, 0, w->sx, w->sy, w->sm, w->tree.climb, w->tree.leaf_parent, w->counter, w->sums);
     k_c_ncells<<<nb, 256, 0, st>>>(n, w->tree.split, w->tree.parent, w->ncell);
     const int sb = blocks_for(n, 1024);
     k_c_scan_block<<<sb, 1024, 0, st>>>(w->ncell, w->cbase, w->bsum, n);
@@ -764,7 +761,7 @@ void FillOutputArray(float* x, float* y, float* out, int n) { ssg::compat_FillOu
 // The existing wrapper grows a cached workspace with cudaMalloc.  This variant
 // takes its scratch from one file-scope __device__ array instead, sized for at
 // most kNoAllocMaxBodies bodies.  Every GPU that loads the library holds that
-// array (about 6 MiB) until the process exits.
+// array (about 8 MiB) until the process exits.
 // ---------------------------------------------------------------------------
 namespace {
 
@@ -777,8 +774,8 @@ constexpr size_t noalloc_bytes(size_t n) {
     return 2 * na_al(8 * n) + 2 * na_al(4 * n)                    // keys, values (ping-pong)
            + na_al(4 * 256 * ((n + kSortTile - 1) / kSortTile))  // digit histograms
            + na_al(4 * 256) + na_al(16) + na_al(8)                // totals, box, system offsets
-           + 8 * na_al(4 * n)                                     // tree arrays + counter
-           + 5 * na_al(4 * n)                                     // node sums
+           + 8 * na_al(4 * n) + na_al(16 * n)                     // tree arrays, counter, climb
+           + 2 * na_al(16 * n)                                    // node sums
            + 3 * na_al(4 * n)                                     // gathered x, y, m
            + 2 * na_al(4 * n)                                     // cells per node, cell base
            + na_al(4 * ((n + 1023) / 1024)) + na_al(4) + na_al(4);  // block sums, total, status
@@ -843,12 +840,9 @@ void noalloc_layout(unsigned char* base, size_t n, Workspace* w) {
     w->tree.first = (int*)take(4 * n);
     w->tree.last = (int*)take(4 * n);
     w->counter = (int*)take(4 * n);
-    w->sums.m = (float*)take(4 * n);
-    w->sums.mx = (float*)take(4 * n);
-    w->sums.my = (float*)take(4 * n);
-    w->sums.cx = (float*)take(4 * n);
-    w->sums.cy = (float*)take(4 * n);
-    w->sums.quad = nullptr;  // only written in the accuracy modes, never here
+    w->tree.climb = (int4*)take(16 * n);
+    w->sums.s0 = (float4*)take(16 * n);
+    w->sums.s1 = (float4*)take(16 * n);
     w->sx = (float*)take(4 * n);
     w->sy = (float*)take(4 * n);
     w->sm = (float*)take(4 * n);
@@ -903,9 +897,8 @@ extern "C" int BuildQuadTreeNoAlloc(float* x, float* y, float* mass, int* count,
     }
     k_c_gather3<<<nb, 256, 0, st>>>(n, va, x, y, mass, w.sx, w.sy, w.sm);
     k_build<<<nb, 256, 0, st>>>(ka, n, segs, w.tree, w.status);
-    k_moments<256><<<nb, 256, 0, st>>>(n, 0, w.sx, w.sy, w.sm, w.tree.left, w.tree.right,
-                                       w.tree.parent, w.tree.leaf_parent, w.tree.first,
-                                       w.tree.last, w.counter, w.sums);
+    k_moments<<<(n + kMomentsThreads - 1) / kMomentsThreads, kMomentsThreads, 0, st>>>(
+        n, 0, w.sx, w.sy, w.sm, w.tree.climb, w.tree.leaf_parent, w.counter, w.sums);
     k_c_ncells<<<nb, 256, 0, st>>>(n, w.tree.split, w.tree.parent, w.ncell);
     const int sb = blocks_for(n, 1024);
     k_c_scan_block<<<sb, 1024, 0, st>>>(w.ncell, w.cbase, w.bsum, n);

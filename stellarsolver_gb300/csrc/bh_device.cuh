@@ -215,30 +215,38 @@ __device__ __forceinline__ uint32_t radix_digit(uint64_t k, uint32_t v, int shif
 constexpr int kSortThreads = 256;
 constexpr int kSortItems = 8;
 constexpr int kSortTile = kSortThreads * kSortItems;
+static_assert(kSortThreads == 256, "one thread per digit in the sort kernels");
 
-// per-tile digit counts, written digit-major: hist[d * tiles + tile]
+// per-tile digit counts, written digit-major: hist[d * tiles + tile].  Each
+// warp counts into its own shared sub-histogram with plain shared atomics
+// (twice as fast as aggregating equal digits with warp votes first).
 static __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint64_t* __restrict__ keys,
                                                              const uint32_t* __restrict__ vals, int n,
                                                              int shift, int use_seg,
                                                              const int* __restrict__ seg_of_pos,
                                                              uint32_t* __restrict__ hist, int tiles) {
-    __shared__ uint32_t s_hist[256];
-    s_hist[threadIdx.x] = 0;
+    constexpr int W = kSortThreads / 32;
+    __shared__ uint32_t s_h[W][256];
+    for (int i = threadIdx.x; i < W * 256; i += kSortThreads) (&s_h[0][0])[i] = 0u;
     __syncthreads();
-    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
     const int base = blockIdx.x * kSortTile;
+    uint32_t dg[kSortItems];
 #pragma unroll
     for (int it = 0; it < kSortItems; ++it) {
         int idx = base + it * kSortThreads + threadIdx.x;
-        bool valid = idx < n;
-        uint32_t d = valid ? radix_digit(keys[idx], use_seg ? vals[idx] : 0u, shift, use_seg,
-                                         seg_of_pos)
-                           : 0u;
-        unsigned peers = __match_any_sync(kFull, valid ? d : 256u + lane);
-        if (valid && (__ffs(peers) - 1) == lane) atomicAdd(&s_hist[d], (uint32_t)__popc(peers));
+        dg[it] = idx < n ? radix_digit(keys[idx], use_seg ? vals[idx] : 0u, shift, use_seg,
+                                       seg_of_pos)
+                         : 256u;
     }
+#pragma unroll
+    for (int it = 0; it < kSortItems; ++it)
+        if (dg[it] < 256u) atomicAdd(&s_h[warp][dg[it]], 1u);
     __syncthreads();
-    hist[threadIdx.x * tiles + blockIdx.x] = s_hist[threadIdx.x];
+    uint32_t t = 0;
+#pragma unroll
+    for (int w = 0; w < W; ++w) t += s_h[w][threadIdx.x];
+    hist[threadIdx.x * tiles + blockIdx.x] = t;
 }
 
 // block d turns column d of hist into exclusive offsets; totals[d] = column sum
@@ -289,11 +297,16 @@ static __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(
     int dg[kSortItems];
     const unsigned lt = lanemask_lt();
 #pragma unroll
-    for (int r = 0; r < kSortItems; ++r) {
+    for (int r = 0; r < kSortItems; ++r) {  // the tile's loads, then the ranking
         int idx = base + warp * WCHUNK + r * 32 + lane;
         bool valid = idx < n;
         k[r] = valid ? kin[idx] : 0ull;
         v[r] = valid ? vin[idx] : 0u;
+    }
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        int idx = base + warp * WCHUNK + r * 32 + lane;
+        bool valid = idx < n;
         uint32_t d = valid ? radix_digit(k[r], v[r], shift, use_seg, seg_of_pos) : 0u;
         dg[r] = valid ? (int)d : -1;
         unsigned peers = __match_any_sync(kFull, valid ? d : 256u + lane);
@@ -372,7 +385,14 @@ __device__ __forceinline__ int kdelta(const uint64_t* __restrict__ k, int i, int
 
 struct TreePtrs {
     int *left, *right, *parent, *leaf_parent, *split, *first, *last;
+    int4* climb;  // per internal node: left, right, parent, range inside one moments block
 };
+
+// k_moments runs one thread per leaf in blocks of kMomentsThreads; a node whose
+// body range lies inside one block's leaves is combined with block-scope
+// synchronisation (climb record .w = 1).
+constexpr int kMomentsLog2 = 8;
+constexpr int kMomentsThreads = 1 << kMomentsLog2;
 
 // Karras (2012) radix-tree construction, one thread per internal node.
 static __global__ void k_build(const uint64_t* __restrict__ k, int n, Segs segs, TreePtrs t,
@@ -394,7 +414,10 @@ static __global__ void k_build(const uint64_t* __restrict__ k, int n, Segs segs,
         }
         return;
     }
-    if (i == lo) t.parent[i] = -1;
+    if (i == lo) {
+        t.parent[i] = -1;
+        t.climb[i].z = -1;
+    }
     int dl = kdelta(k, i, i - 1, lo, hi), dr = kdelta(k, i, i + 1, lo, hi);
     int d = dr > dl ? 1 : -1;
     int dmin = min(dl, dr);
@@ -413,142 +436,168 @@ static __global__ void k_build(const uint64_t* __restrict__ k, int n, Segs segs,
     }
     int g = i + sp * d + min(d, 0);
     int a = min(i, j), b = max(i, j);
+    int lc, rc;
     if (a == g) {
-        t.left[i] = ~g;
+        lc = ~g;
         t.leaf_parent[g] = i;
     } else {
-        t.left[i] = g;
+        lc = g;
         t.parent[g] = i;
+        t.climb[g].z = i;
     }
     if (b == g + 1) {
-        t.right[i] = ~(g + 1);
+        rc = ~(g + 1);
         t.leaf_parent[g + 1] = i;
     } else {
-        t.right[i] = g + 1;
+        rc = g + 1;
         t.parent[g + 1] = i;
+        t.climb[g + 1].z = i;
     }
+    t.left[i] = lc;
+    t.right[i] = rc;
     t.split[i] = dnode;
     t.first[i] = a;
     t.last[i] = b;
+    // .z (parent) is written by the parent's thread
+    t.climb[i].x = lc;
+    t.climb[i].y = rc;
+    t.climb[i].w = (a >> kMomentsLog2) == (b >> kMomentsLog2);
 }
 
 // ------------------------------------------------------------------ (c) moments
 
+// Node sums, two 16-byte records per node so that a child is read with two
+// loads (REFERENCE: one) and a node written with two stores.
 struct NodeSums {
-    float *m, *mx, *my, *cx, *cy;
-    float4* quad;  // Sxx, Sxy, Syy about the centre of mass (accuracy modes)
+    float4* s0;  // M, sum m*x, sum m*y, centre-of-mass x
+    float4* s1;  // centre-of-mass y, Sxx, Sxy, Syy (second moments about it; accuracy modes)
 };
 
 struct ChildVals {
     float m, mx, my, cx, cy, sxx, sxy, syy;
 };
 
+__device__ __forceinline__ ChildVals body_vals(int bi, const float* __restrict__ sx,
+                                               const float* __restrict__ sy,
+                                               const float* __restrict__ sm) {
+    ChildVals v;
+    v.m = sm[bi];
+    v.cx = sx[bi];
+    v.cy = sy[bi];
+    v.mx = __fmul_rn(v.m, v.cx);  // kernels.cu:180: mass*x
+    v.my = __fmul_rn(v.m, v.cy);
+    v.sxx = v.sxy = v.syy = 0.0f;
+    return v;
+}
+
 __device__ __forceinline__ ChildVals load_child(int c, const float* __restrict__ sx,
                                                 const float* __restrict__ sy,
                                                 const float* __restrict__ sm, const NodeSums& ns,
                                                 bool quad) {
+    if (c < 0) return body_vals(~c, sx, sy, sm);
+    // written by another thread of this launch: read through L2
     ChildVals v;
-    if (c < 0) {
-        int bi = ~c;
-        v.m = sm[bi];
-        v.cx = sx[bi];
-        v.cy = sy[bi];
-        v.mx = __fmul_rn(v.m, v.cx);  // kernels.cu:180: mass*x
-        v.my = __fmul_rn(v.m, v.cy);
-        v.sxx = v.sxy = v.syy = 0.0f;
+    const float4 a = __ldcg(ns.s0 + c);
+    v.m = a.x;
+    v.mx = a.y;
+    v.my = a.z;
+    v.cx = a.w;
+    if (quad) {
+        const float4 b = __ldcg(ns.s1 + c);
+        v.cy = b.x;
+        v.sxx = b.y;
+        v.sxy = b.z;
+        v.syy = b.w;
     } else {
-        // written by another thread of this launch: read through L2
-        v.m = __ldcg(ns.m + c);
-        v.mx = __ldcg(ns.mx + c);
-        v.my = __ldcg(ns.my + c);
-        v.cx = __ldcg(ns.cx + c);
-        v.cy = __ldcg(ns.cy + c);
-        if (quad) {
-            float4 q = __ldcg(ns.quad + c);
-            v.sxx = q.x;
-            v.sxy = q.y;
-            v.syy = q.z;
-        } else {
-            v.sxx = v.sxy = v.syy = 0.0f;
-        }
+        v.cy = 0.0f;  // not an input of the REFERENCE combination
+        v.sxx = v.sxy = v.syy = 0.0f;
     }
     return v;
 }
 
-__device__ __forceinline__ void combine_node(int p, int accuracy, const float* __restrict__ sx,
-                                             const float* __restrict__ sy,
-                                             const float* __restrict__ sm,
-                                             const int* __restrict__ left,
-                                             const int* __restrict__ right, const NodeSums& ns) {
-    ChildVals a = load_child(left[p], sx, sy, sm, ns, accuracy);
-    ChildVals b = load_child(right[p], sx, sy, sm, ns, accuracy);
-    float M = __fadd_rn(a.m, b.m);
-    float MX = __fadd_rn(a.mx, b.mx);
-    float MY = __fadd_rn(a.my, b.my);
-    float cx, cy;
+// Node p from its left child a and right child b; returns p's values.
+__device__ __forceinline__ ChildVals combine_node(int p, const ChildVals& a, const ChildVals& b,
+                                                  int accuracy, const NodeSums& ns) {
+    ChildVals r;
+    r.m = __fadd_rn(a.m, b.m);
+    r.mx = __fadd_rn(a.mx, b.mx);
+    r.my = __fadd_rn(a.my, b.my);
     if (!accuracy) {
-        cx = __fdiv_rn(MX, M);
-        cy = __fdiv_rn(MY, M);
+        r.cx = __fdiv_rn(r.mx, r.m);
+        r.cy = __fdiv_rn(r.my, r.m);
+        r.sxx = r.sxy = r.syy = 0.0f;
     } else {
-        float w = M > 0.0f ? b.m / M : 0.5f;
-        cx = fmaf(w, b.cx - a.cx, a.cx);
-        cy = fmaf(w, b.cy - a.cy, a.cy);
-        float ax = a.cx - cx, ay = a.cy - cy, bx = b.cx - cx, by = b.cy - cy;
-        float sxx = a.sxx + b.sxx + a.m * ax * ax + b.m * bx * bx;
-        float sxy = a.sxy + b.sxy + a.m * ax * ay + b.m * bx * by;
-        float syy = a.syy + b.syy + a.m * ay * ay + b.m * by * by;
-        ns.quad[p] = make_float4(sxx, sxy, syy, 0.0f);
+        float w = r.m > 0.0f ? b.m / r.m : 0.5f;
+        r.cx = fmaf(w, b.cx - a.cx, a.cx);
+        r.cy = fmaf(w, b.cy - a.cy, a.cy);
+        float ax = a.cx - r.cx, ay = a.cy - r.cy, bx = b.cx - r.cx, by = b.cy - r.cy;
+        r.sxx = a.sxx + b.sxx + a.m * ax * ax + b.m * bx * bx;
+        r.sxy = a.sxy + b.sxy + a.m * ax * ay + b.m * bx * by;
+        r.syy = a.syy + b.syy + a.m * ay * ay + b.m * by * by;
     }
-    ns.m[p] = M;
-    ns.mx[p] = MX;
-    ns.my[p] = MY;
-    ns.cx[p] = cx;
-    ns.cy[p] = cy;
+    ns.s0[p] = make_float4(r.m, r.mx, r.my, r.cx);
+    ns.s1[p] = make_float4(r.cy, r.sxx, r.sxy, r.syy);
+    return r;
 }
 
 // Bottom-up: each body climbs from its leaf; the second thread to reach a node
 // combines both children (left + right, so the sums do not depend on which
 // thread arrives last) and continues.  REFERENCE mode keeps the reference's
 // definition com = (sum m*x) / (sum m) (kernels.cu:283-284); accuracy modes
-// combine centres relative to each other and add second moments.
+// combine centres relative to each other and add second moments.  The child a
+// thread climbs from stays in its registers; only the sibling is loaded.
 //
-// A warp owns 32 consecutive leaves.  A node whose body range lies inside its
-// warp's 32 leaves is reached only by lanes of that warp: its arrival counter
-// lives in shared memory and block-scope fences order the child data.  Only
-// nodes that span two warps' leaves use a global counter and device-scope
-// fences.
-template <int THREADS>
-static __global__ void __launch_bounds__(THREADS) k_moments(int n, int accuracy, const float* __restrict__ sx,
+// A block owns kMomentsThreads consecutive leaves.  A node whose body range
+// lies inside them is reached only by threads of that block: its arrival
+// counter lives in shared memory and block-scope fences order the child data.
+// Only nodes that span two blocks' leaves use a global counter, taken with one
+// acquire-release atomic: its release publishes the node this thread wrote,
+// its acquire makes the sibling's sums visible to the loads that follow.  The
+// parent's climb record is loaded while the counter is taken.
+__device__ __forceinline__ int atomic_add_acq_rel_gpu(int* p, int v) {
+    int old;
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;"
+                 : "=r"(old)
+                 : "l"(p), "r"(v)
+                 : "memory");
+    return old;
+}
+
+static __global__ void __launch_bounds__(kMomentsThreads) k_moments(int n, int accuracy, const float* __restrict__ sx,
                                                      const float* __restrict__ sy,
                                                      const float* __restrict__ sm,
-                                                     const int* __restrict__ left,
-                                                     const int* __restrict__ right,
-                                                     const int* __restrict__ parent,
+                                                     const int4* __restrict__ climb,
                                                      const int* __restrict__ leaf_parent,
-                                                     const int* __restrict__ first,
-                                                     const int* __restrict__ last,
                                                      int* __restrict__ counter, NodeSums ns) {
-    __shared__ int s_cnt[THREADS];
-    const int j = blockIdx.x * THREADS + threadIdx.x;
+    __shared__ int s_cnt[kMomentsThreads];
+    const int c0 = blockIdx.x * kMomentsThreads;  // this block's leaves: [c0, c0 + kMomentsThreads)
+    const int j = c0 + threadIdx.x;
     s_cnt[threadIdx.x] = 0;
-    __syncwarp();
+    __syncthreads();
     if (j >= n) return;
-    const int c0 = j & ~31;  // this warp's leaves: [c0, c0 + 32)
-    int* wcnt = s_cnt + (threadIdx.x & ~31);
     int p = leaf_parent[j];
-    while (p >= 0) {
-        const bool local = first[p] >= c0 && last[p] < c0 + 32;
-        if (local) {
+    if (p < 0) return;
+    int4 T = climb[p];  // left, right, parent, range inside one 32-leaf chunk
+    int from = ~j;      // the child this thread climbs from
+    ChildVals own = body_vals(j, sx, sy, sm);
+    for (;;) {
+        int4 TN = make_int4(0, 0, -1, 0);
+        if (T.z >= 0) TN = climb[T.z];
+        if (T.w) {
             __threadfence_block();
-            if (atomicAdd(wcnt + (p - c0), 1) == 0) return;
+            if (atomicAdd(s_cnt + (p - c0), 1) == 0) return;
             __threadfence_block();
         } else {
-            __threadfence();
-            if (atomicAdd(counter + p, 1) == 0) return;
-            __threadfence();
+            if (atomic_add_acq_rel_gpu(counter + p, 1) == 0) return;
         }
-        combine_node(p, accuracy, sx, sy, sm, left, right, ns);
-        p = parent[p];
+        const bool from_left = T.x == from;
+        const ChildVals sib = load_child(from_left ? T.y : T.x, sx, sy, sm, ns, accuracy);
+        own = from_left ? combine_node(p, own, sib, accuracy, ns)
+                        : combine_node(p, sib, own, accuracy, ns);
+        if (T.z < 0) return;
+        from = p;
+        p = T.z;
+        T = TN;
     }
 }
 
@@ -592,6 +641,11 @@ __device__ __forceinline__ float ref_dp(Box bx, float theta, int level) {
 
 // Walk record of branching node i, from its sums and the tree (the body of
 // k_records).
+// Opening angle of the bootstrap pass (|a| estimate after bh_set_state).  At
+// 1.0 its |a| is within ~5% RMS and costs ~40% of the theta = 0.5 walk; the
+// relative rule it feeds opens the same nodes as with exact |a| to within 0.1%.
+constexpr float kBootstrapTheta = 1.0f;
+
 __device__ __forceinline__ void emit_record(int i, int sp, int accuracy, float theta, float G,
                                             const int* __restrict__ box_ord, int seg,
                                             const uint64_t* __restrict__ skeys,
@@ -634,7 +688,9 @@ __device__ __forceinline__ void emit_record(int i, int sp, int accuracy, float t
     const float r = l / theta + delta;
     rec.A[i] = make_float4(cx, cy, M, r * r);
     const float qerr = G * M * l * l * l;
-    rec.D[i] = make_int4(f, cnt, __float_as_int(qerr), 0);
+    // the bootstrap pass only needs |a| to a few per cent: a wider opening angle
+    const float rb = l / fmaxf(theta, kBootstrapTheta) + delta;
+    rec.D[i] = make_int4(f, cnt, __float_as_int(qerr), __float_as_int(rb * rb));
     rec.B[i] = make_float4(3.0f * quad.x, 3.0f * quad.y, 3.0f * quad.z, 1.5f * (quad.x + quad.z));
 }
 
@@ -647,9 +703,10 @@ static __global__ void k_records(int n, Segs segs, int accuracy, float theta, fl
     if (sp < 0) return;  // unused slot
     const int pa = t.parent[i];
     if (pa >= 0 && merged_into(sp, t.split[pa])) return;  // folded into its parent
-    const float4 q = accuracy ? ns.quad[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    emit_record(i, sp, accuracy, theta, G, box_ord, seg_of(segs, i), skeys, t, ns.m[i], ns.cx[i],
-                ns.cy[i], q, rec);
+    const float4 a = ns.s0[i], b = ns.s1[i];
+    const float4 q = accuracy ? make_float4(b.y, b.z, b.w, 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+    emit_record(i, sp, accuracy, theta, G, box_ord, seg_of(segs, i), skeys, t, a.x, a.w, b.x, q,
+                rec);
 }
 
 }  // namespace ssg

@@ -239,7 +239,7 @@ int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev)
     Segs segs{s->nseg, s->seg_off, s->nseg > 1 ? s->seg_of_pos : nullptr};
     CK(cudaMemsetAsync(s->box_ord, 0, sizeof(int) * 4 * s->nseg, st));  // origin box
     CK(cudaMemsetAsync(s->counter, 0, sizeof(int) * n, st));
-    CK(cudaMemsetAsync(s->inter, 0, sizeof(unsigned long long), st));
+    CK(cudaMemsetAsync(s->inter, 0, 2 * sizeof(unsigned long long), st));
     CK(cudaMemsetAsync(s->work, 0, 6 * sizeof(int), st));
 
     BodyPtrs cur = s->st[0];
@@ -282,9 +282,9 @@ int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev)
     CK(mark(4));
     k_build<<<nb, tb, 0, st>>>(ka, n, segs, s->tree, s->status);
     CK(mark(5));
-    k_moments<256><<<nb, 256, 0, st>>>(n, accuracy ? 1 : 0, dst.x, dst.y, dst.m, s->tree.left,
-                                       s->tree.right, s->tree.parent, s->tree.leaf_parent,
-                                       s->tree.first, s->tree.last, s->counter, s->sums);
+    k_moments<<<(n + kMomentsThreads - 1) / kMomentsThreads, kMomentsThreads, 0, st>>>(
+        n, accuracy ? 1 : 0, dst.x, dst.y, dst.m, s->tree.climb, s->tree.leaf_parent, s->counter,
+        s->sums);
     k_records<<<nb, tb, 0, st>>>(n, segs, accuracy ? 1 : 0, s->p.theta, s->p.gravity, s->box_ord,
                                  ka, s->tree, s->sums, s->rec);
     CK(cudaGetLastError());
@@ -396,9 +396,23 @@ int build_graph(bh_system* s) {
     return BH_OK;
 }
 
-__global__ void k_iota(int* id, int n) {
+// State of a freshly loaded system: caller order, zero position tails and
+// accelerations, status cleared, bootstrap pass requested.
+__global__ void k_state_init(int n, int* id, float* xlo, float* ylo, float* ax, float* ay,
+                             float* amag, int* status, int* fresh) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) id[i] = i;
+    if (i < n) {
+        id[i] = i;
+        xlo[i] = 0.0f;
+        ylo[i] = 0.0f;
+        ax[i] = 0.0f;
+        ay[i] = 0.0f;
+        amag[i] = 0.0f;
+    }
+    if (i == 0) {
+        *status = 0;
+        *fresh = 1;
+    }
 }
 
 // out[id[j]] = in[j] for up to four arrays
@@ -481,11 +495,11 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     bytes += span<uint32_t>((size_t)256 * s->tiles) + span<uint32_t>(256);
     bytes += span<int>(4 * (size_t)nseg) + 2 * span<int>(nseg + 1) + span<int>(N);
     bytes += 3 * span<int>(s->nchunks);
-    bytes += 8 * span<int>(N);
-    bytes += 5 * span<float>(N) + span<float4>(N);
-    bytes += 2 * span<float4>(N) + 2 * span<int4>(N);
-    bytes += 2 * span<float>(N) + span<int>(1) + span<unsigned long long>(1) + span<int>(9) + span<double>(4 * (size_t)nseg) +
-             span<int>(1);
+    bytes += 8 * span<int>(N) + span<int4>(N);                  // tree arrays, counter, climb
+    bytes += 2 * span<float4>(N);                               // node sums
+    bytes += 2 * span<float4>(N) + 2 * span<int4>(N);           // walk records
+    bytes += 2 * span<float>(N) + span<int>(1) + span<unsigned long long>(2) + span<int>(9) +
+             span<double>(4 * (size_t)nseg) + span<int>(1);
     cudaError_t e = cudaMalloc(&s->arena, bytes);
     if (e != cudaSuccess) {
         cuda_fail(e, "cudaMalloc(arena)");
@@ -527,12 +541,9 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     s->tree.first = carve<int>(c, N);
     s->tree.last = carve<int>(c, N);
     s->counter = carve<int>(c, N);
-    s->sums.m = carve<float>(c, N);
-    s->sums.mx = carve<float>(c, N);
-    s->sums.my = carve<float>(c, N);
-    s->sums.cx = carve<float>(c, N);
-    s->sums.cy = carve<float>(c, N);
-    s->sums.quad = carve<float4>(c, N);
+    s->tree.climb = carve<int4>(c, N);
+    s->sums.s0 = carve<float4>(c, N);
+    s->sums.s1 = carve<float4>(c, N);
     s->rec.A = carve<float4>(c, N);
     s->rec.B = carve<float4>(c, N);
     s->rec.C = carve<int4>(c, N);
@@ -540,7 +551,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     s->ax = carve<float>(c, N);
     s->ay = carve<float>(c, N);
     s->status = carve<int>(c, 1);
-    s->inter = carve<unsigned long long>(c, 1);
+    s->inter = carve<unsigned long long>(c, 2);  // all interactions, body-cell ones
     s->work = carve<int>(c, 9);
     s->diag = carve<double>(c, 4 * (size_t)nseg);
     s->fresh = carve<int>(c, 1);
@@ -675,17 +686,9 @@ int bh_set_state(bh_system* s, const float* x, const float* y, const float* vx, 
     CK(cudaMemcpyAsync(c.vx, vx, b, cudaMemcpyDefault, st));
     CK(cudaMemcpyAsync(c.vy, vy, b, cudaMemcpyDefault, st));
     CK(cudaMemcpyAsync(c.m, mass, b, cudaMemcpyDefault, st));
-    CK(cudaMemsetAsync(c.xlo, 0, b, st));
-    CK(cudaMemsetAsync(c.ylo, 0, b, st));
-    CK(cudaMemsetAsync(s->ax, 0, b, st));
-    CK(cudaMemsetAsync(s->ay, 0, b, st));
-    CK(cudaMemsetAsync(s->status, 0, sizeof(int), st));
-    CK(cudaMemsetAsync(c.amag, 0, b, st));
-    const int one = 1;
-    CK(cudaMemcpyAsync(s->fresh, &one, sizeof(int), cudaMemcpyHostToDevice, st));
-    k_iota<<<(s->n + 255) / 256, 256, 0, st>>>(c.id, s->n);
+    k_state_init<<<(s->n + 255) / 256, 256, 0, st>>>(s->n, c.id, c.xlo, c.ylo, s->ax, s->ay,
+                                                     c.amag, s->status, s->fresh);
     CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(st));  // `one` lives on this stack frame
     s->have_state = true;
     s->caller_order = true;
     return BH_OK;
@@ -807,7 +810,7 @@ int bh_get_stats(bh_system* s, bh_stats* out, void* stream) {
     CK(cudaSetDevice(s->device));
     CK(cudaStreamSynchronize((cudaStream_t)stream));
     int bits = 0;
-    unsigned long long inter = 0;
+    unsigned long long inter[2] = {0, 0};
     int box[4] = {0, 0, 0, 0};
     int wst[3] = {0, 0, 0};
     CK(cudaMemcpy(wst, s->work + 3, sizeof(wst), cudaMemcpyDeviceToHost));
@@ -815,10 +818,11 @@ int bh_get_stats(bh_system* s, bh_stats* out, void* stream) {
     out->walk_rounds = wst[1];
     out->nodes_tested = wst[2];
     CK(cudaMemcpy(&bits, s->status, sizeof(int), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(&inter, s->inter, sizeof(inter), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(inter, s->inter, sizeof(inter), cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(box, s->box_ord, sizeof(box), cudaMemcpyDeviceToHost));
     out->status = status_code(bits, s->p.mode);
-    out->interactions = (int64_t)inter;
+    out->interactions = (int64_t)inter[0];
+    out->cell_interactions = (int64_t)inter[1];
     for (int k = 0; k < 4; ++k) {
         int i = box[k];
         int b = i >= 0 ? i : (i ^ 0x7fffffff);
@@ -882,12 +886,19 @@ int bh_get_debug(bh_system* s, const char* name, void* host_out, size_t bytes, v
     else if (nm == "node_first") { src = s->tree.first; need = 4 * N; }
     else if (nm == "node_last") { src = s->tree.last; need = 4 * N; }
     else if (nm == "node_parent") { src = s->tree.parent; need = 4 * N; }
-    else if (nm == "node_m") { src = s->sums.m; need = 4 * N; }
-    else if (nm == "node_mx") { src = s->sums.mx; need = 4 * N; }
-    else if (nm == "node_my") { src = s->sums.my; need = 4 * N; }
-    else if (nm == "node_cx") { src = s->sums.cx; need = 4 * N; }
-    else if (nm == "node_cy") { src = s->sums.cy; need = 4 * N; }
-    else return BH_ERR_ARG;
+    else {
+        // node sums: one float of the 16-byte records, a strided copy
+        const float* f = nullptr;
+        if (nm == "node_m") f = &s->sums.s0->x;
+        else if (nm == "node_mx") f = &s->sums.s0->y;
+        else if (nm == "node_my") f = &s->sums.s0->z;
+        else if (nm == "node_cx") f = &s->sums.s0->w;
+        else if (nm == "node_cy") f = &s->sums.s1->x;
+        else return BH_ERR_ARG;
+        if (bytes < 4 * N) return BH_ERR_ARG;
+        CK(cudaMemcpy2D(host_out, 4, f, sizeof(float4), 4, N, cudaMemcpyDeviceToHost));
+        return BH_OK;
+    }
     if (!src) return BH_ERR_STATE;
     if (bytes < need) return BH_ERR_ARG;
     CK(cudaMemcpy(host_out, src, need, cudaMemcpyDeviceToHost));

@@ -254,8 +254,9 @@ __host__ __device__ __forceinline__ int acc_warp_bytes(AccShape sh) {
 }
 
 // PLAIN / MIXED walk.  ESTIMATE = the bootstrap pass after bh_set_state: the
-// geometric rule only, writes |G a| into in.amag and nothing else (skipped
-// unless *fresh is set).  The main pass also applies the relative rule
+// geometric rule only, at opening angle max(theta, kBootstrapTheta) (radius
+// in recD.w), writes |G a| into in.amag and nothing else (skipped unless
+// *fresh is set).  The main pass also applies the relative rule
 //   G M l^3 <= alpha * a_g * d^5,  a_g = max(min |a_old|, 0.1 mean |a_old|) over the group,
 // d = min over the group's bodies of |COM - p|; the geometric rule is d > l/theta + delta.
 // DIAG = diagnostics pass: the main rule, but each body's potential (FP64
@@ -291,7 +292,7 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
     int* clist = reinterpret_cast<int*>(gp + 32);
     int* stack = clist + 64;
     int* blist = stack + ((STACK + 3) & ~3);
-    unsigned long long my_inter = 0;
+    unsigned long long my_inter = 0, my_cinter = 0;
 
     const int WARPS = blockDim.x >> 5;
     (void)WARPS;
@@ -329,7 +330,7 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
         float ax = 0.0f, ay = 0.0f;     // running sums
         float cax = 0.0f, cay = 0.0f;   // Kahan compensation (MIXED)
         double phi = 0.0;               // DIAG: potential
-        long long entries = 0;
+        long long entries = 0, centries = 0;
         bool overflow = false;
         int top = 0, ccnt = 0, bcnt = 0, peak = 0, rounds = 0, tested = 0;
         if (hi - lo >= 2) {
@@ -371,6 +372,7 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
             add_batch(bx, by);
             ccnt -= k;
             entries += k;
+            centries += k;
         };
         auto flush_bodies = [&](int k) {
             __syncwarp();
@@ -435,6 +437,7 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
             if (node >= 0) {
                 A = recA[node];
                 D = recD[node];
+                if (ESTIMATE) A.w = __int_as_float(D.w);  // bootstrap opening radius
                 const float ddx = fmaxf(fmaxf(gx0 - A.x, A.x - gx1), 0.0f);
                 const float ddy = fmaxf(fmaxf(gy0 - A.y, A.y - gy1), 0.0f);
                 d2 = fmaf(ddx, ddx, ddy * ddy);
@@ -517,6 +520,7 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
             continue;
         }
         my_inter += (unsigned long long)(entries * cnt);
+        my_cinter += (unsigned long long)(centries * cnt);
         if (valid) {
             float vx = fmaf(dt, gax, in.vx[j]);
             float vy = fmaf(dt, gay, in.vy[j]);
@@ -549,7 +553,10 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
             out.amag[j] = sqrtf(gax * gax + gay * gay);
         }
     }
-    if (!ESTIMATE && !DIAG && lane == 0 && my_inter) atomicAdd(inter_total, my_inter);
+    if (!ESTIMATE && !DIAG && lane == 0 && my_inter) {
+        atomicAdd(inter_total, my_inter);
+        atomicAdd(inter_total + 1, my_cinter);  // of which body-cell
+    }
 }
 
 }  // namespace ssg
