@@ -249,9 +249,14 @@ __host__ __device__ __forceinline__ int acc_body_cap(int bucket) {
     return 32 + 32 * (bucket > 4 ? bucket : 4);
 }
 __host__ __device__ __forceinline__ int acc_warp_bytes(AccShape sh) {
-    return 3 * 32 * 16 + 32 * 8 + 64 * 4 + ((sh.stack * 4 + 15) & ~15) +
+    return 3 * 32 * 16 + 32 * 8 + 16 + 64 * 4 + ((sh.stack * 4 + 15) & ~15) +
            ((acc_body_cap(sh.bucket) * 4 + 15) & ~15);
 }
+
+// Below this many lanes the exact group distance is taken cooperatively
+// (each lane measures its own body, then a warp minimum) instead of by a
+// loop over the 32 bodies in every lane.
+constexpr int kSerialExactLanes = 8;
 
 // PLAIN / MIXED walk.  ESTIMATE = the bootstrap pass after bh_set_state: the
 // geometric rule only, at opening angle max(theta, kBootstrapTheta) (radius
@@ -289,7 +294,8 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
     float4* cB = cA + 32;
     float4* bP = cB + 32;
     float2* gp = reinterpret_cast<float2*>(bP + 32);
-    int* clist = reinterpret_cast<int*>(gp + 32);
+    float4* gext = reinterpret_cast<float4*>(gp + 32);  // y at min/max x, x at min/max y
+    int* clist = reinterpret_cast<int*>(gext + 1);
     int* stack = clist + 64;
     int* blist = stack + ((STACK + 3) & ~3);
     unsigned long long my_inter = 0, my_cinter = 0;
@@ -315,6 +321,15 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
             gy1 = fmaxf(gy1, __shfl_xor_sync(kFull, gy1, o));
         }
         const float gdiag = sqrtf((gx1 - gx0) * (gx1 - gx0) + (gy1 - gy0) * (gy1 - gy0));
+        {
+            // the group's extreme bodies in x and y: the nearest of them bounds
+            // the exact group distance from above
+            const float ya = __shfl_sync(kFull, py, __ffs(__ballot_sync(kFull, px == gx0)) - 1);
+            const float yb = __shfl_sync(kFull, py, __ffs(__ballot_sync(kFull, px == gx1)) - 1);
+            const float xa = __shfl_sync(kFull, px, __ffs(__ballot_sync(kFull, py == gy0)) - 1);
+            const float xb = __shfl_sync(kFull, px, __ffs(__ballot_sync(kFull, py == gy1)) - 1);
+            if (lane == 0) *gext = make_float4(ya, yb, xa, xb);
+        }
         // relative-rule scale of the group
         float aa = __int_as_float(0x7f800000);
         if (!ESTIMATE && !DIAG && alpha > 0.0f) {
@@ -447,14 +462,47 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
                 }
             }
             if (__any_sync(kFull, need)) {
-                float e2 = __int_as_float(0x7f800000);
-#pragma unroll 8
-                for (int e = 0; e < 32; ++e) {
-                    float2 q = gp[e];
-                    float dx = q.x - A.x, dy = q.y - A.y;
-                    e2 = fminf(e2, fmaf(dx, dx, dy * dy));
+                if (need) {
+                    // an extreme body within the opening radius: the node is opened
+                    const float4 ge = *gext;
+                    float dx = gx0 - A.x, dy = ge.x - A.y;
+                    float ub = fmaf(dx, dx, dy * dy);
+                    dx = gx1 - A.x;
+                    dy = ge.y - A.y;
+                    ub = fminf(ub, fmaf(dx, dx, dy * dy));
+                    dx = ge.z - A.x;
+                    dy = gy0 - A.y;
+                    ub = fminf(ub, fmaf(dx, dx, dy * dy));
+                    dx = ge.w - A.x;
+                    dy = gy1 - A.y;
+                    ub = fminf(ub, fmaf(dx, dx, dy * dy));
+                    if (ub <= A.w) {
+                        d2 = ub;
+                        need = false;
+                    }
                 }
-                if (need) d2 = e2;
+                unsigned nm = __ballot_sync(kFull, need);
+                if (__popc(nm) > kSerialExactLanes) {
+                    float e2 = __int_as_float(0x7f800000);
+#pragma unroll 8
+                    for (int e = 0; e < 32; ++e) {
+                        float2 q = gp[e];
+                        float dx = q.x - A.x, dy = q.y - A.y;
+                        e2 = fminf(e2, fmaf(dx, dx, dy * dy));
+                    }
+                    if (need) d2 = e2;
+                } else {
+                    while (nm) {
+                        const int src = __ffs(nm) - 1;
+                        nm &= nm - 1;
+                        const float dx = px - __shfl_sync(kFull, A.x, src);
+                        const float dy = py - __shfl_sync(kFull, A.y, src);
+                        float e2 = fmaf(dx, dx, dy * dy);
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) e2 = fminf(e2, __shfl_xor_sync(kFull, e2, o));
+                        if (lane == src) d2 = e2;
+                    }
+                }
             }
             if (node >= 0) {
                 bool acc = d2 > A.w;
