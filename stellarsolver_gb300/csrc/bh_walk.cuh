@@ -202,12 +202,22 @@ __device__ __forceinline__ float pot_cell(float4 A, float4 B, float px, float py
     return -(A.z * ri + 0.5f * dtd * r3 * r2 - (B.w * (1.0f / 3.0f)) * r3);
 }
 
+// PTX rsqrt.approx.ftz.f32: the approximate reciprocal square root without the
+// denormal-argument handling that rsqrtf adds (three instructions per call).
+// Used where the argument is a squared distance plus a positive softening, or
+// a squared distance beyond an opening radius: never a denormal.
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 template <bool GUARD>
 __device__ __forceinline__ void p2p(float bx, float by, float bm, float px, float py, float eps2,
                                     float& ax, float& ay) {
     float dx = bx - px, dy = by - py;
     float u = fmaf(dx, dx, fmaf(dy, dy, eps2));
-    float ri = rsqrtf(u);
+    float ri = GUARD ? rsqrtf(u) : rsqrt_ftz(u);  // GUARD: eps2 == 0, u may be tiny
     if (GUARD) ri = u > 0.0f ? ri : 0.0f;
     float f = bm * ri * ri * ri;
     ax = fmaf(f, dx, ax);
@@ -222,7 +232,7 @@ __device__ __forceinline__ void p2m(float4 A, float4 B, float px, float py, floa
                                     float& ay) {
     float dx = A.x - px, dy = A.y - py;
     float u = fmaf(dx, dx, fmaf(dy, dy, eps2));
-    float ri = rsqrtf(u);
+    float ri = rsqrt_ftz(u);
     float r2 = ri * ri;
     float r3 = ri * r2;
     float tdx = fmaf(B.x, dx, B.y * dy);
