@@ -246,6 +246,70 @@ __device__ __forceinline__ void p2m(float4 A, float4 B, float px, float py, floa
     ay = fmaf(r3, fy, ay);
 }
 
+// Two interactions per lane with packed FP32x2 arithmetic (__ffma2_rn and
+// friends: per component the same IEEE operations as the scalar code).  The
+// walk stages cells and bodies in pairs: component .x belongs to the even
+// entry, .y to the odd one.
+//   cells:  xy = (x, y)  mh = (M, -h)  t01 = (-T00, -T01)  t11 = -T11   (T = 3S, h = 1.5 tr S)
+//   bodies: xy = (x, y)  m              index
+// The quadrupole terms are staged negated, so that every subtraction of p2m
+// becomes an FMA with a positive addend: -(T d) = T' d, d.T.d = -(d.T'.d).
+// Staged cell pairs, one array per component (conflict-free staging stores).
+struct CellPairs {
+    float4* xy;   // x0 x1 y0 y1
+    float4* mh;   // M0 M1 -h0 -h1
+    float4* t01;  // -T00_0 -T00_1 -T01_0 -T01_1
+    float2* t11;  // -T11_0 -T11_1
+};
+
+__device__ __forceinline__ void p2m_pair(const float4 xy, const float4 mh, const float4 t01,
+                                         const float2 t11, const float2 npx, const float2 npy,
+                                         const float2 e2, float2& ax, float2& ay) {
+    const float2 dx = __fadd2_rn(make_float2(xy.x, xy.y), npx);
+    const float2 dy = __fadd2_rn(make_float2(xy.z, xy.w), npy);
+    const float2 u = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, e2));
+    const float2 ri = make_float2(rsqrt_ftz(u.x), rsqrt_ftz(u.y));
+    const float2 r2 = __fmul2_rn(ri, ri);
+    const float2 r3 = __fmul2_rn(ri, r2);
+    const float2 txx = make_float2(t01.x, t01.y), txy = make_float2(t01.z, t01.w);
+    const float2 tdx = __ffma2_rn(txx, dx, __fmul2_rn(txy, dy));  // -(T d).x
+    const float2 tdy = __ffma2_rn(txy, dx, __fmul2_rn(t11, dy));  // -(T d).y
+    const float2 dtd = __ffma2_rn(dx, tdx, __fmul2_rn(dy, tdy));  // -d.T.d
+    const float2 t = __ffma2_rn(__fmul2_rn(make_float2(-2.5f, -2.5f), dtd), r2,
+                                make_float2(mh.z, mh.w));         // 2.5 d.T.d / u - h
+    const float2 coef = __ffma2_rn(r2, t, make_float2(mh.x, mh.y));
+    const float2 fx = __ffma2_rn(coef, dx, __fmul2_rn(r2, tdx));
+    const float2 fy = __ffma2_rn(coef, dy, __fmul2_rn(r2, tdy));
+    ax = __ffma2_rn(r3, fx, ax);
+    ay = __ffma2_rn(r3, fy, ay);
+}
+
+__device__ __forceinline__ void p2p_pair(const float4 xy, const float2 m, const float2 npx,
+                                         const float2 npy, const float2 e2, float2& ax,
+                                         float2& ay) {
+    const float2 dx = __fadd2_rn(make_float2(xy.x, xy.y), npx);
+    const float2 dy = __fadd2_rn(make_float2(xy.z, xy.w), npy);
+    const float2 u = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, e2));
+    const float2 ri = make_float2(rsqrt_ftz(u.x), rsqrt_ftz(u.y));
+    const float2 f = __fmul2_rn(__fmul2_rn(m, ri), __fmul2_rn(ri, ri));
+    ax = __ffma2_rn(f, dx, ax);
+    ay = __ffma2_rn(f, dy, ay);
+}
+
+// One staged cell (entry e) back in the record layout of p2m / pot_cell.
+__device__ __forceinline__ void unpair_cell(const CellPairs& cp, int e, float4& A, float4& B) {
+    const int q = e >> 1;
+    const float4 xy = cp.xy[q], mh = cp.mh[q], t01 = cp.t01[q];
+    const float2 t11 = cp.t11[q];
+    if (e & 1) {
+        A = make_float4(xy.y, xy.w, mh.y, 0.0f);
+        B = make_float4(-t01.y, -t01.w, -t11.y, -mh.w);
+    } else {
+        A = make_float4(xy.x, xy.z, mh.x, 0.0f);
+        B = make_float4(-t01.x, -t01.z, -t11.x, -mh.z);
+    }
+}
+
 // Launch-time shape of the accuracy walk (chosen by bh_autotune or the defaults).
 struct AccShape {
     int stack;   // stack entries per warp
@@ -300,10 +364,16 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
     const unsigned lt = lanemask_lt();
     const int STACK = shape.stack, BUCKET = shape.bucket;
     unsigned char* wbase = smem_raw + (size_t)warp * acc_warp_bytes(shape);
-    float4* cA = reinterpret_cast<float4*>(wbase);
-    float4* cB = cA + 32;
-    float4* bP = cB + 32;
-    float2* gp = reinterpret_cast<float2*>(bP + 32);
+    // 1536 bytes: 16 cell pairs (896), 16 body pairs (512), 128 spare
+    CellPairs cpair;
+    cpair.xy = reinterpret_cast<float4*>(wbase);
+    cpair.mh = cpair.xy + 16;
+    cpair.t01 = cpair.mh + 16;
+    cpair.t11 = reinterpret_cast<float2*>(cpair.t01 + 16);
+    float4* bxy = reinterpret_cast<float4*>(cpair.t11 + 16);
+    float2* bm = reinterpret_cast<float2*>(bxy + 16);
+    int2* bid = reinterpret_cast<int2*>(bm + 16);
+    float2* gp = reinterpret_cast<float2*>(wbase + 3 * 32 * 16);
     float4* gext = reinterpret_cast<float4*>(gp + 32);  // y at min/max x, x at min/max y
     int* clist = reinterpret_cast<int*>(gext + 1);
     int* stack = clist + 64;
@@ -375,24 +445,52 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
                 ay += by;
             }
         };
+        // packed-pair constants of this lane's body
+        const float2 npx = make_float2(-px, -px), npy = make_float2(-py, -py);
+        const float2 e2v = make_float2(eps2, eps2);
         auto flush_cells = [&](int k) {  // the last k entries of clist
             __syncwarp();
             if (lane < k) {
-                int node = clist[ccnt - k + lane];
-                cA[lane] = recA[node];
-                cB[lane] = recB[node];
+                const int node = clist[ccnt - k + lane];
+                const float4 A = recA[node], B = recB[node];
+                const int q = lane >> 1, h = lane & 1;
+                reinterpret_cast<float*>(cpair.xy + q)[h] = A.x;
+                reinterpret_cast<float*>(cpair.xy + q)[2 + h] = A.y;
+                reinterpret_cast<float*>(cpair.mh + q)[h] = A.z;
+                reinterpret_cast<float*>(cpair.mh + q)[2 + h] = -B.w;
+                reinterpret_cast<float*>(cpair.t01 + q)[h] = -B.x;
+                reinterpret_cast<float*>(cpair.t01 + q)[2 + h] = -B.y;
+                reinterpret_cast<float*>(cpair.t11 + q)[h] = -B.z;
             }
             __syncwarp();
             float bx = 0.0f, by = 0.0f;
             if (DIAG) {
                 float f = 0.0f;
-                for (int e = 0; e < k; ++e) f += pot_cell(cA[e], cB[e], px, py, eps2);
+                for (int e = 0; e < k; ++e) {
+                    float4 A, B;
+                    unpair_cell(cpair, e, A, B);
+                    f += pot_cell(A, B, px, py, eps2);
+                }
                 phi += (double)f;
-            } else if (k == 32) {
-#pragma unroll 4
-                for (int e = 0; e < 32; ++e) p2m(cA[e], cB[e], px, py, eps2, bx, by);
             } else {
-                for (int e = 0; e < k; ++e) p2m(cA[e], cB[e], px, py, eps2, bx, by);
+                float2 sx = make_float2(0.0f, 0.0f), sy = make_float2(0.0f, 0.0f);
+                if (k == 32) {
+#pragma unroll 4
+                    for (int e = 0; e < 16; ++e)
+                        p2m_pair(cpair.xy[e], cpair.mh[e], cpair.t01[e], cpair.t11[e], npx, npy,
+                                 e2v, sx, sy);
+                } else {
+                    for (int e = 0; e < (k >> 1); ++e)
+                        p2m_pair(cpair.xy[e], cpair.mh[e], cpair.t01[e], cpair.t11[e], npx, npy,
+                                 e2v, sx, sy);
+                    if (k & 1) {
+                        float4 A, B;
+                        unpair_cell(cpair, k - 1, A, B);
+                        p2m(A, B, px, py, eps2, bx, by);
+                    }
+                }
+                bx += sx.x + sx.y;
+                by += sy.x + sy.y;
             }
             add_batch(bx, by);
             ccnt -= k;
@@ -402,35 +500,54 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
         auto flush_bodies = [&](int k) {
             __syncwarp();
             if (lane < k) {
-                int b = blist[bcnt - k + lane];
-                bP[lane] = make_float4(in.x[b], in.y[b], in.m[b], __int_as_float(b));
+                const int b = blist[bcnt - k + lane];
+                const int pi = lane >> 1, h = lane & 1;
+                reinterpret_cast<float*>(&bxy[pi])[h] = in.x[b];
+                reinterpret_cast<float*>(&bxy[pi])[2 + h] = in.y[b];
+                reinterpret_cast<float*>(&bm[pi])[h] = in.m[b];
+                reinterpret_cast<int*>(&bid[pi])[h] = b;
             }
             __syncwarp();
             float bx = 0.0f, by = 0.0f;
+            // entry e of the staged bodies, unpaired
+            auto body = [&](int e, float& x, float& y, float& m) {
+                const float4 q = bxy[e >> 1];
+                const float2 w = bm[e >> 1];
+                x = (e & 1) ? q.y : q.x;
+                y = (e & 1) ? q.w : q.z;
+                m = (e & 1) ? w.y : w.x;
+            };
             if (DIAG) {
                 float f = 0.0f;
                 for (int e = 0; e < k; ++e) {
-                    const float4 P = bP[e];
-                    if (__float_as_int(P.w) == j) continue;  // own body
-                    const float dx = P.x - px, dy = P.y - py;
-                    f -= P.z * rsqrtf(fmaf(dx, dx, fmaf(dy, dy, eps2)));
+                    const int2 ids = bid[e >> 1];
+                    if (((e & 1) ? ids.y : ids.x) == j) continue;  // own body
+                    float x, y, m;
+                    body(e, x, y, m);
+                    const float dx = x - px, dy = y - py;
+                    f -= m * rsqrtf(fmaf(dx, dx, fmaf(dy, dy, eps2)));
                 }
                 phi += (double)f;
-            } else if (eps2 > 0.0f && k == 32) {
-#pragma unroll 4
-                for (int e = 0; e < 32; ++e) {
-                    float4 P = bP[e];
-                    p2p<false>(P.x, P.y, P.z, px, py, eps2, bx, by);
-                }
             } else if (eps2 > 0.0f) {
-                for (int e = 0; e < k; ++e) {
-                    float4 P = bP[e];
-                    p2p<false>(P.x, P.y, P.z, px, py, eps2, bx, by);
+                float2 sx = make_float2(0.0f, 0.0f), sy = make_float2(0.0f, 0.0f);
+                if (k == 32) {
+#pragma unroll 4
+                    for (int e = 0; e < 16; ++e) p2p_pair(bxy[e], bm[e], npx, npy, e2v, sx, sy);
+                } else {
+                    for (int e = 0; e < (k >> 1); ++e) p2p_pair(bxy[e], bm[e], npx, npy, e2v, sx, sy);
+                    if (k & 1) {
+                        float x, y, m;
+                        body(k - 1, x, y, m);
+                        p2p<false>(x, y, m, px, py, eps2, bx, by);
+                    }
                 }
+                bx += sx.x + sx.y;
+                by += sy.x + sy.y;
             } else {
                 for (int e = 0; e < k; ++e) {
-                    float4 P = bP[e];
-                    p2p<true>(P.x, P.y, P.z, px, py, eps2, bx, by);
+                    float x, y, m;
+                    body(e, x, y, m);
+                    p2p<true>(x, y, m, px, py, eps2, bx, by);
                 }
             }
             add_batch(bx, by);
