@@ -212,6 +212,15 @@ __device__ __forceinline__ float rsqrt_ftz(float x) {
     return r;
 }
 
+// PTX sqrt.approx.ftz.f32 (relative error ~2^-22).  The walk's two rules use
+// it with a margin of 2^-18 on the side that opens more nodes, never fewer.
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+constexpr float kRuleMargin = 1.0f - 1.0f / 262144.0f;
+
 template <bool GUARD>
 __device__ __forceinline__ void p2p(float bx, float by, float bm, float px, float py, float eps2,
                                     float& ax, float& ay) {
@@ -556,11 +565,12 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
         };
         while (top > 0) {
             int k = min(32, top);
-            int room = (STACK - top) / 3;  // pop k, push <= 4k: keep top+3k <= STACK
-            if (room < k) k = max(room, 0);
-            if (k == 0) {
-                overflow = true;
-                break;
+            if (top + 3 * k > STACK) {  // pop k, push <= 4k: keep top+3k <= STACK
+                k = max((STACK - top) / 3, 0);
+                if (k == 0) {
+                    overflow = true;
+                    break;
+                }
             }
             __syncwarp();
             const int node = lane < k ? stack[top - 1 - lane] : -1;
@@ -584,8 +594,8 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
                 const float ddy = fmaxf(fmaxf(gy0 - A.y, A.y - gy1), 0.0f);
                 d2 = fmaf(ddx, ddx, ddy * ddy);
                 if (d2 <= A.w) {
-                    const float reach = sqrtf(d2) + gdiag;
-                    need = reach * reach > A.w;
+                    const float reach = sqrt_approx(d2) + gdiag;
+                    need = reach * reach > A.w * kRuleMargin;
                 }
             }
             if (__any_sync(kFull, need)) {
@@ -633,7 +643,8 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
             }
             if (node >= 0) {
                 bool acc = d2 > A.w;
-                if (acc && !ESTIMATE && !DIAG) acc = __int_as_float(D.z) <= aa * d2 * d2 * sqrtf(d2);
+                if (acc && !ESTIMATE && !DIAG)
+                    acc = __int_as_float(D.z) <= aa * kRuleMargin * d2 * d2 * sqrt_approx(d2);
                 cat = acc ? 0 : (D.y <= BUCKET ? 1 : 2);
             }
             unsigned mc = __ballot_sync(kFull, cat == 0);
