@@ -563,7 +563,8 @@ int64_t orc_walk_acc(int n, const float* sx, const float* sy, const float* sm,
                      const uint64_t* skeys, const int32_t* left, const int32_t* right,
                      const int32_t* split, const int32_t* first, const int32_t* last,
                      const int32_t* qchild, const float* box, float theta, float eps2, float G,
-                     int bucket, float alpha, const float* aold, float* sax, float* say) {
+                     int bucket, float alpha, const float* aold, int quadrupole, float* sax,
+                     float* say) {
     if (n < 2) {
         for (int i = 0; i < n; ++i) sax[i] = say[i] = 0.0f;
         return 0;
@@ -650,6 +651,7 @@ int64_t orc_walk_acc(int n, const float* sx, const float* sy, const float* sm,
                     const Mom* M = &mom[node];
                     float T0 = 3.0f * M->sxx, T1 = 3.0f * M->sxy, T2 = 3.0f * M->syy;
                     float h = 1.5f * (M->sxx + M->syy);
+                    if (!quadrupole) T0 = T1 = T2 = h = 0.0f;  /* bootstrap pass: monopoles */
                     for (int k = 0; k < cnt; ++k) {
                         float dx = cx - px[k], dy = cy - py[k];
                         float u = dx * dx + dy * dy + eps2;

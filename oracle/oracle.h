@@ -97,13 +97,15 @@ void orc_energy_f64(int n, const float* x, const float* y, const float* vx, cons
 
 /* CPU restatement of the engine's PLAIN-mode group walk: quadrupoles, leaf
  * buckets, geometric + relative opening rule (see oracle.c; aold = |a| of the
- * previous step in sorted order, NULL for the geometric-only bootstrap pass).
- * Output in sorted order; returns the interaction count. */
+ * previous step in sorted order, NULL for the geometric-only bootstrap pass;
+ * quadrupole = 0 evaluates accepted cells as monopoles, as the engine's
+ * bootstrap pass does).  Output in sorted order; returns the interaction count. */
 int64_t orc_walk_acc(int n, const float* sx, const float* sy, const float* sm,
                      const uint64_t* skeys, const int32_t* left, const int32_t* right,
                      const int32_t* split, const int32_t* first, const int32_t* last,
                      const int32_t* qchild, const float* box, float theta, float eps2, float G,
-                     int bucket, float alpha, const float* aold, float* sax, float* say);
+                     int bucket, float alpha, const float* aold, int quadrupole, float* sax,
+                     float* say);
 
 int orc_num_threads(void);
 

@@ -641,9 +641,10 @@ __device__ __forceinline__ float ref_dp(Box bx, float theta, int level) {
 
 // Walk record of branching node i, from its sums and the tree (the body of
 // k_records).
-// Opening angle of the bootstrap pass (|a| estimate after bh_set_state).  At
-// 1.0 its |a| is within ~5% RMS and costs ~40% of the theta = 0.5 walk; the
-// relative rule it feeds opens the same nodes as with exact |a| to within 0.1%.
+// Opening angle of the bootstrap pass (|a| estimate after bh_set_state, cells
+// as monopoles).  At 1.0 its |a| is within a few per cent and it costs about a
+// third of the theta = 0.5 walk; the relative rule it feeds opens the same
+// nodes as with exact |a| to within 1%.
 constexpr float kBootstrapTheta = 1.0f;
 
 __device__ __forceinline__ void emit_record(int i, int sp, int accuracy, float theta, float G,

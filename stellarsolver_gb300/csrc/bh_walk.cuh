@@ -343,8 +343,8 @@ constexpr int kSerialExactLanes = 8;
 
 // PLAIN / MIXED walk.  ESTIMATE = the bootstrap pass after bh_set_state: the
 // geometric rule only, at opening angle max(theta, kBootstrapTheta) (radius
-// in recD.w), writes |G a| into in.amag and nothing else (skipped unless
-// *fresh is set).  The main pass also applies the relative rule
+// in recD.w), cells as monopoles; writes |G a| into in.amag and nothing else
+// (skipped unless *fresh is set).  The main pass also applies the relative rule
 //   G M l^3 <= alpha * a_g * d^5,  a_g = max(min |a_old|, 0.1 mean |a_old|) over the group,
 // d = min over the group's bodies of |COM - p|; the geometric rule is d > l/theta + delta.
 // DIAG = diagnostics pass: the main rule, but each body's potential (FP64
@@ -483,7 +483,18 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
                 phi += (double)f;
             } else {
                 float2 sx = make_float2(0.0f, 0.0f), sy = make_float2(0.0f, 0.0f);
-                if (k == 32) {
+                if (ESTIMATE) {
+                    // the bootstrap needs |a| to a few per cent: monopoles suffice
+                    for (int e = 0; e < (k >> 1); ++e) {
+                        const float4 mh = cpair.mh[e];
+                        p2p_pair(cpair.xy[e], make_float2(mh.x, mh.y), npx, npy, e2v, sx, sy);
+                    }
+                    if (k & 1) {
+                        float4 A, B;
+                        unpair_cell(cpair, k - 1, A, B);
+                        p2p<false>(A.x, A.y, A.z, px, py, eps2, bx, by);
+                    }
+                } else if (k == 32) {
 #pragma unroll 4
                     for (int e = 0; e < 16; ++e)
                         p2m_pair(cpair.xy[e], cpair.mh[e], cpair.t01[e], cpair.t11[e], npx, npy,
