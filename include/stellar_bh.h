@@ -152,6 +152,24 @@ int bh_sync(bh_system* s, void* stream);
 
 int bh_get_stats(bh_system* s, bh_stats* out, void* stream);
 
+/* Tree invariants of the last step, checked on the device.  The reference
+ * copies every tree array to the host and checks it there (debug.cpp:23-174,
+ * BarnesHutParticleSystem.cpp:331-344); here the same invariants, stated for
+ * the engine's binary radix tree, run as three kernels.  *failed receives the
+ * BH_CHECK_* bits of the invariants that do not hold (0: all hold).
+ * Synchronous.  Checks the tree of the last bh_step (or bh_energy, which
+ * builds one for the current positions); BH_ERR_STATE before the first step
+ * after bh_set_state. */
+#define BH_CHECK_COUNT 1u         /* a node's range is not the union of its children's (count test) */
+#define BH_CHECK_CHILD_SUM 2u     /* some position is not a leaf child exactly once (child test 1) */
+#define BH_CHECK_CHILD_RANGE 4u   /* a child index outside its system (child tests 2-3) */
+#define BH_CHECK_PARENT 8u        /* parent links do not point back */
+#define BH_CHECK_KEYS_SORTED 16u  /* keys not ascending within a system */
+#define BH_CHECK_PERMUTATION 32u  /* positions' caller indices not a permutation (sorted tests) */
+#define BH_CHECK_BOX 64u          /* left > right or bottom > top (bounding box test) */
+#define BH_CHECK_MASS 128u        /* a node's mass is not the sum of its children's */
+int bh_check(bh_system* s, void* stream, unsigned* failed);
+
 /* Copy a named internal array of the last step to host memory (test and
  * debugging aid).  Names and element types:
  *   "box" f32[4], "keys" u64[n] (sorted), "perm" i32[n] (caller index of each

@@ -699,3 +699,78 @@ int64_t orc_walk_acc(int n, const float* sx, const float* sy, const float* sm,
     free(qerr);
     return total;
 }
+
+/* ------------------------------------------------------------------ tree invariants
+ * The engine's bh_check restated (one system).  debug.cpp:23-174 checks the
+ * reference's pointer quadtree on the host: child counts add up (:20-37),
+ * every body is a child once (:43-55), child indices in range (:57-83),
+ * sorted[] a permutation (:110-146), box ordered (:152-166).  The same
+ * statements for a binary radix tree, with every index range-checked. */
+unsigned orc_check_tree(int n, const uint64_t* skeys, const int32_t* left, const int32_t* right,
+                        const int32_t* parent, const int32_t* leaf_parent, const int32_t* first,
+                        const int32_t* last, const float* sm, const float* node_m,
+                        const int32_t* id, const float* box) {
+    enum { COUNT = 1, CHILD_SUM = 2, CHILD_RANGE = 4, PARENT = 8, KEYS = 16, PERM = 32, BOX = 64,
+           MASS = 128 };
+    unsigned f = 0;
+    unsigned long long psum = 0, leaves = 0;
+    if (n == 1) {
+        psum = 0;
+        leaves = 1;
+    }
+    for (int i = 0; i < n - 1; ++i) {
+        const int a = first[i], b = last[i];
+        if (a < 0 || b > n - 1 || a >= b || (a != i && b != i)) f |= COUNT;
+        const int ch[2] = {left[i], right[i]};
+        int cf[2] = {0, 0}, cl[2] = {0, 0};
+        float cm[2] = {0.0f, 0.0f};
+        int ok = 1;
+        for (int q = 0; q < 2; ++q) {
+            const int c = ch[q];
+            if (c == INT32_MIN) {
+                ok = 0;
+            } else if (c < 0) {
+                const int body = ~c;
+                if (body < 0 || body > n - 1) {
+                    ok = 0;
+                } else {
+                    psum += (unsigned long long)body;
+                    leaves += 1;
+                    if (leaf_parent[body] != i) f |= PARENT;
+                    cf[q] = cl[q] = body;
+                    cm[q] = sm[body];
+                }
+            } else if (c >= n - 1) {
+                ok = 0;
+            } else {
+                if (parent[c] != i) f |= PARENT;
+                cf[q] = first[c];
+                cl[q] = last[c];
+                cm[q] = node_m[c];
+            }
+        }
+        if (!ok) {
+            f |= CHILD_RANGE;
+        } else {
+            if (cf[0] != a || cl[1] != b || cl[0] + 1 != cf[1]) f |= COUNT;
+            const float msum = cm[0] + cm[1];
+            if (msum != node_m[i]) f |= MASS;
+        }
+    }
+    const unsigned long long nn = (unsigned long long)n;
+    if (psum != nn * (nn - 1) / 2 || leaves != nn) f |= CHILD_SUM;
+    int* seen = (int*)calloc((size_t)n, sizeof(int));
+    for (int j = 0; j < n; ++j) {
+        if (j + 1 < n && skeys[j] > skeys[j + 1]) f |= KEYS;
+        const int c = id[j];
+        if (c < 0 || c >= n)
+            f |= PERM;
+        else
+            seen[c] += 1;
+    }
+    for (int j = 0; j < n; ++j)
+        if (seen[j] != 1) f |= PERM;
+    free(seen);
+    if (!(box[0] <= box[1]) || !(box[2] <= box[3])) f |= BOX;
+    return f;
+}

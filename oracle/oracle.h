@@ -107,6 +107,16 @@ int64_t orc_walk_acc(int n, const float* sx, const float* sy, const float* sm,
                      int bucket, float alpha, const float* aold, int quadrupole, float* sax,
                      float* say);
 
+/* Tree invariants (the engine's bh_check, restated for one system; the
+ * reference's debug.cpp:23-174 on a binary radix tree): returns the mask of
+ * failing checks, bits as BH_CHECK_* in include/stellar_bh.h.  Node arrays have
+ * n - 1 entries; sm = masses in sorted order; id = caller index per position;
+ * box = left, right, bottom, top. */
+unsigned orc_check_tree(int n, const uint64_t* skeys, const int32_t* left, const int32_t* right,
+                        const int32_t* parent, const int32_t* leaf_parent, const int32_t* first,
+                        const int32_t* last, const float* sm, const float* node_m,
+                        const int32_t* id, const float* box);
+
 int orc_num_threads(void);
 
 #ifdef __cplusplus

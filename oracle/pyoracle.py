@@ -53,6 +53,8 @@ def lib() -> ctypes.CDLL:
         L.orc_energy_f64.restype = None
         L.orc_walk_acc.argtypes = [i32] + [vp] * 11 + [f32, f32, f32, i32, f32, vp, i32, vp, vp]
         L.orc_walk_acc.restype = i64
+        L.orc_check_tree.argtypes = [i32] + [vp] * 11
+        L.orc_check_tree.restype = ctypes.c_uint
         L.orc_num_threads.restype = i32
         _lib = L
     return _lib
@@ -157,6 +159,20 @@ def walk_acc(sx, sy, sm, skeys, tree: Tree, box, theta, eps2, G=1.0, bucket=8, a
                                _p(_f32(aold)) if aold is not None else None,
                                1 if quadrupole else 0, _p(sax), _p(say))
     return sax, say, int(inter)
+
+
+def check_tree(skeys, tree: Tree, sm, node_m, ids, box, left=None, right=None, parent=None,
+               leaf_parent=None, first=None, last=None) -> int:
+    """Tree invariants of one system (the engine's bh_check restated): the mask
+    of failing checks.  Any tree array may be overridden (tests plant errors)."""
+    n = len(skeys)
+    arr = lambda a, d: np.ascontiguousarray(d if a is None else a, dtype=np.int32)
+    return int(lib().orc_check_tree(
+        n, _p(np.ascontiguousarray(skeys, dtype=np.uint64)), _p(arr(left, tree.left)),
+        _p(arr(right, tree.right)), _p(arr(parent, tree.parent)),
+        _p(arr(leaf_parent, tree.leaf_parent)), _p(arr(first, tree.first)),
+        _p(arr(last, tree.last)), _p(_f32(sm)), _p(_f32(node_m)),
+        _p(np.ascontiguousarray(ids, dtype=np.int32)), _p(_f32(box))))
 
 
 def step_ref(x, y, vx, vy, m, theta=0.5, eps2=0.025, dt=1e-3, damp=1.0):

@@ -16,6 +16,8 @@ import numpy as np
 from . import build as _build
 
 MODES = {"reference": 0, "plain": 1, "mixed": 2}
+CHECK_BITS = {"count": 1, "child_sum": 2, "child_range": 4, "parent": 8, "keys_sorted": 16,
+              "permutation": 32, "box": 64, "mass": 128}
 PHASES = ("bbox", "keys", "sort", "reorder", "build", "moments", "bootstrap", "walk")
 PHASES_N = len(PHASES)
 
@@ -87,6 +89,7 @@ def lib() -> ctypes.CDLL:
     L.bh_sync.argtypes = [vp, vp]
     L.bh_get_stats.argtypes = [vp, P(Stats), vp]
     L.bh_get_debug.argtypes = [vp, ctypes.c_char_p, vp, sz, vp]
+    L.bh_check.argtypes = [vp, vp, P(ctypes.c_uint)]
     L.bh_step_profiled.argtypes = [vp, vp, vp]
     L.bh_direct_sum_f64.argtypes = [vp, i32, vp, vp, vp]
     L.bh_measure_fp32_peak.argtypes = [i32, P(ctypes.c_double)]
@@ -298,6 +301,13 @@ class BarnesHutSystem:
                     max_stack=int(s.max_stack), walk_rounds=int(s.walk_rounds),
                     nodes_tested=int(s.nodes_tested),
                     cell_interactions=int(s.cell_interactions))
+
+    def check(self, stream=None) -> int:
+        """Tree invariants of the last step checked on the device (bh_check):
+        the mask of BH_CHECK_* bits that fail, 0 when all hold."""
+        f = ctypes.c_uint(0)
+        _check(lib().bh_check(self._h, stream, ctypes.byref(f)), "bh_check")
+        return int(f.value)
 
     def debug(self, name: str):
         n = self.n

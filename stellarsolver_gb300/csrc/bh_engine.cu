@@ -13,6 +13,7 @@
 #include <string>
 #include <vector>
 
+#include "bh_check.cuh"
 #include "bh_engine.h"
 #include "bh_walk.cuh"
 #include "stellar_bh.h"
@@ -849,6 +850,34 @@ int bh_get_stats(bh_system* s, bh_stats* out, void* stream) {
     out->cells = (int32_t)cells;
     out->nodes = nodes;
     out->max_depth = maxd;
+    return BH_OK;
+}
+
+int bh_check(bh_system* s, void* stream, unsigned* failed) {
+    if (!s || !failed) return BH_ERR_ARG;
+    if (!s->have_state || s->caller_order || !s->kfinal) return BH_ERR_STATE;  // needs a step
+    CK(cudaSetDevice(s->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    const int n = s->n;
+    // scratch: the key buffer the last sort did not end in, and the arrival counters
+    auto* acc = reinterpret_cast<unsigned long long*>(s->kfinal == s->keys ? s->keys_alt : s->keys);
+    auto* flags = reinterpret_cast<unsigned*>(acc + 2);
+    CK(cudaMemsetAsync(acc, 0, 3 * sizeof(unsigned long long), st));
+    CK(cudaMemsetAsync(s->counter, 0, sizeof(int) * n, st));
+    Segs segs{s->nseg, s->seg_off, s->nseg > 1 ? s->seg_of_pos : nullptr};
+    const int nb = (n + 255) / 256;
+    k_check_nodes<<<nb, 256, 0, st>>>(n, segs, s->tree, s->st[1].m, s->sums, acc, flags);
+    k_check_bodies<<<nb, 256, 0, st>>>(n, segs, s->kfinal, s->st[0].id, s->counter, s->box_ord,
+                                       flags);
+    k_check_seen<<<nb, 256, 0, st>>>(n, s->counter, flags);
+    CK(cudaGetLastError());
+    unsigned long long h[3] = {0, 0, 0};
+    CK(cudaMemcpyAsync(h, acc, sizeof h, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    unsigned f = (unsigned)(h[2] & 0xffffffffull);
+    const unsigned long long nn = (unsigned long long)n;
+    if (h[0] != nn * (nn - 1) / 2 || h[1] != nn) f |= CK_CHILD_SUM;
+    *failed = f;
     return BH_OK;
 }
 

@@ -11,7 +11,6 @@
 #include <cstdio>
 #include <cstdlib>
 #include <iostream>
-#include <numeric>
 
 
 namespace {
@@ -132,49 +131,20 @@ void BarnesHutParticleSystem::update() {
 
 const float* BarnesHutParticleSystem::getOutputBuffer() { return h_output.data(); }
 
-// debug.cpp:23-174, restated on the engine's tree (counts per node, every body
-// once, sorted order a permutation, box ordered).
+// debug.cpp:23-174, restated on the engine's tree and run on the device
+// (bh_check); one line per invariant, in the reference's format.
 void BarnesHutParticleSystem::runDebugTests() {
-    const int n = numParticles;
-    if (n < 2) return;
-    std::vector<int> left(n), right(n), first(n), last(n), split(n), perm(n);
-    float box[4];
-    check(bh_get_debug(sys, "node_left", left.data(), sizeof(int) * n, nullptr), "debug");
-    check(bh_get_debug(sys, "node_right", right.data(), sizeof(int) * n, nullptr), "debug");
-    check(bh_get_debug(sys, "node_first", first.data(), sizeof(int) * n, nullptr), "debug");
-    check(bh_get_debug(sys, "node_last", last.data(), sizeof(int) * n, nullptr), "debug");
-    check(bh_get_debug(sys, "node_split", split.data(), sizeof(int) * n, nullptr), "debug");
-    check(bh_get_debug(sys, "perm", perm.data(), sizeof(int) * n, nullptr), "debug");
-    check(bh_get_debug(sys, "box", box, sizeof(box), nullptr), "debug");
-    auto cnt = [&](int c) { return c < 0 ? 1 : last[c] - first[c] + 1; };
-    bool count_ok = true, child_ok = true;
-    std::vector<int> seen(n, 0);
-    for (int i = 0; i < n; ++i) {
-        if (split[i] < 0) continue;
-        if (cnt(left[i]) + cnt(right[i]) != last[i] - first[i] + 1) count_ok = false;
-        for (int c : {left[i], right[i]}) {
-            if (c < 0) {
-                if (~c < 0 || ~c >= n) child_ok = false;
-                else seen[~c]++;
-            } else if (c >= n) {
-                child_ok = false;
-            }
-        }
-    }
-    for (int v : seen) child_ok = child_ok && v == 1;
-    std::vector<int> chk(n, 0);
-    bool sorted_ok = true;
-    for (int v : perm) {
-        if (v < 0 || v >= n || chk[v]++) sorted_ok = false;
-    }
-    long long sum = std::accumulate(perm.begin(), perm.end(), 0LL);
-    bool box_ok = box[0] <= box[1] && box[2] <= box[3];
-    auto line = [](const char* what, bool ok) {
-        std::cout << what << " RESULT = " << (ok ? "PASS: " : "FAIL: ") << std::endl;
+    unsigned failed = 0;
+    check(bh_check(sys, nullptr, &failed), "bh_check");
+    auto line = [&](const char* what, unsigned bits) {
+        std::cout << what << " RESULT = " << ((failed & bits) ? "FAIL: " : "PASS: ") << std::endl;
     };
-    line("COUNT ARRAY TEST 1", count_ok);
-    line("CHILD ARRAY TEST 1", child_ok);
-    line("SORTED ARRAY TEST 1", sum == (long long)n * (n - 1) / 2);
-    line("SORTED ARRAY TEST 2", sorted_ok);
-    line("BOUNDING BOX TEST 1", box_ok);
+    line("COUNT ARRAY TEST 1", BH_CHECK_COUNT);
+    line("CHILD ARRAY TEST 1", BH_CHECK_CHILD_SUM);
+    line("CHILD ARRAY TEST 2", BH_CHECK_CHILD_RANGE);
+    line("CHILD ARRAY TEST 3", BH_CHECK_PARENT);
+    line("SORTED ARRAY TEST 1", BH_CHECK_PERMUTATION);
+    line("SORTED ARRAY TEST 2", BH_CHECK_KEYS_SORTED);
+    line("BOUNDING BOX TEST 1", BH_CHECK_BOX);
+    line("MASS SUM TEST 1", BH_CHECK_MASS);
 }

@@ -35,7 +35,7 @@ def test_debug_invariants_pass(mode):
                        capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stderr
     results = re.findall(r"RESULT = (PASS|FAIL)", r.stdout)
-    assert len(results) == 10 and set(results) == {"PASS"}, r.stdout
+    assert len(results) == 16 and set(results) == {"PASS"}, r.stdout
 
 
 def test_opengl_is_headless_and_fills_the_output_buffer():
