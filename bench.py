@@ -13,7 +13,10 @@ force walk fused with the integration.
           copies the state in from pinned host memory, steps, and reads the
           positions back.
   roofline  the force walk against the measured FP32 FMA peak (14 flops per
-          body-node interaction); per-phase HBM fractions beside it.
+          body-body and 33 per body-cell interaction); per-phase HBM
+          fractions beside it.
+  ensemble  256 systems, N log-uniform in [2^10, 2^17]: the batched MIXED
+          engine against one PLAIN handle per system.
 
 --impl reference times the reference's algorithm on the host cores (the CPU
 restatement in oracle/, the reference having no CPU path) on the same
@@ -40,35 +43,7 @@ N_BODIES = 1 << 20
 EPS = 0.01
 DT = 1e-4
 THETA = 0.5
-# FP32 flops per interaction (an FMA counts 2, rsqrt 1), from the kernels' arithmetic:
-#   body-body  (p2p): dx,dy 2; u 4; rsqrt 1; r^-3 2; m*r^-3 1; two FMAs 4           = 14
-#   body-cell  (p2m): dx,dy 2; u 4; rsqrt 1; r^-2,r^-3 2; T.d 6; d.T.d 3; t 3;
-#                     coef 2; fx,fy 6; two FMAs 4                                    = 33
-FLOPS_P2P = 14
-FLOPS_P2M = 33
 LAUNCHES_PER_STEP = 32       # bbox, keys, sort 8 x (hist, scan, scatter), reorder, build, moments, records, walk x2
-
-
-def peaks():
-    try:
-        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            p = json.load(f)
-        return float(p["hbm_gbs"]), "measured"
-    except Exception:
-        return 6800.0, "fallback"
-
-
-def phase_bytes(n, mixed, passes=8):
-    """Algorithmic bytes per launch of each HBM-bound phase (each array once)."""
-    lo = 16 * n if mixed else 0
-    return {
-        "bbox": 8 * n,
-        "keys": 20 * n,
-        "sort": 24 * n * passes,  # one read + one write of (key, index) per pass
-        "reorder": 52 * n + lo,
-        "build": 36 * n,
-        "moments": 68 * n + 108 * n,  # sums, then walk records (two kernels)
-    }
 
 
 def dist_init():
@@ -136,7 +111,7 @@ class ClockSampler:
 def run_engine(args):
     import torch
 
-    from stellarsolver_gb300 import bh, models
+    from stellarsolver_gb300 import bh, models, roofline
 
     world, rank, local = dist_init()
     torch.cuda.set_device(local)
@@ -146,7 +121,7 @@ def run_engine(args):
         dist.init_process_group("nccl")
     stream = torch.cuda.current_stream()
     sp = ctypes_stream(stream)
-    hbm_peak, hbm_kind = peaks()
+    hbm_peak, hbm_kind = roofline.hbm_peak()
 
     x, y, vx, vy, m = models.plummer(N_BODIES, models.SEED_BASE + 1)
     n = len(x)
@@ -242,11 +217,10 @@ def run_engine(args):
     sysm.sync(sp)
     walk_ms = float(phase_ms[bh.PHASES.index("walk")])
     fp32_peak = bh.measure_fp32_peak(local)
-    cell_inter = stats["cell_interactions"]
-    walk_flops = FLOPS_P2P * (stats["interactions"] - cell_inter) + FLOPS_P2M * cell_inter
+    walk_flops = roofline.walk_flops(stats)
     achieved = walk_flops / (walk_ms * 1e-3) / 1e12
     traffic = recorded_traffic("walk")
-    pb = phase_bytes(n, args.mode == "mixed")
+    pb = roofline.phase_bytes(n, args.mode == "mixed")
     phases = {}
     for i, name in enumerate(bh.PHASES):
         ms = float(phase_ms[i])

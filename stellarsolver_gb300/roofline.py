@@ -1,0 +1,44 @@
+"""Roofline bookkeeping shared by bench.py and workloads.py: the algorithmic
+bytes of the HBM-bound phases, the walk's flop count and the HBM peak."""
+from __future__ import annotations
+
+import json
+import os
+
+# FP32 flops per interaction (an FMA counts 2, rsqrt 1), from the kernels' arithmetic:
+#   body-body  (p2p): dx,dy 2; u 4; rsqrt 1; r^-3 2; m*r^-3 1; two FMAs 4           = 14
+#   body-cell  (p2m): dx,dy 2; u 4; rsqrt 1; r^-2,r^-3 2; T.d 6; d.T.d 3; t 3;
+#                     coef 2; fx,fy 6; two FMAs 4                                    = 33
+FLOPS_P2P = 14
+FLOPS_P2M = 33
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def walk_flops(stats: dict) -> int:
+    """Algorithmic FP32 flops of one walk from its exact interaction counts."""
+    cells = stats["cell_interactions"]
+    return FLOPS_P2P * (stats["interactions"] - cells) + FLOPS_P2M * cells
+
+
+def phase_bytes(n: int, mixed: bool, passes: int = 8) -> dict:
+    """Algorithmic bytes per launch of each HBM-bound phase (each array once)."""
+    lo = 16 * n if mixed else 0
+    return {
+        "bbox": 8 * n,
+        "keys": 20 * n,
+        "sort": 24 * n * passes,  # one read + one write of (key, index) per pass
+        "reorder": 52 * n + lo,
+        "build": 36 * n + 16 * n,  # keys and node arrays, climb records
+        "moments": 12 * n + 64 * n + 108 * n,  # bodies, node sums, then walk records
+    }
+
+
+def hbm_peak() -> tuple[float, str]:
+    """Measured STREAM-style copy bandwidth (GB/s) of the GB300s, else
+    the fallback figure."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
