@@ -152,6 +152,18 @@ int bh_sync(bh_system* s, void* stream);
 
 int bh_get_stats(bh_system* s, bh_stats* out, void* stream);
 
+/* Headless rendering of the current positions, in place of the reference's
+ * OpenGL viewer (StellarSolverVisualizer.cpp:4-20, 208-253: one-pixel points,
+ * glm::ortho(-25, 25, -25, 25) on a 1000x1000 window, colour (1,1,1,0.1)
+ * blended with (GL_SRC_ALPHA, GL_ONE) over a (0,0,0,0.5) clear).  A body at
+ * (x, y) lights pixel column floor((x - x0) * width / (x1 - x0)) and row
+ * floor((y - y0) * height / (y1 - y0)) counted from the bottom; rgba receives
+ * width*height RGBA8 pixels, top row first.  A pixel hit by c bodies has
+ * colour min(1, 0.1 c) and alpha min(1, 0.5 + 0.01 c), rounded to 1/255.
+ * rgba may be host or device memory; the copy is ordered on `stream`. */
+int bh_render(bh_system* s, int width, int height, float x0, float x1, float y0, float y1,
+              unsigned char* rgba, void* stream);
+
 /* Tree invariants of the last step, checked on the device.  The reference
  * copies every tree array to the host and checks it there (debug.cpp:23-174,
  * BarnesHutParticleSystem.cpp:331-344); here the same invariants, stated for

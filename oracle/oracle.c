@@ -774,3 +774,30 @@ unsigned orc_check_tree(int n, const uint64_t* skeys, const int32_t* left, const
     if (!(box[0] <= box[1]) || !(box[2] <= box[3])) f |= BOX;
     return f;
 }
+
+/* ------------------------------------------------------------------ rendering
+ * The reference draws the output buffer as one-pixel points through
+ * glm::ortho(-25, 25, -25, 25) with colour (1,1,1,0.1) and blend
+ * (GL_SRC_ALPHA, GL_ONE) over a (0,0,0,0.5) clear
+ * (StellarSolverVisualizer.cpp:4-20, 208-253).  Restated with an exact
+ * per-pixel point count, as the engine's bh_render does. */
+void orc_render(int n, const float* x, const float* y, int width, int height, float x0, float x1,
+                float y0, float y1, unsigned char* rgba) {
+    const float sx = (float)width / (x1 - x0), sy = (float)height / (y1 - y0);
+    uint32_t* counts = (uint32_t*)calloc((size_t)width * height, sizeof(uint32_t));
+    for (int i = 0; i < n; ++i) {
+        const float fx = (x[i] - x0) * sx, fy = (y[i] - y0) * sy;
+        if (!(fx >= 0.0f) || !(fy >= 0.0f) || !(fx < (float)width) || !(fy < (float)height)) continue;
+        const int ix = (int)fx, iy = (int)fy;
+        if (ix >= width || iy >= height) continue;
+        counts[(size_t)(height - 1 - iy) * width + ix] += 1;
+    }
+    for (size_t p = 0; p < (size_t)width * height; ++p) {
+        const unsigned long long c = counts[p];
+        const unsigned v = c >= 10 ? 255u : (unsigned)((255ull * c + 5ull) / 10ull);
+        const unsigned a = c >= 50 ? 255u : (unsigned)((255ull * (50ull + c) + 50ull) / 100ull);
+        rgba[4 * p] = rgba[4 * p + 1] = rgba[4 * p + 2] = (unsigned char)v;
+        rgba[4 * p + 3] = (unsigned char)a;
+    }
+    free(counts);
+}

@@ -117,6 +117,13 @@ unsigned orc_check_tree(int n, const uint64_t* skeys, const int32_t* left, const
                         const int32_t* last, const float* sm, const float* node_m,
                         const int32_t* id, const float* box);
 
+/* Headless point rendering (the engine's bh_render restated): counts of
+ * points per pixel, column floor((x - x0) * sx), row from the bottom, with
+ * sx = width / (x1 - x0); then RGBA8 with colour min(1, 0.1 c) and alpha
+ * min(1, 0.5 + 0.01 c) rounded to 1/255.  rgba: width*height*4, top row first. */
+void orc_render(int n, const float* x, const float* y, int width, int height, float x0, float x1,
+                float y0, float y1, unsigned char* rgba);
+
 int orc_num_threads(void);
 
 #ifdef __cplusplus

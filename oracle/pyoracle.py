@@ -55,6 +55,8 @@ def lib() -> ctypes.CDLL:
         L.orc_walk_acc.restype = i64
         L.orc_check_tree.argtypes = [i32] + [vp] * 11
         L.orc_check_tree.restype = ctypes.c_uint
+        L.orc_render.argtypes = [i32, vp, vp, i32, i32, f32, f32, f32, f32, vp]
+        L.orc_render.restype = None
         L.orc_num_threads.restype = i32
         _lib = L
     return _lib
@@ -173,6 +175,14 @@ def check_tree(skeys, tree: Tree, sm, node_m, ids, box, left=None, right=None, p
         _p(arr(leaf_parent, tree.leaf_parent)), _p(arr(first, tree.first)),
         _p(arr(last, tree.last)), _p(_f32(sm)), _p(_f32(node_m)),
         _p(np.ascontiguousarray(ids, dtype=np.int32)), _p(_f32(box))))
+
+
+def render(x, y, width=1000, height=1000, extent=(-25.0, 25.0, -25.0, 25.0)):
+    """Headless point rendering (the engine's bh_render restated): uint8 (height, width, 4)."""
+    x, y = _f32(x), _f32(y)
+    out = np.zeros((height, width, 4), np.uint8)
+    lib().orc_render(len(x), _p(x), _p(y), width, height, *[float(e) for e in extent], _p(out))
+    return out
 
 
 def step_ref(x, y, vx, vy, m, theta=0.5, eps2=0.025, dt=1e-3, damp=1.0):

@@ -90,6 +90,8 @@ def lib() -> ctypes.CDLL:
     L.bh_get_stats.argtypes = [vp, P(Stats), vp]
     L.bh_get_debug.argtypes = [vp, ctypes.c_char_p, vp, sz, vp]
     L.bh_check.argtypes = [vp, vp, P(ctypes.c_uint)]
+    f32 = ctypes.c_float
+    L.bh_render.argtypes = [vp, i32, i32, f32, f32, f32, f32, vp, vp]
     L.bh_step_profiled.argtypes = [vp, vp, vp]
     L.bh_direct_sum_f64.argtypes = [vp, i32, vp, vp, vp]
     L.bh_measure_fp32_peak.argtypes = [i32, P(ctypes.c_double)]
@@ -301,6 +303,17 @@ class BarnesHutSystem:
                     max_stack=int(s.max_stack), walk_rounds=int(s.walk_rounds),
                     nodes_tested=int(s.nodes_tested),
                     cell_interactions=int(s.cell_interactions))
+
+    def render(self, width: int = 1000, height: int = 1000,
+               extent=(-25.0, 25.0, -25.0, 25.0), stream=None) -> np.ndarray:
+        """The current positions as one-pixel points (bh_render): uint8 array
+        (height, width, 4), RGBA, top row first.  The default view is the
+        reference viewer's: 1000 x 1000 pixels over [-25, 25]^2."""
+        out = np.empty((height, width, 4), np.uint8)
+        _check(lib().bh_render(self._h, width, height, *[float(e) for e in extent], _p(out),
+                               stream), "bh_render")
+        self.sync(stream)
+        return out
 
     def check(self, stream=None) -> int:
         """Tree invariants of the last step checked on the device (bh_check):

@@ -15,6 +15,7 @@
 
 #include "bh_check.cuh"
 #include "bh_engine.h"
+#include "bh_render.cuh"
 #include "bh_walk.cuh"
 #include "stellar_bh.h"
 
@@ -173,6 +174,9 @@ struct bh_system {
     int walk_grid_ref = 0, walk_grid_acc = 0;
     bool have_state = false;
     bool caller_order = false;  // true from bh_set_state until the next step
+
+    uint32_t* image = nullptr;  // bh_render: per-pixel counts, then RGBA8
+    size_t image_pixels = 0;
 
     cudaStream_t cap_stream = nullptr;
     cudaGraph_t graph = nullptr;
@@ -648,6 +652,7 @@ int bh_destroy(bh_system* s) {
     cudaSetDevice(s->device);
     drop_graph(s);
     if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
+    cudaFree(s->image);
     cudaFree(s->arena);
     delete s;
     return BH_OK;
@@ -850,6 +855,33 @@ int bh_get_stats(bh_system* s, bh_stats* out, void* stream) {
     out->cells = (int32_t)cells;
     out->nodes = nodes;
     out->max_depth = maxd;
+    return BH_OK;
+}
+
+int bh_render(bh_system* s, int width, int height, float x0, float x1, float y0, float y1,
+              unsigned char* rgba, void* stream) {
+    if (!s || !rgba || width <= 0 || height <= 0 || (long long)width * height > (1ll << 28) ||
+        !(x1 > x0) || !(y1 > y0))
+        return BH_ERR_ARG;
+    if (!s->have_state) return BH_ERR_STATE;
+    CK(cudaSetDevice(s->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t pixels = (size_t)width * height;
+    if (pixels > s->image_pixels) {
+        CK(cudaStreamSynchronize(st));  // the old buffer may still be read
+        cudaFree(s->image);
+        s->image = nullptr;
+        s->image_pixels = 0;
+        CK(cudaMalloc(&s->image, sizeof(uint32_t) * pixels));
+        s->image_pixels = pixels;
+    }
+    const float sx = (float)width / (x1 - x0), sy = (float)height / (y1 - y0);
+    CK(cudaMemsetAsync(s->image, 0, sizeof(uint32_t) * pixels, st));
+    k_splat<<<(s->n + 255) / 256, 256, 0, st>>>(s->n, s->st[0].x, s->st[0].y, width, height, x0,
+                                                sx, y0, sy, s->image);
+    k_shade<<<(int)((pixels + 255) / 256), 256, 0, st>>>((int)pixels, s->image);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(rgba, s->image, sizeof(uint32_t) * pixels, cudaMemcpyDefault, st));
     return BH_OK;
 }
 

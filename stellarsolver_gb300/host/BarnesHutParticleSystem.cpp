@@ -131,6 +131,21 @@ void BarnesHutParticleSystem::update() {
 
 const float* BarnesHutParticleSystem::getOutputBuffer() { return h_output.data(); }
 
+bool BarnesHutParticleSystem::writeImage(const char* path, int width, int height) {
+    std::vector<unsigned char> rgba((size_t)width * height * 4);
+    check(bh_render(sys, width, height, -25.0f, 25.0f, -25.0f, 25.0f, rgba.data(), nullptr),
+          "bh_render");
+    check(bh_sync(sys, nullptr), "bh_sync");
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return false;
+    std::fprintf(f, "P6\n%d %d\n255\n", width, height);
+    std::vector<unsigned char> rgb((size_t)width * height * 3);
+    for (size_t p = 0; p < (size_t)width * height; ++p)
+        for (int c = 0; c < 3; ++c) rgb[3 * p + c] = rgba[4 * p + c];
+    const bool ok = std::fwrite(rgb.data(), 1, rgb.size(), f) == rgb.size();
+    return std::fclose(f) == 0 && ok;
+}
+
 // debug.cpp:23-174, restated on the engine's tree and run on the device
 // (bh_check); one line per invariant, in the reference's format.
 void BarnesHutParticleSystem::runDebugTests() {

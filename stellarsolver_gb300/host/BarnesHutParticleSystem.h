@@ -35,6 +35,10 @@ class BarnesHutParticleSystem {
     void reset();
 
     const float* getOutputBuffer();
+    // Headless stand-in for the reference's viewer frame (StellarSolverVisualizer.cpp:
+    // 208-253): the current positions as one-pixel points over [-25, 25]^2, written to
+    // `path` as a binary PPM (P6, RGB).  Returns false if the file cannot be written.
+    bool writeImage(const char* path, int width = 1000, int height = 1000);
 
     // Additions: the engine settings that the reference fixes at compile time.
     void setEngineParams(const bh_params& p);

@@ -2,9 +2,10 @@
 // README.md:47-55): -disk | -plummer | -colliding-disks, -opengl, -benchmark,
 // -debug, -fullscreen, -iterations=<n>, -timestep=<f>, -gravity=<f>,
 // -dampening=<f>.  Additions: -n=<bodies> (the reference hard-codes 512*256),
-// -mode=reference|plain|mixed, -theta=<f>, -eps2=<f>, -graph.
+// -mode=reference|plain|mixed, -theta=<f>, -eps2=<f>, -graph, -image=<file.ppm>.
 // Headless: the reference's OpenGL viewer needs a graphics stack; -opengl
-// still fills the host output buffer every step, and nothing is drawn.
+// still fills the host output buffer every step, and -image writes the final
+// frame (the viewer's view, rendered by bh_render) to a PPM file.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -98,5 +99,12 @@ int main(int argc, char** argv) {
     const float* out = particles.getOutputBuffer();
     if (parameters.opengl && n > 0)
         std::printf("body 0 at (%g, %g)\n", out[0], out[1]);
+    if (const char* img = value(argc, argv, "image")) {
+        if (!particles.writeImage(img)) {
+            std::fprintf(stderr, "cannot write %s\n", img);
+            return 1;
+        }
+        std::printf("image written to %s\n", img);
+    }
     return 0;
 }

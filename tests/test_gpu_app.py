@@ -43,3 +43,17 @@ def test_opengl_is_headless_and_fills_the_output_buffer():
                        capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stderr
     assert "headless" in r.stdout and "body 0 at" in r.stdout
+
+
+def test_image_flag_writes_the_viewer_frame(tmp_path):
+    import numpy as np
+
+    path = tmp_path / "frame.ppm"
+    r = subprocess.run([app(), "-disk", "-iterations=3", "-n=20000", f"-image={path}"],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    data = path.read_bytes()
+    header = b"P6\n1000 1000\n255\n"
+    assert data.startswith(header) and len(data) == len(header) + 1000 * 1000 * 3
+    rgb = np.frombuffer(data[len(header):], np.uint8).reshape(1000, 1000, 3)
+    assert (rgb[..., 0] > 0).sum() > 1000 and np.array_equal(rgb[..., 0], rgb[..., 2])
