@@ -216,6 +216,17 @@ int bh_direct_sum_f64(bh_system* s, int ns, const int* idx, double* ax, double* 
  * changed.  Synchronous.  No reference counterpart. */
 int bh_energy(bh_system* s, void* stream, double* out);
 
+/* The same diagnostics recorded on the device after every `every`-th step of
+ * bh_step, into a ring of `capacity` records of 4*systems doubles (layout as
+ * bh_energy).  In graph mode the diagnostics pass is captured once as its own
+ * CUDA graph and launched after every k-th step graph; no host synchronisation.
+ * every = 0 turns the log off.  Resets the record count. */
+int bh_set_energy_log(bh_system* s, int every, int capacity);
+/* Synchronises `stream`; *records = records written since bh_set_energy_log
+ * (record r follows step every*(r+1)); out receives the last
+ * min(*records, capacity, max_records) of them, oldest first. */
+int bh_get_energy_log(bh_system* s, double* out, int max_records, int* records, void* stream);
+
 /* Measure the device's FP32 FMA throughput (TFLOP/s, 2 flops per FMA) with a
  * register-only kernel on every SM; the roofline denominator of the force
  * walk.  device -1 = current.  No reference counterpart. */

@@ -90,6 +90,8 @@ def lib() -> ctypes.CDLL:
     L.bh_get_stats.argtypes = [vp, P(Stats), vp]
     L.bh_get_debug.argtypes = [vp, ctypes.c_char_p, vp, sz, vp]
     L.bh_check.argtypes = [vp, vp, P(ctypes.c_uint)]
+    L.bh_set_energy_log.argtypes = [vp, i32, i32]
+    L.bh_get_energy_log.argtypes = [vp, vp, i32, P(ctypes.c_int), vp]
     f32 = ctypes.c_float
     L.bh_render.argtypes = [vp, i32, i32, f32, f32, f32, f32, vp, vp]
     L.bh_step_profiled.argtypes = [vp, vp, vp]
@@ -267,6 +269,21 @@ class BarnesHutSystem:
         out = np.zeros(4 * self.num_systems, np.float64)
         _check(lib().bh_energy(self._h, stream, _p(out)), "bh_energy")
         return out.reshape(-1, 4)
+
+    def set_energy_log(self, every: int, capacity: int = 64):
+        """Record FP64 energy/momentum on the device after every `every`-th step."""
+        _check(lib().bh_set_energy_log(self._h, every, capacity), "bh_set_energy_log")
+        self._elog_cap = capacity
+
+    def energy_log(self, stream=None):
+        """(records written, array (kept, systems, 4)) of the energy log, oldest first."""
+        cap = getattr(self, "_elog_cap", 0)
+        out = np.zeros(max(cap, 1) * 4 * self.num_systems, np.float64)
+        rec = ctypes.c_int(0)
+        _check(lib().bh_get_energy_log(self._h, _p(out), cap, ctypes.byref(rec), stream),
+               "bh_get_energy_log")
+        kept = min(rec.value, cap)
+        return rec.value, out[: kept * 4 * self.num_systems].reshape(kept, self.num_systems, 4)
 
     def autotune(self, stream=None) -> dict:
         """Pick the walk's block size, leaf bucket and stack depth (bh_autotune)."""

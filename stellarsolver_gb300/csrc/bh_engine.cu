@@ -178,6 +178,14 @@ struct bh_system {
     uint32_t* image = nullptr;  // bh_render: per-pixel counts, then RGBA8
     size_t image_pixels = 0;
 
+    // energy log: FP64 diagnostics after every `energy_every`-th bh_step
+    int energy_every = 0, energy_cap = 0;
+    long long energy_steps = 0;     // steps since bh_set_energy_log
+    double* elog = nullptr;         // [energy_cap][4 * nseg] ring
+    int* elog_count = nullptr;      // records written (device)
+    cudaGraph_t egraph = nullptr;   // captured diagnostics pass (graph mode)
+    cudaGraphExec_t egraph_exec = nullptr;
+
     cudaStream_t cap_stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
@@ -190,6 +198,10 @@ void drop_graph(bh_system* s) {
     if (s->graph) cudaGraphDestroy(s->graph);
     s->graph_exec = nullptr;
     s->graph = nullptr;
+    if (s->egraph_exec) cudaGraphExecDestroy(s->egraph_exec);
+    if (s->egraph) cudaGraphDestroy(s->egraph);
+    s->egraph_exec = nullptr;
+    s->egraph = nullptr;
 }
 
 bool params_ok(const bh_params* p) {
@@ -653,6 +665,8 @@ int bh_destroy(bh_system* s) {
     drop_graph(s);
     if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
     cudaFree(s->image);
+    cudaFree(s->elog);
+    cudaFree(s->elog_count);
     cudaFree(s->arena);
     delete s;
     return BH_OK;
@@ -772,6 +786,9 @@ int bh_get_positions_hilo(bh_system* s, float* xhi, float* xlo, float* yhi, floa
     return scatter_out(s, c.x, c.xlo, c.y, c.ylo, xhi, xlo, yhi, ylo, (cudaStream_t)stream);
 }
 
+int build_energy_graph(bh_system* s);
+int enqueue_energy_log(bh_system* s, cudaStream_t st);
+
 int bh_step(bh_system* s, int steps, void* stream) {
     if (!s || steps < 0) return BH_ERR_ARG;
     if (!s->have_state) return BH_ERR_STATE;
@@ -789,14 +806,33 @@ int bh_step(bh_system* s, int steps, void* stream) {
             int rc = build_graph(s);
             if (rc != BH_OK) return rc;
         }
-        for (int k = 0; k < steps; ++k) CK(cudaGraphLaunch(s->graph_exec, st));
-        if (steps > 0) s->caller_order = false;
+        for (int k = 0; k < steps; ++k) {
+            CK(cudaGraphLaunch(s->graph_exec, st));
+            s->caller_order = false;
+            if (s->energy_every > 0 && ++s->energy_steps % s->energy_every == 0) {
+                if (!s->egraph_exec) {
+                    // the capture stream must see what `stream` has produced
+                    cudaEvent_t ev;
+                    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+                    CK(cudaEventRecord(ev, st));
+                    CK(cudaStreamWaitEvent(s->cap_stream, ev, 0));
+                    cudaEventDestroy(ev);
+                    int rc = build_energy_graph(s);
+                    if (rc != BH_OK) return rc;
+                }
+                CK(cudaGraphLaunch(s->egraph_exec, st));
+            }
+        }
         return BH_OK;
     }
     for (int k = 0; k < steps; ++k) {
         int rc = enqueue_step(s, st);
         if (rc != BH_OK) return rc;
         s->caller_order = false;
+        if (s->energy_every > 0 && ++s->energy_steps % s->energy_every == 0) {
+            rc = enqueue_energy_log(s, st);
+            if (rc != BH_OK) return rc;
+        }
     }
     return BH_OK;
 }
@@ -1076,11 +1112,10 @@ __global__ void k_energy_reduce(int n, Segs segs, const float* __restrict__ m,
     atomicAdd(o + 3, mi * v);
 }
 
-int bh_energy(bh_system* s, void* stream, double* out) {
-    if (!s || !out) return BH_ERR_ARG;
-    if (!s->have_state) return BH_ERR_STATE;
-    CK(cudaSetDevice(s->device));
-    cudaStream_t st = (cudaStream_t)stream;
+// The diagnostics pass on `st`, no synchronisation: the tree of the current
+// positions, a potential walk (FP64 sums per body), then per-system sums of
+// kinetic and potential energy and momentum into s->diag.
+int enqueue_energy(bh_system* s, cudaStream_t st) {
     int rc = enqueue_front(s, st, true, nullptr);  // tree of the current positions
     if (rc != BH_OK) return rc;
     StepArgs a = step_args(s);
@@ -1102,11 +1137,100 @@ int bh_energy(bh_system* s, void* stream, double* out) {
     const BodyPtrs& g = s->st[1];
     k_energy_reduce<<<(s->n + 255) / 256, 256, 0, st>>>(s->n, segs, g.m, g.vx, g.vy, pot, s->diag);
     CK(cudaGetLastError());
+    return BH_OK;
+}
+
+int bh_energy(bh_system* s, void* stream, double* out) {
+    if (!s || !out) return BH_ERR_ARG;
+    if (!s->have_state) return BH_ERR_STATE;
+    CK(cudaSetDevice(s->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    int rc = enqueue_energy(s, st);
+    if (rc != BH_OK) return rc;
     CK(cudaMemcpyAsync(out, s->diag, sizeof(double) * 4 * s->nseg, cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     int bits = 0;
     CK(cudaMemcpy(&bits, s->status, sizeof(int), cudaMemcpyDeviceToHost));
     return status_code(bits, BH_MODE_PLAIN);
+}
+
+// Append s->diag to the ring log (one block).
+__global__ void k_energy_log(const double* __restrict__ diag, int values, double* __restrict__ log,
+                             int* __restrict__ count, int cap) {
+    __shared__ int s_slot;
+    if (threadIdx.x == 0) s_slot = *count % cap;
+    __syncthreads();
+    for (int i = threadIdx.x; i < values; i += blockDim.x) log[(size_t)s_slot * values + i] = diag[i];
+    __syncthreads();
+    if (threadIdx.x == 0) *count += 1;
+}
+
+int enqueue_energy_log(bh_system* s, cudaStream_t st) {
+    int rc = enqueue_energy(s, st);
+    if (rc != BH_OK) return rc;
+    k_energy_log<<<1, 256, 0, st>>>(s->diag, 4 * s->nseg, s->elog, s->elog_count, s->energy_cap);
+    CK(cudaGetLastError());
+    return BH_OK;
+}
+
+int build_energy_graph(bh_system* s) {
+    if (!s->cap_stream) CK(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
+    CK(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal));
+    int st = enqueue_energy_log(s, s->cap_stream);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s->cap_stream, &g);
+    if (st != BH_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    s->egraph = g;
+    CK(cudaGraphInstantiate(&s->egraph_exec, g, 0));
+    return BH_OK;
+}
+
+int bh_set_energy_log(bh_system* s, int every, int capacity) {
+    if (!s || every < 0 || (every > 0 && capacity <= 0)) return BH_ERR_ARG;
+    CK(cudaSetDevice(s->device));
+    CK(cudaDeviceSynchronize());  // no step may still write the old log
+    cudaFree(s->elog);
+    cudaFree(s->elog_count);
+    s->elog = nullptr;
+    s->elog_count = nullptr;
+    if (s->egraph_exec) cudaGraphExecDestroy(s->egraph_exec);
+    if (s->egraph) cudaGraphDestroy(s->egraph);
+    s->egraph_exec = nullptr;
+    s->egraph = nullptr;
+    s->energy_every = 0;
+    s->energy_cap = 0;
+    s->energy_steps = 0;
+    if (every == 0) return BH_OK;
+    CK(cudaMalloc(&s->elog, sizeof(double) * 4 * s->nseg * (size_t)capacity));
+    CK(cudaMalloc(&s->elog_count, sizeof(int)));
+    CK(cudaMemset(s->elog_count, 0, sizeof(int)));
+    s->energy_every = every;
+    s->energy_cap = capacity;
+    return BH_OK;
+}
+
+int bh_get_energy_log(bh_system* s, double* out, int max_records, int* records, void* stream) {
+    if (!s || !records || (max_records > 0 && !out)) return BH_ERR_ARG;
+    *records = 0;
+    if (!s->energy_every) return BH_OK;
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize((cudaStream_t)stream));
+    int count = 0;
+    CK(cudaMemcpy(&count, s->elog_count, sizeof(int), cudaMemcpyDeviceToHost));
+    *records = count;
+    // the last min(count, capacity, max_records) records, oldest first
+    const int keep = std::min(std::min(count, s->energy_cap), std::max(max_records, 0));
+    const size_t rec = 4 * (size_t)s->nseg;
+    for (int r = 0; r < keep; ++r) {
+        const int idx = count - keep + r;
+        CK(cudaMemcpy(out + r * rec, s->elog + (size_t)(idx % s->energy_cap) * rec,
+                      sizeof(double) * rec, cudaMemcpyDeviceToHost));
+    }
+    return BH_OK;
 }
 
 int bh_autotune(bh_system* s, void* stream, bh_params* chosen) {

@@ -227,3 +227,28 @@ def test_autotune_keeps_results_and_accuracy(bh, oracle):
         ax, ay = s.get_accel()
     rms, mx = force_error(oracle, x, y, m, ax, ay, 1e-4)
     assert rms <= 1e-3, (rms, mx)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_energy_log_every_k_steps(bh, graph):
+    """Diagnostics recorded on the device every 5 steps equal bh_energy called at
+    those steps (FP64 sums with atomics: equal to 1e-12 relative)."""
+    from stellarsolver_gb300 import models
+
+    x, y, vx, vy, m = models.plummer(1 << 14, 0x5EED7000)
+    kw = dict(mode="mixed", eps2=1e-4, timestep=1e-3, use_graph=graph)
+    with bh.BarnesHutSystem(len(x), **kw) as a, bh.BarnesHutSystem(len(x), **kw) as b:
+        a.set_state(x, y, vx, vy, m)
+        b.set_state(x, y, vx, vy, m)
+        a.set_energy_log(5, capacity=3)
+        a.step(23)
+        count, log = a.energy_log()
+        want = []
+        for _ in range(4):
+            b.step(5)
+            want.append(b.energy())
+        b.step(3)
+        assert count == 4 and log.shape == (3, 1, 4)
+        np.testing.assert_allclose(log, np.array(want[1:]), rtol=1e-12, atol=0)
+        st_a, st_b = a.get_state(), b.get_state()
+        assert np.array_equal(st_a["x"], st_b["x"])  # the diagnostics leave the state alone
