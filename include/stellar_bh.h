@@ -35,6 +35,9 @@ extern "C" {
 #define BH_ERR_NOMEM 7          /* device or host allocation failed */
 #define BH_ERR_STATE 8          /* call out of order (e.g. step before set_state) */
 #define BH_ERR_NO_DEVICE 9      /* no CUDA device, or not an sm_103 device */
+#define BH_ERR_TREE 10          /* a traversal exceeded its bound: the tree is not a valid
+                                   tree of the keys (never for a valid build; reported
+                                   instead of looping) */
 
 /* ---------------------------------------------------------------- modes */
 /* REFERENCE: the reference's force law and opening rule, bit-for-bit tree:

@@ -25,7 +25,7 @@ BH_OK = 0
 STATUS_NAMES = {
     0: "BH_OK", 1: "BH_ERR_ARG", 2: "BH_ERR_DUPLICATE_KEYS", 3: "BH_ERR_NONFINITE",
     4: "BH_ERR_CAPACITY", 5: "BH_ERR_STACK", 6: "BH_ERR_CUDA", 7: "BH_ERR_NOMEM",
-    8: "BH_ERR_STATE", 9: "BH_ERR_NO_DEVICE",
+    8: "BH_ERR_STATE", 9: "BH_ERR_NO_DEVICE", 10: "BH_ERR_TREE",
 }
 
 

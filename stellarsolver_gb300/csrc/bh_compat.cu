@@ -553,6 +553,7 @@ int fetch_status(Workspace* w) {
     if (bits & ST_DUP) return BH_ERR_DUPLICATE_KEYS;
     if (bits & ST_STACK) return BH_ERR_STACK;
     if (bits & ST_CAPACITY) return BH_ERR_CAPACITY;
+    if (bits & ST_TREE) return BH_ERR_TREE;
     return BH_OK;
 }
 
@@ -670,7 +671,8 @@ void compat_BuildQuadTree(float* x, float* y, float* mass, int* count, int* star
     k_build<<<nb, 256, 0, st>>>(ka, n, segs, w->tree, w->status);
     record_cuda(cudaMemsetAsync(w->counter, 0, sizeof(int) * n, st), "BuildQuadTree memset");
     k_moments<<<(n + kMomentsThreads - 1) / kMomentsThreads, kMomentsThreads, 0, st>>>(
-        n, 0, w->sx, w->sy, w->sm, w->tree.climb, w->tree.leaf_parent, w->counter, w->sums);
+        n, 0, w->sx, w->sy, w->sm, w->tree.climb, w->tree.leaf_parent, w->counter, w->sums,
+        w->status);
     k_c_ncells<<<nb, 256, 0, st>>>(n, w->tree.split, w->tree.parent, w->ncell);
     const int sb = blocks_for(n, 1024);
     k_c_scan_block<<<sb, 1024, 0, st>>>(w->ncell, w->cbase, w->bsum, n);
@@ -898,7 +900,7 @@ extern "C" int BuildQuadTreeNoAlloc(float* x, float* y, float* mass, int* count,
     k_c_gather3<<<nb, 256, 0, st>>>(n, va, x, y, mass, w.sx, w.sy, w.sm);
     k_build<<<nb, 256, 0, st>>>(ka, n, segs, w.tree, w.status);
     k_moments<<<(n + kMomentsThreads - 1) / kMomentsThreads, kMomentsThreads, 0, st>>>(
-        n, 0, w.sx, w.sy, w.sm, w.tree.climb, w.tree.leaf_parent, w.counter, w.sums);
+        n, 0, w.sx, w.sy, w.sm, w.tree.climb, w.tree.leaf_parent, w.counter, w.sums, w.status);
     k_c_ncells<<<nb, 256, 0, st>>>(n, w.tree.split, w.tree.parent, w.ncell);
     const int sb = blocks_for(n, 1024);
     k_c_scan_block<<<sb, 1024, 0, st>>>(w.ncell, w.cbase, w.bsum, n);
@@ -918,5 +920,6 @@ extern "C" int BuildQuadTreeNoAlloc(float* x, float* y, float* mass, int* count,
     if (bits & ST_DUP) return BH_ERR_DUPLICATE_KEYS;
     if (bits & ST_CAPACITY) return BH_ERR_CAPACITY;
     if (bits & ST_NONFINITE) return BH_ERR_NONFINITE;
+    if (bits & ST_TREE) return BH_ERR_TREE;
     return BH_OK;
 }

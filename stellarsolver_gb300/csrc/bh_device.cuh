@@ -29,7 +29,7 @@ constexpr unsigned kFull = 0xffffffffu;
 constexpr int kNoChild = INT_MIN;
 
 // sticky device status bits, mapped to BH_* codes by the host
-enum : int { ST_DUP = 1, ST_NONFINITE = 2, ST_STACK = 4, ST_CAPACITY = 8 };
+enum : int { ST_DUP = 1, ST_NONFINITE = 2, ST_STACK = 4, ST_CAPACITY = 8, ST_TREE = 16 };
 
 // ------------------------------------------------------------------ helpers
 
@@ -563,12 +563,15 @@ __device__ __forceinline__ int atomic_add_acq_rel_gpu(int* p, int v) {
     return old;
 }
 
+constexpr int kMaxClimb = 256;
+
 static __global__ void __launch_bounds__(kMomentsThreads) k_moments(int n, int accuracy, const float* __restrict__ sx,
                                                      const float* __restrict__ sy,
                                                      const float* __restrict__ sm,
                                                      const int4* __restrict__ climb,
                                                      const int* __restrict__ leaf_parent,
-                                                     int* __restrict__ counter, NodeSums ns) {
+                                                     int* __restrict__ counter, NodeSums ns,
+                                                     int* __restrict__ status) {
     __shared__ int s_cnt[kMomentsThreads];
     const int c0 = blockIdx.x * kMomentsThreads;  // this block's leaves: [c0, c0 + kMomentsThreads)
     const int j = c0 + threadIdx.x;
@@ -577,10 +580,15 @@ static __global__ void __launch_bounds__(kMomentsThreads) k_moments(int n, int a
     if (j >= n) return;
     int p = leaf_parent[j];
     if (p < 0) return;
-    int4 T = climb[p];  // left, right, parent, range inside one 32-leaf chunk
+    int4 T = climb[p];  // left, right, parent, range inside one moments block
     int from = ~j;      // the child this thread climbs from
     ChildVals own = body_vals(j, sx, sy, sm);
-    for (;;) {
+    // a radix tree of 64-bit keys (ties broken by position) is at most 96 levels deep
+    for (int level = 0;; ++level) {
+        if (level == kMaxClimb) {
+            atomicOr(status, ST_TREE);
+            return;
+        }
         int4 TN = make_int4(0, 0, -1, 0);
         if (T.z >= 0) TN = climb[T.z];
         if (T.w) {

@@ -301,7 +301,7 @@ int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev)
     CK(mark(5));
     k_moments<<<(n + kMomentsThreads - 1) / kMomentsThreads, kMomentsThreads, 0, st>>>(
         n, accuracy ? 1 : 0, dst.x, dst.y, dst.m, s->tree.climb, s->tree.leaf_parent, s->counter,
-        s->sums);
+        s->sums, s->status);
     k_records<<<nb, tb, 0, st>>>(n, segs, accuracy ? 1 : 0, s->p.theta, s->p.gravity, s->box_ord,
                                  ka, s->tree, s->sums, s->rec);
     CK(cudaGetLastError());
@@ -450,6 +450,7 @@ int status_code(int bits, int mode) {
     if ((bits & ST_DUP) && mode == BH_MODE_REFERENCE) return BH_ERR_DUPLICATE_KEYS;
     if (bits & ST_STACK) return BH_ERR_STACK;
     if (bits & ST_CAPACITY) return BH_ERR_CAPACITY;
+    if (bits & ST_TREE) return BH_ERR_TREE;
     return BH_OK;
 }
 
@@ -1331,6 +1332,7 @@ const char* bh_status_string(int st) {
         case BH_ERR_NONFINITE: return "non-finite position";
         case BH_ERR_CAPACITY: return "capacity exceeded";
         case BH_ERR_STACK: return "walk stack overflow";
+        case BH_ERR_TREE: return "tree traversal bound exceeded";
         case BH_ERR_CUDA: return "CUDA error";
         case BH_ERR_NOMEM: return "out of memory";
         case BH_ERR_STATE: return "call out of order";

@@ -75,6 +75,10 @@ __device__ __forceinline__ float ref_r(float cx, float cy, float px, float py, f
     return __fadd_rn(__fadd_rn(__fmul_rn(*dx, *dx), __fmul_rn(*dy, *dy)), eps2);
 }
 
+// Rounds of node tests one group may take.  A valid tree gives a group at most
+// one test per node, far below this; beyond it the tree is not a tree.
+constexpr int kMaxWalkRounds = 1 << 22;
+
 template <int WARPS, int STACK>
 __global__ void __launch_bounds__(WARPS * 32) k_walk_ref(Segs segs, Groups gr, WalkIn in,
                                                          const float4* __restrict__ recA,
@@ -114,7 +118,12 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk_ref(Segs segs, Groups gr, W
                     top = 1;
                 }
             }
+            int pops = 0;
             while (top > 0 && !overflow) {
+                if (++pops > kMaxWalkRounds) {  // far beyond any valid tree
+                    if (lane == 0) atomicOr(status, ST_TREE);
+                    break;
+                }
                 __syncwarp();
                 const int node = stack[--top];
                 const int4 C = recC[node];
@@ -575,6 +584,10 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
             entries += k;
         };
         while (top > 0) {
+            if (rounds == kMaxWalkRounds) {  // far beyond any valid tree: report, do not loop
+                if (lane == 0) atomicOr(status, ST_TREE);
+                break;
+            }
             int k = min(32, top);
             if (top + 3 * k > STACK) {  // pop k, push <= 4k: keep top+3k <= STACK
                 k = max((STACK - top) / 3, 0);
