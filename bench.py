@@ -315,7 +315,8 @@ def run_e2e(bh, torch, stream, sp, n, x, y, vx, vy, m, params, local, args):
                             theta=params.theta, eps2=params.eps2, gravity=params.gravity,
                             timestep=params.timestep, dampening=params.dampening,
                             leaf_bucket=params.leaf_bucket, block_size=params.block_size,
-                            stack_depth=params.stack_depth, alpha=params.alpha) as s:
+                            stack_depth=params.stack_depth, alpha=params.alpha,
+                            bodies_per_lane=params.bodies_per_lane) as s:
         def one():
             rc = lib.bh_set_state(s.handle, ptr["x"], ptr["y"], ptr["vx"], ptr["vy"], ptr["m"], sp)
             rc |= lib.bh_step(s.handle, 1, sp)

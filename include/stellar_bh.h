@@ -73,6 +73,8 @@ typedef struct bh_params {
     float alpha;       /* PLAIN/MIXED relative opening tolerance: a cell of mass M and size l
                           at distance d is approximated only if G M l^3 / d^5 <= alpha |a_old|
                           (Springel 2005-style); 0 = geometric rule only; default 0.01 */
+    int bodies_per_lane; /* PLAIN/MIXED walk: a warp walks the tree once for 32 (1) or 64 (2)
+                            consecutive bodies; 0 = tuned default */
 } bh_params;
 
 typedef struct bh_system bh_system;

@@ -563,8 +563,8 @@ int64_t orc_walk_acc(int n, const float* sx, const float* sy, const float* sm,
                      const uint64_t* skeys, const int32_t* left, const int32_t* right,
                      const int32_t* split, const int32_t* first, const int32_t* last,
                      const int32_t* qchild, const float* box, float theta, float eps2, float G,
-                     int bucket, float alpha, const float* aold, int quadrupole, float* sax,
-                     float* say) {
+                     int bucket, float alpha, const float* aold, int quadrupole, int group,
+                     float* sax, float* say) {
     if (n < 2) {
         for (int i = 0; i < n; ++i) sax[i] = say[i] = 0.0f;
         return 0;
@@ -593,7 +593,8 @@ int64_t orc_walk_acc(int n, const float* sx, const float* sy, const float* sm,
         qerr[i] = (float)((double)G * mom[i].m * l * l * l);
     }
     const int relative = aold != NULL && alpha > 0.0f;
-    int groups = (n + 31) / 32;
+    if (group != 64) group = 32;  /* bodies per group: 32, or 64 (two per lane) */
+    int groups = (n + group - 1) / group;
     int64_t total = 0;
 #pragma omp parallel reduction(+ : total)
     {
@@ -601,8 +602,8 @@ int64_t orc_walk_acc(int n, const float* sx, const float* sy, const float* sm,
         int32_t* stack = (int32_t*)malloc(sizeof(int32_t) * (size_t)cap);
 #pragma omp for schedule(dynamic, 4)
         for (int g = 0; g < groups; ++g) {
-            int g0 = 32 * g, cnt = n - g0 < 32 ? n - g0 : 32;
-            float px[32], py[32], ax[32], ay[32];
+            int g0 = group * g, cnt = n - g0 < group ? n - g0 : group;
+            float px[64], py[64], ax[64], ay[64];
             float aa = INFINITY;
             if (relative) {
                 float amin = INFINITY, amean = 0.0f;

@@ -99,13 +99,13 @@ void orc_energy_f64(int n, const float* x, const float* y, const float* vx, cons
  * buckets, geometric + relative opening rule (see oracle.c; aold = |a| of the
  * previous step in sorted order, NULL for the geometric-only bootstrap pass;
  * quadrupole = 0 evaluates accepted cells as monopoles, as the engine's
- * bootstrap pass does).  Output in sorted order; returns the interaction count. */
+ * bootstrap pass does; group = bodies per walk group, 32 or 64).  Output in sorted order; returns the interaction count. */
 int64_t orc_walk_acc(int n, const float* sx, const float* sy, const float* sm,
                      const uint64_t* skeys, const int32_t* left, const int32_t* right,
                      const int32_t* split, const int32_t* first, const int32_t* last,
                      const int32_t* qchild, const float* box, float theta, float eps2, float G,
-                     int bucket, float alpha, const float* aold, int quadrupole, float* sax,
-                     float* say);
+                     int bucket, float alpha, const float* aold, int quadrupole, int group,
+                     float* sax, float* say);
 
 /* Tree invariants (the engine's bh_check, restated for one system; the
  * reference's debug.cpp:23-174 on a binary radix tree): returns the mask of

@@ -51,7 +51,8 @@ def lib() -> ctypes.CDLL:
         L.orc_direct_f64_hilo.restype = None
         L.orc_energy_f64.argtypes = [i32] + [vp] * 5 + [f64, f64, vp]
         L.orc_energy_f64.restype = None
-        L.orc_walk_acc.argtypes = [i32] + [vp] * 11 + [f32, f32, f32, i32, f32, vp, i32, vp, vp]
+        L.orc_walk_acc.argtypes = [i32] + [vp] * 11 + [f32, f32, f32, i32, f32, vp, i32, i32, vp,
+                                                        vp]
         L.orc_walk_acc.restype = i64
         L.orc_check_tree.argtypes = [i32] + [vp] * 11
         L.orc_check_tree.restype = ctypes.c_uint
@@ -145,11 +146,12 @@ def walk_ref(sx, sy, sm, tree: Tree, node_m, node_cx, node_cy, box, theta, eps2)
 
 
 def walk_acc(sx, sy, sm, skeys, tree: Tree, box, theta, eps2, G=1.0, bucket=8, alpha=0.0,
-             aold=None, quadrupole=True):
+             aold=None, quadrupole=True, group=32):
     """The engine's PLAIN-mode walk restated on the CPU; returns (sax, say, interactions).
 
     aold: |a| of the previous step per sorted body (None = geometric rule only).
-    quadrupole=False: accepted cells as monopoles (the engine's bootstrap pass)."""
+    quadrupole=False: accepted cells as monopoles (the engine's bootstrap pass).
+    group: bodies per walk group (32, or 64 for two bodies per lane)."""
     n = len(sx)
     sax = np.zeros(n, np.float32)
     say = np.zeros(n, np.float32)
@@ -159,7 +161,7 @@ def walk_acc(sx, sy, sm, skeys, tree: Tree, box, theta, eps2, G=1.0, bucket=8, a
                                _p(tree.right), _p(tree.split), _p(tree.first), _p(tree.last),
                                _p(tree.qchild), _p(_f32(box)), theta, eps2, G, bucket, alpha,
                                _p(_f32(aold)) if aold is not None else None,
-                               1 if quadrupole else 0, _p(sax), _p(say))
+                               1 if quadrupole else 0, int(group), _p(sax), _p(say))
     return sax, say, int(inter)
 
 

@@ -41,7 +41,8 @@ class Params(ctypes.Structure):
                 ("gravity", ctypes.c_float), ("timestep", ctypes.c_float),
                 ("dampening", ctypes.c_float), ("leaf_bucket", ctypes.c_int),
                 ("block_size", ctypes.c_int), ("stack_depth", ctypes.c_int),
-                ("use_graph", ctypes.c_int), ("alpha", ctypes.c_float)]
+                ("use_graph", ctypes.c_int), ("alpha", ctypes.c_float),
+                ("bodies_per_lane", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -154,7 +155,7 @@ def measure_fp32_peak(device: int = -1) -> float:
 
 def make_params(mode="reference", theta=0.5, eps2=0.025, gravity=1.0, timestep=1e-3,
                 dampening=1.0, leaf_bucket=0, use_graph=False, stack_depth=0,
-                block_size=0, alpha=0.01) -> Params:
+                block_size=0, alpha=0.01, bodies_per_lane=0) -> Params:
     p = Params()
     lib().bh_default_params(ctypes.byref(p))
     p.mode = MODES[mode] if isinstance(mode, str) else int(mode)
@@ -163,6 +164,7 @@ def make_params(mode="reference", theta=0.5, eps2=0.025, gravity=1.0, timestep=1
     p.leaf_bucket, p.use_graph = int(leaf_bucket), int(bool(use_graph))
     p.stack_depth, p.block_size = int(stack_depth), int(block_size)
     p.alpha = alpha
+    p.bodies_per_lane = int(bodies_per_lane)
     return p
 
 
@@ -291,7 +293,7 @@ class BarnesHutSystem:
         _check(lib().bh_autotune(self._h, stream, ctypes.byref(p)), "bh_autotune")
         self.params = p
         return {"block_size": p.block_size, "leaf_bucket": p.leaf_bucket,
-                "stack_depth": p.stack_depth}
+                "stack_depth": p.stack_depth, "bodies_per_lane": p.bodies_per_lane}
 
     def step_profiled(self, phase_ms: np.ndarray, stream=None):
         """One non-graph step with events at the phase boundaries; adds each

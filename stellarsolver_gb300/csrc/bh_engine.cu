@@ -43,9 +43,11 @@ constexpr int kRefStack = 256;
 constexpr int kDefaultStack = 768;  // deepest measured: 670 (2D Plummer, N = 2^24)
 constexpr int kMaxStack = 2048;
 constexpr int kDefaultBucket = 8;
+constexpr int kDefaultBpl = 1;  // bodies per lane of the accuracy walk
 constexpr int kMaxBucket = 32;
 // worst case: 8 warps x (staging + 2048-entry stack + 32-body buckets)
-constexpr int kMaxWalkSmem = 8 * (3 * 32 * 16 + 32 * 8 + 64 * 4 + kMaxStack * 4 + (32 + 32 * kMaxBucket) * 4);
+constexpr int kMaxWalkSmem = 8 * (3 * 32 * 16 + 32 * 8 * 2 + 16 + 64 * 4 + kMaxStack * 4 +
+                                  (32 + 32 * kMaxBucket) * 4);
 constexpr int kBboxThreads = 256;
 constexpr int kBboxChunk = 8192;
 
@@ -72,37 +74,44 @@ namespace ssg {
 
 // Opt the accuracy walk into the largest shared-memory size it may use, once,
 // at creation (never while a graph is being captured).
-cudaError_t init_walk_attributes() {
-    const int bytes = kMaxWalkSmem;
-    cudaError_t e = cudaFuncSetAttribute(k_walk_acc<false, false>,
+template <int BPL>
+static cudaError_t walk_attributes(int bytes) {
+    cudaError_t e = cudaFuncSetAttribute(k_walk_acc<false, false, false, BPL>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_walk_acc<false, false, true>,
+        e = cudaFuncSetAttribute(k_walk_acc<false, false, true, BPL>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_walk_acc<true, false>,
+        e = cudaFuncSetAttribute(k_walk_acc<true, false, false, BPL>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_walk_acc<false, true>,
+        e = cudaFuncSetAttribute(k_walk_acc<false, true, false, BPL>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     return e;
 }
 
-template <bool MIXED>
+cudaError_t init_walk_attributes() {
+    cudaError_t e = walk_attributes<1>(kMaxWalkSmem);
+    if (e == cudaSuccess) e = walk_attributes<2>(kMaxWalkSmem);
+    return e;
+}
+
+template <bool MIXED, int BPL>
 static cudaError_t launch_acc(const StepArgs& a, cudaStream_t st, int part) {
-    const AccShape sh{a.stack, a.bucket};
+    const AccShape sh{a.stack, a.bucket, BPL};
+    const Groups& gr = BPL == 2 ? a.groups2 : a.groups;
     const int warps = a.warps;
     const size_t smem = (size_t)warps * acc_warp_bytes(sh);
-    int grid = std::min(a.walk_grid_acc, (a.groups.ngroups + warps - 1) / warps);
+    int grid = std::min(a.walk_grid_acc, (gr.ngroups + warps - 1) / warps);
     if (grid < 1) grid = 1;
     if (part == 0) {
         // bootstrap pass: exits at once unless bh_set_state left the state fresh
-        k_walk_acc<false, true><<<grid, warps * 32, smem, st>>>(
-            sh, a.segs, a.groups, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt,
+        k_walk_acc<false, true, false, BPL><<<grid, warps * 32, smem, st>>>(
+            sh, a.segs, gr, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt,
             a.alpha, a.out, a.status, a.inter, a.work + 1, a.fresh, a.max_stack);
     } else {
-        k_walk_acc<MIXED, false><<<grid, warps * 32, smem, st>>>(
-            sh, a.segs, a.groups, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt,
+        k_walk_acc<MIXED, false, false, BPL><<<grid, warps * 32, smem, st>>>(
+            sh, a.segs, gr, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt,
             a.alpha, a.out, a.status, a.inter, a.work + 2, a.fresh, a.max_stack);
     }
     return cudaGetLastError();
@@ -120,11 +129,16 @@ cudaError_t launch_walk(const StepArgs& a, cudaStream_t st, int part) {
             a.work);
         return cudaGetLastError();
     }
-    return a.mode == BH_MODE_MIXED ? launch_acc<true>(a, st, part) : launch_acc<false>(a, st, part);
+    if (a.bpl == 2)
+        return a.mode == BH_MODE_MIXED ? launch_acc<true, 2>(a, st, part)
+                                       : launch_acc<false, 2>(a, st, part);
+    return a.mode == BH_MODE_MIXED ? launch_acc<true, 1>(a, st, part)
+                                   : launch_acc<false, 1>(a, st, part);
 }
 
 int normalized_bucket(int b) { return b <= 0 ? kDefaultBucket : std::min(b, kMaxBucket); }
 int normalized_stack(int s) { return s <= 0 ? kDefaultStack : std::max(64, std::min(s, kMaxStack)); }
+int normalized_bpl(int b) { return b == 2 ? 2 : (b <= 0 ? kDefaultBpl : 1); }
 int normalized_warps(int block) {
     int w = block <= 0 ? kWalkWarps : block / 32;
     return std::max(1, std::min(w, 8));
@@ -154,10 +168,10 @@ struct bh_system {
     uint32_t *hist = nullptr, *totals = nullptr;
     int tiles = 0;
     int* box_ord = nullptr;
-    int *seg_off = nullptr, *seg_of_pos = nullptr, *gseg_off = nullptr;
+    int *seg_off = nullptr, *seg_of_pos = nullptr, *gseg_off = nullptr, *gseg_off2 = nullptr;
     int *chunk_seg = nullptr, *chunk_begin = nullptr, *chunk_end = nullptr;
     int nchunks = 0;
-    int ngroups = 0;
+    int ngroups = 0, ngroups2 = 0;  // groups of 32 and of 64 bodies
     TreePtrs tree{};
     int* counter = nullptr;
     NodeSums sums{};
@@ -217,6 +231,7 @@ ssg::StepArgs step_args(bh_system* s) {
     a.mode = s->p.mode;
     a.segs = Segs{s->nseg, s->seg_off, s->nseg > 1 ? s->seg_of_pos : nullptr};
     a.groups = Groups{s->ngroups, s->nseg > 1 ? s->gseg_off : nullptr};
+    a.groups2 = Groups{s->ngroups2, s->nseg > 1 ? s->gseg_off2 : nullptr};
     const BodyPtrs& g = s->st[1];
     const BodyPtrs& c = s->st[0];
     bool mixed = s->p.mode == BH_MODE_MIXED;
@@ -240,6 +255,7 @@ ssg::StepArgs step_args(bh_system* s) {
     a.max_stack = s->work + 3;
     a.bucket = normalized_bucket(s->p.leaf_bucket);
     a.stack = normalized_stack(s->p.stack_depth);
+    a.bpl = normalized_bpl(s->p.bodies_per_lane);
     a.warps = normalized_warps(s->p.block_size);
     a.walk_grid_ref = s->walk_grid_ref;
     a.walk_grid_acc = s->walk_grid_acc;
@@ -495,7 +511,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     s->seg_passes = nseg == 1 ? 0 : (nseg <= 256 ? 1 : 2);
 
     // chunk table for the box reduction and group table for the walks
-    std::vector<int> cseg, cbeg, cend, goff(nseg + 1, 0);
+    std::vector<int> cseg, cbeg, cend, goff(nseg + 1, 0), goff2(nseg + 1, 0);
     for (int sg = 0; sg < nseg; ++sg) {
         for (int b = s->h_off[sg]; b < s->h_off[sg + 1]; b += kBboxChunk) {
             cseg.push_back(sg);
@@ -503,15 +519,17 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
             cend.push_back(std::min(b + kBboxChunk, s->h_off[sg + 1]));
         }
         goff[sg + 1] = goff[sg] + (sizes[sg] + 31) / 32;
+        goff2[sg + 1] = goff2[sg] + (sizes[sg] + 63) / 64;
     }
     s->nchunks = (int)cseg.size();
     s->ngroups = goff[nseg];
+    s->ngroups2 = goff2[nseg];
 
     size_t bytes = 0;
     bytes += 2 * (8 * span<float>(N) + span<int>(N));
     bytes += 2 * span<uint64_t>(N) + 2 * span<uint32_t>(N);
     bytes += span<uint32_t>((size_t)256 * s->tiles) + span<uint32_t>(256);
-    bytes += span<int>(4 * (size_t)nseg) + 2 * span<int>(nseg + 1) + span<int>(N);
+    bytes += span<int>(4 * (size_t)nseg) + 3 * span<int>(nseg + 1) + span<int>(N);
     bytes += 3 * span<int>(s->nchunks);
     bytes += 8 * span<int>(N) + span<int4>(N);                  // tree arrays, counter, climb
     bytes += 2 * span<float4>(N);                               // node sums
@@ -547,6 +565,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     s->box_ord = carve<int>(c, 4 * (size_t)nseg);
     s->seg_off = carve<int>(c, nseg + 1);
     s->gseg_off = carve<int>(c, nseg + 1);
+    s->gseg_off2 = carve<int>(c, nseg + 1);
     s->seg_of_pos = carve<int>(c, N);
     s->chunk_seg = carve<int>(c, s->nchunks);
     s->chunk_begin = carve<int>(c, s->nchunks);
@@ -589,6 +608,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     };
     up(s->seg_off, s->h_off.data(), sizeof(int) * (nseg + 1));
     up(s->gseg_off, goff.data(), sizeof(int) * (nseg + 1));
+    up(s->gseg_off2, goff2.data(), sizeof(int) * (nseg + 1));
     if (nseg > 1) up(s->seg_of_pos, sop.data(), sizeof(int) * N);
     up(s->chunk_seg, cseg.data(), sizeof(int) * s->nchunks);
     up(s->chunk_begin, cbeg.data(), sizeof(int) * s->nchunks);
@@ -604,7 +624,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(
             &bref, k_walk_ref<kWalkWarps, kRefStack>, kWalkWarps * 32, 0);
         // grid cap from the worst-case shape; the walks fetch groups dynamically
-        const AccShape sh{kDefaultStack, kDefaultBucket};
+        const AccShape sh{kDefaultStack, kDefaultBucket, 1};
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bacc, k_walk_acc<true, false>,
                                                       kWalkWarps * 32,
                                                       (size_t)kWalkWarps * acc_warp_bytes(sh));
@@ -641,6 +661,7 @@ void bh_default_params(bh_params* p) {
     p->stack_depth = 0;
     p->use_graph = 0;
     p->alpha = 0.01f;
+    p->bodies_per_lane = 0;
 }
 
 int bh_create(const bh_params* p, int n, int device, bh_system** out) {
@@ -1121,17 +1142,23 @@ int enqueue_energy(bh_system* s, cudaStream_t st) {
     if (rc != BH_OK) return rc;
     StepArgs a = step_args(s);
     a.alpha = 0.0f;
-    const AccShape sh{a.stack, a.bucket};
+    const AccShape sh{a.stack, a.bucket, a.bpl};
+    const Groups& gr = a.bpl == 2 ? a.groups2 : a.groups;
     const size_t smem = (size_t)a.warps * acc_warp_bytes(sh);
-    int grid = std::min(a.walk_grid_acc, (a.groups.ngroups + a.warps - 1) / a.warps);
+    int grid = std::min(a.walk_grid_acc, (gr.ngroups + a.warps - 1) / a.warps);
     if (grid < 1) grid = 1;
     // the sort's spare key buffer holds the per-body potential (8 bytes per body)
     double* pot = reinterpret_cast<double*>(s->kfinal == s->keys ? s->keys_alt : s->keys);
     int* counter = s->work + 6;  // dynamic scheduling of this pass; work[7]: its stack peak
     CK(cudaMemsetAsync(counter, 0, 2 * sizeof(int), st));
-    k_walk_acc<false, false, true><<<grid, a.warps * 32, smem, st>>>(
-        sh, a.segs, a.groups, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt, 0.0f,
-        a.out, a.status, a.inter, counter, a.fresh, s->work + 7, pot);
+    if (a.bpl == 2)
+        k_walk_acc<false, false, true, 2><<<grid, a.warps * 32, smem, st>>>(
+            sh, a.segs, gr, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt, 0.0f,
+            a.out, a.status, a.inter, counter, a.fresh, s->work + 7, pot);
+    else
+        k_walk_acc<false, false, true, 1><<<grid, a.warps * 32, smem, st>>>(
+            sh, a.segs, gr, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt, 0.0f,
+            a.out, a.status, a.inter, counter, a.fresh, s->work + 7, pot);
     CK(cudaGetLastError());
     CK(cudaMemsetAsync(s->diag, 0, sizeof(double) * 4 * s->nseg, st));
     Segs segs{s->nseg, s->seg_off, s->nseg > 1 ? s->seg_of_pos : nullptr};
@@ -1279,16 +1306,19 @@ int bh_autotune(bh_system* s, void* stream, bh_params* chosen) {
         const int stack = std::min(kMaxStack, std::max(256, ((peak * 3 / 2) + 127) / 128 * 128));
         const int blocks[2] = {128, 256};
         const int buckets[3] = {4, 8, 16};
+        const int bpls[2] = {1, 2};
         cudaEvent_t e0 = nullptr, e1 = nullptr;
         if (rc == BH_OK) {
             CK(cudaEventCreate(&e0));
             CK(cudaEventCreate(&e1));
         }
+        for (int li = 0; li < 2 && rc == BH_OK; ++li)
         for (int bi = 0; bi < 2 && rc == BH_OK; ++bi) {
             for (int ki = 0; ki < 3 && rc == BH_OK; ++ki) {
                 bh_params cand = orig;
                 cand.block_size = blocks[bi];
                 cand.leaf_bucket = buckets[ki];
+                cand.bodies_per_lane = bpls[li];
                 cand.stack_depth = stack;
                 cand.use_graph = 0;
                 s->p = cand;

@@ -17,7 +17,8 @@ int cuda_fail(cudaError_t e, const char* what);
 struct StepArgs {
     int mode;
     Segs segs;
-    Groups groups;
+    Groups groups;   // groups of 32 consecutive bodies
+    Groups groups2;  // groups of 64 (accuracy walk with two bodies per lane)
     WalkIn in;
     WalkOut out;
     const float4* recA;
@@ -31,6 +32,7 @@ struct StepArgs {
     int* fresh;  // set by bh_set_state: the next step bootstraps |a_old|
     int* max_stack;  // deepest accuracy-walk stack of the step
     int bucket, stack, warps;  // accuracy-walk shape: leaf bucket, stack entries, warps/block
+    int bpl;                   // accuracy walk: bodies per lane (1 or 2)
     int walk_grid_ref, walk_grid_acc;
 };
 
@@ -38,6 +40,7 @@ cudaError_t launch_walk(const StepArgs& a, cudaStream_t st, int part);
 cudaError_t init_walk_attributes();
 int normalized_bucket(int b);
 int normalized_stack(int s);
+int normalized_bpl(int b);
 int normalized_warps(int block);
 
 // Create a batch of independent systems of the given sizes (bh_create is the

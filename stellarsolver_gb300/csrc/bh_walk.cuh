@@ -47,7 +47,7 @@ struct Groups {
 };
 
 __device__ __forceinline__ void group_range(const Segs& segs, const Groups& gr, int g, int* lo,
-                                            int* hi, int* gstart) {
+                                            int* hi, int* gstart, int width = 32) {
     int s = 0;
     if (segs.nseg > 1) {
         int a = 0, b = segs.nseg;  // find s with gseg_off[s] <= g < gseg_off[s+1]
@@ -63,7 +63,7 @@ __device__ __forceinline__ void group_range(const Segs& segs, const Groups& gr, 
     *lo = segs.off[s];
     *hi = segs.off[s + 1];
     int g0 = segs.nseg > 1 ? __ldg(gr.gseg_off + s) : 0;
-    *gstart = *lo + 32 * (g - g0);
+    *gstart = *lo + width * (g - g0);
 }
 
 // ------------------------------------------------------------------ REFERENCE walk
@@ -332,6 +332,7 @@ __device__ __forceinline__ void unpair_cell(const CellPairs& cp, int e, float4& 
 struct AccShape {
     int stack;   // stack entries per warp
     int bucket;  // a node of <= bucket bodies is a leaf: its bodies interact directly
+    int bpl;     // bodies per lane: a warp walks for a group of 32 * bpl bodies (1 or 2)
 };
 
 // Per-warp shared memory of the accuracy walk (bytes, 16-byte aligned pieces):
@@ -341,7 +342,7 @@ __host__ __device__ __forceinline__ int acc_body_cap(int bucket) {
     return 32 + 32 * (bucket > 4 ? bucket : 4);
 }
 __host__ __device__ __forceinline__ int acc_warp_bytes(AccShape sh) {
-    return 3 * 32 * 16 + 32 * 8 + 16 + 64 * 4 + ((sh.stack * 4 + 15) & ~15) +
+    return 3 * 32 * 16 + 32 * 8 * sh.bpl + 16 + 64 * 4 + ((sh.stack * 4 + 15) & ~15) +
            ((acc_body_cap(sh.bucket) * 4 + 15) & ~15);
 }
 
@@ -359,8 +360,8 @@ constexpr int kSerialExactLanes = 8;
 // DIAG = diagnostics pass: the main rule, but each body's potential (FP64
 // accumulation of float batches, own body excluded) goes to pot[] and nothing
 // is integrated.
-template <bool MIXED, bool ESTIMATE, bool DIAG = false>
-__global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, Groups gr, WalkIn in,
+template <bool MIXED, bool ESTIMATE, bool DIAG = false, int BPL = 1>
+__global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape shape, Segs segs, Groups gr, WalkIn in,
                                                          const float4* __restrict__ recA,
                                                          const float4* __restrict__ recB,
                                                          const int4* __restrict__ recC,
@@ -372,6 +373,7 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
                                                          int* __restrict__ fresh,
                                                          int* __restrict__ max_stack,
                                                          double* __restrict__ pot = nullptr) {
+    static_assert(BPL == 1 || BPL == 2, "one or two bodies per lane");
     if (ESTIMATE) {
         if (*(volatile int*)fresh == 0) return;
     } else if (!DIAG && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -381,6 +383,7 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned lt = lanemask_lt();
     const int STACK = shape.stack, BUCKET = shape.bucket;
+    constexpr int GW = 32 * BPL;  // bodies per group
     unsigned char* wbase = smem_raw + (size_t)warp * acc_warp_bytes(shape);
     // 1536 bytes: 16 cell pairs (896), 16 body pairs (512), 128 spare
     CellPairs cpair;
@@ -391,26 +394,40 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
     float4* bxy = reinterpret_cast<float4*>(cpair.t11 + 16);
     float2* bm = reinterpret_cast<float2*>(bxy + 16);
     int2* bid = reinterpret_cast<int2*>(bm + 16);
-    float2* gp = reinterpret_cast<float2*>(wbase + 3 * 32 * 16);
-    float4* gext = reinterpret_cast<float4*>(gp + 32);  // y at min/max x, x at min/max y
+    float2* gp = reinterpret_cast<float2*>(wbase + 3 * 32 * 16);  // the group's GW positions
+    float4* gext = reinterpret_cast<float4*>(gp + GW);  // y at min/max x, x at min/max y
     int* clist = reinterpret_cast<int*>(gext + 1);
     int* stack = clist + 64;
     int* blist = stack + ((STACK + 3) & ~3);
     unsigned long long my_inter = 0, my_cinter = 0;
 
-    const int WARPS = blockDim.x >> 5;
-    (void)WARPS;
     for (int g = next_group(work); g < gr.ngroups; g = next_group(work)) {
         int lo, hi, gstart;
-        group_range(segs, gr, g, &lo, &hi, &gstart);
-        const int j = gstart + lane;
-        const bool valid = j < hi;
-        const int cnt = min(32, hi - gstart);
-        const int jj = valid ? j : gstart;  // invalid lanes mirror the group's first body
-        const float px = in.x[jj], py = in.y[jj];
+        group_range(segs, gr, g, &lo, &hi, &gstart, GW);
+        const int cnt = min(GW, hi - gstart);
+        // body b of this lane is position gstart + 32 b + lane; invalid ones
+        // mirror the group's first body
+        int j[BPL];
+        bool valid[BPL];
+        float px[BPL], py[BPL];
+#pragma unroll
+        for (int b = 0; b < BPL; ++b) {
+            j[b] = gstart + 32 * b + lane;
+            valid[b] = j[b] < hi;
+            const int jj = valid[b] ? j[b] : gstart;
+            px[b] = in.x[jj];
+            py[b] = in.y[jj];
+        }
         __syncwarp();
-        gp[lane] = make_float2(px, py);
-        float gx0 = px, gx1 = px, gy0 = py, gy1 = py;
+        float gx0 = px[0], gx1 = px[0], gy0 = py[0], gy1 = py[0];
+#pragma unroll
+        for (int b = 0; b < BPL; ++b) {
+            gp[32 * b + lane] = make_float2(px[b], py[b]);
+            gx0 = fminf(gx0, px[b]);
+            gx1 = fmaxf(gx1, px[b]);
+            gy0 = fminf(gy0, py[b]);
+            gy1 = fmaxf(gy1, py[b]);
+        }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             gx0 = fminf(gx0, __shfl_xor_sync(kFull, gx0, o));
@@ -422,17 +439,37 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
         {
             // the group's extreme bodies in x and y: the nearest of them bounds
             // the exact group distance from above
-            const float ya = __shfl_sync(kFull, py, __ffs(__ballot_sync(kFull, px == gx0)) - 1);
-            const float yb = __shfl_sync(kFull, py, __ffs(__ballot_sync(kFull, px == gx1)) - 1);
-            const float xa = __shfl_sync(kFull, px, __ffs(__ballot_sync(kFull, py == gy0)) - 1);
-            const float xb = __shfl_sync(kFull, px, __ffs(__ballot_sync(kFull, py == gy1)) - 1);
-            if (lane == 0) *gext = make_float4(ya, yb, xa, xb);
+            float ext[4];
+            const float key[4] = {gx0, gx1, gy0, gy1};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                float v = 0.0f;
+                bool found = false;
+#pragma unroll
+                for (int b = 0; b < BPL; ++b) {
+                    const float c = q < 2 ? px[b] : py[b];
+                    const float other = q < 2 ? py[b] : px[b];
+                    const unsigned hit = __ballot_sync(kFull, c == key[q]);
+                    const float w = __shfl_sync(kFull, other, __ffs(hit) - 1);
+                    if (!found && hit) {
+                        v = w;
+                        found = true;
+                    }
+                }
+                ext[q] = v;
+            }
+            if (lane == 0) *gext = make_float4(ext[0], ext[1], ext[2], ext[3]);
         }
         // relative-rule scale of the group
         float aa = __int_as_float(0x7f800000);
         if (!ESTIMATE && !DIAG && alpha > 0.0f) {
-            float a = in.amag[jj];
-            float amin = a, asum = valid ? a : 0.0f;
+            float amin = __int_as_float(0x7f800000), asum = 0.0f;
+#pragma unroll
+            for (int b = 0; b < BPL; ++b) {
+                const float a = in.amag[valid[b] ? j[b] : gstart];
+                amin = fminf(amin, a);
+                asum += valid[b] ? a : 0.0f;
+            }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 amin = fminf(amin, __shfl_xor_sync(kFull, amin, o));
@@ -440,9 +477,11 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
             }
             aa = alpha * fmaxf(amin, 0.1f * asum / (float)cnt);
         }
-        float ax = 0.0f, ay = 0.0f;     // running sums
-        float cax = 0.0f, cay = 0.0f;   // Kahan compensation (MIXED)
-        double phi = 0.0;               // DIAG: potential
+        float ax[BPL], ay[BPL];    // running sums
+        float cax[BPL], cay[BPL];  // Kahan compensation (MIXED)
+        double phi[BPL];           // DIAG: potential
+#pragma unroll
+        for (int b = 0; b < BPL; ++b) ax[b] = ay[b] = cax[b] = cay[b] = 0.0f, phi[b] = 0.0;
         long long entries = 0, centries = 0;
         bool overflow = false;
         int top = 0, ccnt = 0, bcnt = 0, peak = 0, rounds = 0, tested = 0;
@@ -450,21 +489,26 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
             if (lane == 0) stack[0] = lo;
             top = 1;
         }
-        auto add_batch = [&](float bx, float by) {
+        auto add_batch = [&](int b, float bx, float by) {
             if (MIXED) {
-                float yx = bx - cax, tx = ax + yx;
-                cax = (tx - ax) - yx;
-                ax = tx;
-                float yy = by - cay, ty = ay + yy;
-                cay = (ty - ay) - yy;
-                ay = ty;
+                float yx = bx - cax[b], tx = ax[b] + yx;
+                cax[b] = (tx - ax[b]) - yx;
+                ax[b] = tx;
+                float yy = by - cay[b], ty = ay[b] + yy;
+                cay[b] = (ty - ay[b]) - yy;
+                ay[b] = ty;
             } else {
-                ax += bx;
-                ay += by;
+                ax[b] += bx;
+                ay[b] += by;
             }
         };
-        // packed-pair constants of this lane's body
-        const float2 npx = make_float2(-px, -px), npy = make_float2(-py, -py);
+        // packed-pair constants of this lane's bodies
+        float2 npx[BPL], npy[BPL];
+#pragma unroll
+        for (int b = 0; b < BPL; ++b) {
+            npx[b] = make_float2(-px[b], -px[b]);
+            npy[b] = make_float2(-py[b], -py[b]);
+        }
         const float2 e2v = make_float2(eps2, eps2);
         auto flush_cells = [&](int k) {  // the last k entries of clist
             __syncwarp();
@@ -481,47 +525,70 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
                 reinterpret_cast<float*>(cpair.t11 + q)[h] = -B.z;
             }
             __syncwarp();
-            float bx = 0.0f, by = 0.0f;
             if (DIAG) {
-                float f = 0.0f;
+                float f[BPL];
+#pragma unroll
+                for (int b = 0; b < BPL; ++b) f[b] = 0.0f;
                 for (int e = 0; e < k; ++e) {
                     float4 A, B;
                     unpair_cell(cpair, e, A, B);
-                    f += pot_cell(A, B, px, py, eps2);
+#pragma unroll
+                    for (int b = 0; b < BPL; ++b) f[b] += pot_cell(A, B, px[b], py[b], eps2);
                 }
-                phi += (double)f;
+#pragma unroll
+                for (int b = 0; b < BPL; ++b) phi[b] += (double)f[b];
             } else {
-                float2 sx = make_float2(0.0f, 0.0f), sy = make_float2(0.0f, 0.0f);
+                float bx[BPL], by[BPL];
+                float2 sx[BPL], sy[BPL];
+#pragma unroll
+                for (int b = 0; b < BPL; ++b) {
+                    bx[b] = by[b] = 0.0f;
+                    sx[b] = sy[b] = make_float2(0.0f, 0.0f);
+                }
                 if (ESTIMATE) {
                     // the bootstrap needs |a| to a few per cent: monopoles suffice
                     for (int e = 0; e < (k >> 1); ++e) {
                         const float4 mh = cpair.mh[e];
-                        p2p_pair(cpair.xy[e], make_float2(mh.x, mh.y), npx, npy, e2v, sx, sy);
+                        const float4 xy = cpair.xy[e];
+#pragma unroll
+                        for (int b = 0; b < BPL; ++b)
+                            p2p_pair(xy, make_float2(mh.x, mh.y), npx[b], npy[b], e2v, sx[b], sy[b]);
                     }
                     if (k & 1) {
                         float4 A, B;
                         unpair_cell(cpair, k - 1, A, B);
-                        p2p<false>(A.x, A.y, A.z, px, py, eps2, bx, by);
+#pragma unroll
+                        for (int b = 0; b < BPL; ++b)
+                            p2p<false>(A.x, A.y, A.z, px[b], py[b], eps2, bx[b], by[b]);
                     }
                 } else if (k == 32) {
 #pragma unroll 4
-                    for (int e = 0; e < 16; ++e)
-                        p2m_pair(cpair.xy[e], cpair.mh[e], cpair.t01[e], cpair.t11[e], npx, npy,
-                                 e2v, sx, sy);
+                    for (int e = 0; e < 16; ++e) {
+                        const float4 xy = cpair.xy[e], mh = cpair.mh[e], t01 = cpair.t01[e];
+                        const float2 t11 = cpair.t11[e];
+#pragma unroll
+                        for (int b = 0; b < BPL; ++b)
+                            p2m_pair(xy, mh, t01, t11, npx[b], npy[b], e2v, sx[b], sy[b]);
+                    }
                 } else {
-                    for (int e = 0; e < (k >> 1); ++e)
-                        p2m_pair(cpair.xy[e], cpair.mh[e], cpair.t01[e], cpair.t11[e], npx, npy,
-                                 e2v, sx, sy);
+                    for (int e = 0; e < (k >> 1); ++e) {
+                        const float4 xy = cpair.xy[e], mh = cpair.mh[e], t01 = cpair.t01[e];
+                        const float2 t11 = cpair.t11[e];
+#pragma unroll
+                        for (int b = 0; b < BPL; ++b)
+                            p2m_pair(xy, mh, t01, t11, npx[b], npy[b], e2v, sx[b], sy[b]);
+                    }
                     if (k & 1) {
                         float4 A, B;
                         unpair_cell(cpair, k - 1, A, B);
-                        p2m(A, B, px, py, eps2, bx, by);
+#pragma unroll
+                        for (int b = 0; b < BPL; ++b) p2m(A, B, px[b], py[b], eps2, bx[b], by[b]);
                     }
                 }
-                bx += sx.x + sx.y;
-                by += sy.x + sy.y;
+#pragma unroll
+                for (int b = 0; b < BPL; ++b)
+                    add_batch(b, bx[b] + (sx[b].x + sx[b].y), by[b] + (sy[b].x + sy[b].y));
             }
-            add_batch(bx, by);
             ccnt -= k;
             entries += k;
             centries += k;
@@ -529,15 +596,14 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
         auto flush_bodies = [&](int k) {
             __syncwarp();
             if (lane < k) {
-                const int b = blist[bcnt - k + lane];
+                const int bi = blist[bcnt - k + lane];
                 const int pi = lane >> 1, h = lane & 1;
-                reinterpret_cast<float*>(&bxy[pi])[h] = in.x[b];
-                reinterpret_cast<float*>(&bxy[pi])[2 + h] = in.y[b];
-                reinterpret_cast<float*>(&bm[pi])[h] = in.m[b];
-                reinterpret_cast<int*>(&bid[pi])[h] = b;
+                reinterpret_cast<float*>(&bxy[pi])[h] = in.x[bi];
+                reinterpret_cast<float*>(&bxy[pi])[2 + h] = in.y[bi];
+                reinterpret_cast<float*>(&bm[pi])[h] = in.m[bi];
+                reinterpret_cast<int*>(&bid[pi])[h] = bi;
             }
             __syncwarp();
-            float bx = 0.0f, by = 0.0f;
             // entry e of the staged bodies, unpaired
             auto body = [&](int e, float& x, float& y, float& m) {
                 const float4 q = bxy[e >> 1];
@@ -547,39 +613,70 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
                 m = (e & 1) ? w.y : w.x;
             };
             if (DIAG) {
-                float f = 0.0f;
+                float f[BPL];
+#pragma unroll
+                for (int b = 0; b < BPL; ++b) f[b] = 0.0f;
                 for (int e = 0; e < k; ++e) {
                     const int2 ids = bid[e >> 1];
-                    if (((e & 1) ? ids.y : ids.x) == j) continue;  // own body
+                    const int who = (e & 1) ? ids.y : ids.x;
                     float x, y, m;
                     body(e, x, y, m);
-                    const float dx = x - px, dy = y - py;
-                    f -= m * rsqrtf(fmaf(dx, dx, fmaf(dy, dy, eps2)));
-                }
-                phi += (double)f;
-            } else if (eps2 > 0.0f) {
-                float2 sx = make_float2(0.0f, 0.0f), sy = make_float2(0.0f, 0.0f);
-                if (k == 32) {
-#pragma unroll 4
-                    for (int e = 0; e < 16; ++e) p2p_pair(bxy[e], bm[e], npx, npy, e2v, sx, sy);
-                } else {
-                    for (int e = 0; e < (k >> 1); ++e) p2p_pair(bxy[e], bm[e], npx, npy, e2v, sx, sy);
-                    if (k & 1) {
-                        float x, y, m;
-                        body(k - 1, x, y, m);
-                        p2p<false>(x, y, m, px, py, eps2, bx, by);
+#pragma unroll
+                    for (int b = 0; b < BPL; ++b) {
+                        if (who == j[b]) continue;  // own body
+                        const float dx = x - px[b], dy = y - py[b];
+                        f[b] -= m * rsqrtf(fmaf(dx, dx, fmaf(dy, dy, eps2)));
                     }
                 }
-                bx += sx.x + sx.y;
-                by += sy.x + sy.y;
+#pragma unroll
+                for (int b = 0; b < BPL; ++b) phi[b] += (double)f[b];
             } else {
-                for (int e = 0; e < k; ++e) {
-                    float x, y, m;
-                    body(e, x, y, m);
-                    p2p<true>(x, y, m, px, py, eps2, bx, by);
+                float bx[BPL], by[BPL];
+                float2 sx[BPL], sy[BPL];
+#pragma unroll
+                for (int b = 0; b < BPL; ++b) {
+                    bx[b] = by[b] = 0.0f;
+                    sx[b] = sy[b] = make_float2(0.0f, 0.0f);
                 }
+                if (eps2 > 0.0f) {
+                    if (k == 32) {
+#pragma unroll 4
+                        for (int e = 0; e < 16; ++e) {
+                            const float4 xy = bxy[e];
+                            const float2 w = bm[e];
+#pragma unroll
+                            for (int b = 0; b < BPL; ++b)
+                                p2p_pair(xy, w, npx[b], npy[b], e2v, sx[b], sy[b]);
+                        }
+                    } else {
+                        for (int e = 0; e < (k >> 1); ++e) {
+                            const float4 xy = bxy[e];
+                            const float2 w = bm[e];
+#pragma unroll
+                            for (int b = 0; b < BPL; ++b)
+                                p2p_pair(xy, w, npx[b], npy[b], e2v, sx[b], sy[b]);
+                        }
+                        if (k & 1) {
+                            float x, y, m;
+                            body(k - 1, x, y, m);
+#pragma unroll
+                            for (int b = 0; b < BPL; ++b)
+                                p2p<false>(x, y, m, px[b], py[b], eps2, bx[b], by[b]);
+                        }
+                    }
+                } else {
+                    for (int e = 0; e < k; ++e) {
+                        float x, y, m;
+                        body(e, x, y, m);
+#pragma unroll
+                        for (int b = 0; b < BPL; ++b)
+                            p2p<true>(x, y, m, px[b], py[b], eps2, bx[b], by[b]);
+                    }
+                }
+#pragma unroll
+                for (int b = 0; b < BPL; ++b)
+                    add_batch(b, bx[b] + (sx[b].x + sx[b].y), by[b] + (sy[b].x + sy[b].y));
             }
-            add_batch(bx, by);
             bcnt -= k;
             entries += k;
         };
@@ -604,9 +701,9 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
             int cat = -1;  // 0 approximate, 1 leaf bodies, 2 open
             int4 D = make_int4(0, 0, 0, 0);
             // Distance from the node's centre of mass to the group's bodies:
-            // the group box gives a lower bound; the exact minimum over the 32
-            // bodies is needed only when the box test is inconclusive, i.e.
-            // d_box <= ropen < d_box + box diagonal, for some lane.
+            // the group box gives a lower bound; the exact minimum over the
+            // group's bodies is needed only when the box test is inconclusive,
+            // i.e. d_box <= ropen < d_box + box diagonal, for some lane.
             float4 A = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             float d2 = 0.0f;
             bool need = false;
@@ -646,7 +743,7 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
                 if (__popc(nm) > kSerialExactLanes) {
                     float e2 = __int_as_float(0x7f800000);
 #pragma unroll 8
-                    for (int e = 0; e < 32; ++e) {
+                    for (int e = 0; e < GW; ++e) {
                         float2 q = gp[e];
                         float dx = q.x - A.x, dy = q.y - A.y;
                         e2 = fminf(e2, fmaf(dx, dx, dy * dy));
@@ -656,9 +753,14 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
                     while (nm) {
                         const int src = __ffs(nm) - 1;
                         nm &= nm - 1;
-                        const float dx = px - __shfl_sync(kFull, A.x, src);
-                        const float dy = py - __shfl_sync(kFull, A.y, src);
-                        float e2 = fmaf(dx, dx, dy * dy);
+                        const float cx = __shfl_sync(kFull, A.x, src);
+                        const float cy = __shfl_sync(kFull, A.y, src);
+                        float e2 = __int_as_float(0x7f800000);
+#pragma unroll
+                        for (int b = 0; b < BPL; ++b) {
+                            const float dx = px[b] - cx, dy = py[b] - cy;
+                            e2 = fminf(e2, fmaf(dx, dx, dy * dy));
+                        }
 #pragma unroll
                         for (int o = 16; o > 0; o >>= 1) e2 = fminf(e2, __shfl_xor_sync(kFull, e2, o));
                         if (lane == src) d2 = e2;
@@ -719,48 +821,53 @@ __global__ void __launch_bounds__(256, 4) k_walk_acc(AccShape shape, Segs segs, 
                 atomicAdd(max_stack + 2, tested);
             }
         }
-        const float gax = G * (MIXED ? ax - cax : ax);
-        const float gay = G * (MIXED ? ay - cay : ay);
-        if (DIAG) {
-            if (valid) pot[j] = (double)G * phi;
-            continue;
+        if (!ESTIMATE && !DIAG) {
+            my_inter += (unsigned long long)(entries * cnt);
+            my_cinter += (unsigned long long)(centries * cnt);
         }
-        if (ESTIMATE) {
-            if (valid) in.amag[j] = sqrtf(gax * gax + gay * gay);
-            continue;
-        }
-        my_inter += (unsigned long long)(entries * cnt);
-        my_cinter += (unsigned long long)(centries * cnt);
-        if (valid) {
-            float vx = fmaf(dt, gax, in.vx[j]);
-            float vy = fmaf(dt, gay, in.vy[j]);
+#pragma unroll
+        for (int b = 0; b < BPL; ++b) {
+            if (!valid[b]) continue;
+            const int jb = j[b];
+            const float gax = G * (MIXED ? ax[b] - cax[b] : ax[b]);
+            const float gay = G * (MIXED ? ay[b] - cay[b] : ay[b]);
+            if (DIAG) {
+                pot[jb] = (double)G * phi[b];
+                continue;
+            }
+            if (ESTIMATE) {
+                in.amag[jb] = sqrtf(gax * gax + gay * gay);
+                continue;
+            }
+            float vx = fmaf(dt, gax, in.vx[jb]);
+            float vy = fmaf(dt, gay, in.vy[jb]);
             if (MIXED) {
                 // x_hi + x_lo += d*dt*v with an error-free sum (TwoSum), renormalised
-                float inc = ddt * vx, hx = px, s = hx + inc, bb = s - hx;
+                float inc = ddt * vx, hx = px[b], s = hx + inc, bb = s - hx;
                 float e = (hx - (s - bb)) + (inc - bb);
-                float lo2 = in.xlo[j] + e, h2 = s + lo2;
-                out.x[j] = h2;
-                out.xlo[j] = lo2 - (h2 - s);
+                float lo2 = in.xlo[jb] + e, h2 = s + lo2;
+                out.x[jb] = h2;
+                out.xlo[jb] = lo2 - (h2 - s);
                 inc = ddt * vy;
-                hx = py;
+                hx = py[b];
                 s = hx + inc;
                 bb = s - hx;
                 e = (hx - (s - bb)) + (inc - bb);
-                lo2 = in.ylo[j] + e;
+                lo2 = in.ylo[jb] + e;
                 h2 = s + lo2;
-                out.y[j] = h2;
-                out.ylo[j] = lo2 - (h2 - s);
+                out.y[jb] = h2;
+                out.ylo[jb] = lo2 - (h2 - s);
             } else {
-                out.x[j] = fmaf(ddt, vx, px);
-                out.y[j] = fmaf(ddt, vy, py);
+                out.x[jb] = fmaf(ddt, vx, px[b]);
+                out.y[jb] = fmaf(ddt, vy, py[b]);
             }
-            out.vx[j] = vx;
-            out.vy[j] = vy;
-            out.m[j] = in.m[j];
-            out.id[j] = in.id[j];
-            out.ax[j] = gax;
-            out.ay[j] = gay;
-            out.amag[j] = sqrtf(gax * gax + gay * gay);
+            out.vx[jb] = vx;
+            out.vy[jb] = vy;
+            out.m[jb] = in.m[jb];
+            out.id[jb] = in.id[jb];
+            out.ax[jb] = gax;
+            out.ay[jb] = gay;
+            out.amag[jb] = sqrtf(gax * gax + gay * gay);
         }
     }
     if (!ESTIMATE && !DIAG && lane == 0 && my_inter) {

@@ -11,6 +11,8 @@ once unless the state was just set, and the main k_walk_acc).
 """
 import argparse
 
+import numpy as np
+
 from . import bh, models
 
 
@@ -21,6 +23,11 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=1)
     ap.add_argument("--bucket", type=int, default=0)
+    ap.add_argument("--bpl", type=int, default=0, help="bodies per lane of the accuracy walk")
+    ap.add_argument("--block", type=int, default=0, help="walk threads per block")
+    ap.add_argument("--phases", action="store_true", help="also print event-timed phase ms")
+    ap.add_argument("--error", action="store_true",
+                    help="also print the force error against the FP64 direct sum (4096 bodies)")
     ap.add_argument("--graph", action="store_true")
     ap.add_argument("--model", default="plummer", choices=["plummer", "disk", "colliding"])
     a = ap.parse_args()
@@ -31,8 +38,17 @@ def main():
     else:
         x, y, vx, vy, m = models.colliding_disks(a.n, models.SEED_BASE + 2)
     with bh.BarnesHutSystem(a.n, mode=a.mode, theta=0.5, eps2=1e-4, timestep=1e-4,
-                            leaf_bucket=a.bucket, use_graph=a.graph) as s:
+                            leaf_bucket=a.bucket, use_graph=a.graph, bodies_per_lane=a.bpl,
+                            block_size=a.block) as s:
         s.set_state(x, y, vx, vy, m)
+        if a.error:
+            idx = np.sort(np.random.default_rng(7).choice(a.n, size=min(4096, a.n),
+                                                          replace=False)).astype(np.int32)
+            rx, ry = s.direct_sum_f64(idx)
+            s.step(1)
+            ax, ay = s.get_accel()
+            rel = np.hypot(ax[idx] - rx, ay[idx] - ry) / np.hypot(rx, ry)
+            print(f"force error vs FP64: rms {np.sqrt(np.mean(rel ** 2)):.4e} max {rel.max():.4e}")
         for _ in range(a.warmup):
             s.step(1)
             s.sync()
@@ -40,6 +56,11 @@ def main():
             s.step(1)
             s.sync()
         st = s.stats()
+        if a.phases:
+            ms = np.zeros(bh.PHASES_N, np.float32)
+            for _ in range(5):
+                s.step_profiled(ms)
+            print("phases ms:", {k: round(float(v) / 5, 4) for k, v in zip(bh.PHASES, ms)})
     print(f"profile_step n={a.n} mode={a.mode} steps={a.steps} interactions={st['interactions']} "
           f"status={st['status']} max_stack={st['max_stack']} nodes={st['nodes']} "
           f"rounds={st['walk_rounds']} tested={st['nodes_tested']}")

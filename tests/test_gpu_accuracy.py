@@ -40,13 +40,14 @@ def run(bh, x, y, vx, vy, m, steps=1, **kw):
 
 @pytest.mark.parametrize("mode", ["plain", "mixed"])
 @pytest.mark.parametrize("bucket", [1, 4, 8, 16])
-def test_plummer_2e17_error_bound(bh, oracle, mode, bucket):
+@pytest.mark.parametrize("bpl", [1, 2])
+def test_plummer_2e17_error_bound(bh, oracle, mode, bucket, bpl):
     from stellarsolver_gb300 import models
 
     x, y, vx, vy, m = models.plummer(1 << 17, 0x5EED2000)
     eps2 = 1e-4
     ax, ay, _, stats = run(bh, x, y, vx, vy, m, mode=mode, theta=0.5, eps2=eps2, timestep=0.0,
-                           leaf_bucket=bucket)
+                           leaf_bucket=bucket, bodies_per_lane=bpl)
     rms, mx = force_error(oracle, x, y, m, ax, ay, eps2)
     assert stats["status"] == 0
     assert rms <= 1e-3, (rms, mx)
@@ -117,7 +118,8 @@ def test_momentum_nearly_conserved(bh):
     assert np.abs(p1 - p0).max() <= 1e-4 * scale
 
 
-def test_walk_matches_cpu_restatement(bh, oracle):
+@pytest.mark.parametrize("bpl", [1, 2])
+def test_walk_matches_cpu_restatement(bh, oracle, bpl):
     """The GPU PLAIN walk against oracle.walk_acc (same tree, same rule: the
     bootstrap pass at opening angle 1 with monopole cells, then the relative
     rule with alpha = 0.01).  Moments are
@@ -128,7 +130,8 @@ def test_walk_matches_cpu_restatement(bh, oracle):
     n = 1 << 16
     x, y, vx, vy, m = models.plummer(n, 0x5EED3000)
     eps2 = 1e-4
-    with bh.BarnesHutSystem(n, mode="plain", theta=0.5, eps2=eps2, timestep=0.0) as s:
+    with bh.BarnesHutSystem(n, mode="plain", theta=0.5, eps2=eps2, timestep=0.0,
+                            bodies_per_lane=bpl) as s:
         s.set_state(x, y, vx, vy, m)
         s.step(1)
         s.sync()
@@ -142,9 +145,10 @@ def test_walk_matches_cpu_restatement(bh, oracle):
     sk = k[operm]
     t = oracle.Tree(sk)
     sx, sy, sm = x[operm], y[operm], m[operm]
-    a0x, a0y, _ = oracle.walk_acc(sx, sy, sm, sk, t, box, 1.0, eps2, quadrupole=False)  # bootstrap
+    a0x, a0y, _ = oracle.walk_acc(sx, sy, sm, sk, t, box, 1.0, eps2, quadrupole=False,
+                                  group=32 * bpl)  # bootstrap
     ox, oy, ointer = oracle.walk_acc(sx, sy, sm, sk, t, box, 0.5, eps2, alpha=0.01,
-                                     aold=np.hypot(a0x, a0y))
+                                     aold=np.hypot(a0x, a0y), group=32 * bpl)
     gx, gy = acc[:n], acc[n:]
     rms = np.sqrt(np.mean(ox.astype(np.float64) ** 2 + oy.astype(np.float64) ** 2))
     d = np.hypot(gx - ox, gy - oy)

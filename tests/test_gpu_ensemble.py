@@ -24,11 +24,12 @@ def _systems(sizes):
     return models.ensemble(sizes)
 
 
-@pytest.mark.parametrize("mode", ["reference", "mixed"])
-def test_batch_equals_systems_alone(bh, mode):
-    sizes = [1000, 33, 4096, 1, 2, 777, 20000, 64]
+@pytest.mark.parametrize("mode,bpl", [("reference", 0), ("mixed", 1), ("mixed", 2)])
+def test_batch_equals_systems_alone(bh, mode, bpl):
+    sizes = [1000, 33, 4096, 1, 2, 777, 20000, 64, 65, 95]
     systems = _systems(sizes)
-    kw = dict(mode=mode, theta=0.5, eps2=0.01 if mode == "reference" else 1e-3, timestep=1e-3)
+    kw = dict(mode=mode, theta=0.5, eps2=0.01 if mode == "reference" else 1e-3, timestep=1e-3,
+              bodies_per_lane=bpl)
     cat = [np.concatenate([s[k] for s in systems]) for k in range(5)]
     with bh.BarnesHutSystem(sizes=sizes, **kw) as b:
         assert b.num_systems == len(sizes)
