@@ -105,9 +105,14 @@ static cudaError_t launch_acc(const StepArgs& a, cudaStream_t st, int part) {
     int grid = std::min(a.walk_grid_acc, (gr.ngroups + warps - 1) / warps);
     if (grid < 1) grid = 1;
     if (part == 0) {
-        // bootstrap pass: exits at once unless bh_set_state left the state fresh
-        k_walk_acc<false, true, false, BPL><<<grid, warps * 32, smem, st>>>(
-            sh, a.segs, gr, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt,
+        // bootstrap pass: exits at once unless bh_set_state left the state fresh.  Always
+        // 64-body groups: its cost is the traversal, which they halve per body.
+        const AccShape sb{a.stack, a.bucket, 2};
+        const size_t smb = (size_t)warps * acc_warp_bytes(sb);
+        int gb = std::min(a.walk_grid_acc, (a.groups2.ngroups + warps - 1) / warps);
+        if (gb < 1) gb = 1;
+        k_walk_acc<false, true, false, 2><<<gb, warps * 32, smb, st>>>(
+            sb, a.segs, a.groups2, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt,
             a.alpha, a.out, a.status, a.inter, a.work + 1, a.fresh, a.max_stack);
     } else {
         k_walk_acc<MIXED, false, false, BPL><<<grid, warps * 32, smem, st>>>(

@@ -353,8 +353,8 @@ constexpr int kSerialExactLanes = 8;
 
 // PLAIN / MIXED walk.  ESTIMATE = the bootstrap pass after bh_set_state: the
 // geometric rule only, at opening angle max(theta, kBootstrapTheta) (radius
-// in recD.w), cells as monopoles; writes |G a| into in.amag and nothing else
-// (skipped unless *fresh is set).  The main pass also applies the relative rule
+// in recD.w), cells as monopoles, launched with 64-body groups; writes |G a|
+// into in.amag and nothing else (skipped unless *fresh is set).  The main pass also applies the relative rule
 //   G M l^3 <= alpha * a_g * d^5,  a_g = max(min |a_old|, 0.1 mean |a_old|) over the group,
 // d = min over the group's bodies of |COM - p|; the geometric rule is d > l/theta + delta.
 // DIAG = diagnostics pass: the main rule, but each body's potential (FP64
