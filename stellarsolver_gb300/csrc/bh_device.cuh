@@ -385,7 +385,8 @@ __device__ __forceinline__ int kdelta(const uint64_t* __restrict__ k, int i, int
 
 struct TreePtrs {
     int *left, *right, *parent, *leaf_parent, *split, *first, *last;
-    int4* climb;  // per internal node: left, right, parent, range inside one moments block
+    int4* climb;  // per internal node: left, right, parent, w = (split << 1) | inside one
+                  // moments block
 };
 
 // k_moments runs one thread per leaf in blocks of kMomentsThreads; a node whose
@@ -461,7 +462,7 @@ static __global__ void k_build(const uint64_t* __restrict__ k, int n, Segs segs,
     // .z (parent) is written by the parent's thread
     t.climb[i].x = lc;
     t.climb[i].y = rc;
-    t.climb[i].w = (a >> kMomentsLog2) == (b >> kMomentsLog2);
+    t.climb[i].w = (dnode << 1) | ((a >> kMomentsLog2) == (b >> kMomentsLog2) ? 1 : 0);
 }
 
 // ------------------------------------------------------------------ (c) moments
@@ -591,7 +592,7 @@ static __global__ void __launch_bounds__(kMomentsThreads) k_moments(int n, int a
         }
         int4 TN = make_int4(0, 0, -1, 0);
         if (T.z >= 0) TN = climb[T.z];
-        if (T.w) {
+        if (T.w & 1) {
             __threadfence_block();
             if (atomicAdd(s_cnt + (p - c0), 1) == 0) return;
             __threadfence_block();
@@ -647,28 +648,30 @@ __device__ __forceinline__ float ref_dp(Box bx, float theta, int level) {
 }
 
 
-// Walk record of branching node i, from its sums and the tree (the body of
-// k_records).
 // Opening angle of the bootstrap pass (|a| estimate after bh_set_state, cells
 // as monopoles).  At 1.0 its |a| is within a few per cent and it costs about a
 // third of the theta = 0.5 walk; the relative rule it feeds opens the same
 // nodes as with exact |a| to within 1%.
 constexpr float kBootstrapTheta = 1.0f;
 
-__device__ __forceinline__ void emit_record(int i, int sp, int accuracy, float theta, float G,
-                                            const int* __restrict__ box_ord, int seg,
+// Walk record of branching node i, from its sums and the tree (the body of
+// k_records).
+__device__ __forceinline__ void emit_record(int i, int sp, int4 T, int accuracy, float theta,
+                                            float G, const int* __restrict__ box_ord, int seg,
                                             const uint64_t* __restrict__ skeys,
                                             const TreePtrs& t, float M, float cx, float cy,
                                             float4 quad, Records rec) {
     int ch[4] = {kNoChild, kNoChild, kNoChild, kNoChild};
     int nc = 0;
-    const int lr[2] = {t.left[i], t.right[i]};
+    const int lr[2] = {T.x, T.y};
 #pragma unroll
     for (int s2 = 0; s2 < 2; ++s2) {
         const int c = lr[s2];
-        if (c >= 0 && merged_into(t.split[c], sp)) {
-            ch[nc++] = t.left[c];
-            ch[nc++] = t.right[c];
+        int4 Tc = make_int4(0, 0, 0, 0);
+        if (c >= 0) Tc = t.climb[c];
+        if (c >= 0 && merged_into(Tc.w >> 1, sp)) {
+            ch[nc++] = Tc.x;
+            ch[nc++] = Tc.y;
         } else {
             ch[nc++] = c;
         }
@@ -690,10 +693,12 @@ __device__ __forceinline__ void emit_record(int i, int sp, int accuracy, float t
     const float scale = ldexpf(1.0f, -L);
     const float wx = bx.r - bx.l, wy = bx.t - bx.b;
     const float l = fmaxf(wx, wy) * scale;
-    const double hs = 0.5 * (double)scale;
-    const double ddx = (double)cx - ((double)bx.l + (double)wx * ((double)ix * (double)scale + hs));
-    const double ddy = (double)cy - ((double)bx.b + (double)wy * ((double)iy * (double)scale + hs));
-    const float delta = sqrtf((float)(ddx * ddx + ddy * ddy));
+    // cell centre in FP32: exact in ix, iy up to level 23, then within an ulp of
+    // the box width, as precise as the centre of mass it is compared with
+    const float ccx = fmaf(wx, ((float)ix + 0.5f) * scale, bx.l);
+    const float ccy = fmaf(wy, ((float)iy + 0.5f) * scale, bx.b);
+    const float ddx = cx - ccx, ddy = cy - ccy;
+    const float delta = sqrtf(fmaf(ddx, ddx, ddy * ddy));
     const float r = l / theta + delta;
     rec.A[i] = make_float4(cx, cy, M, r * r);
     const float qerr = G * M * l * l * l;
@@ -703,6 +708,9 @@ __device__ __forceinline__ void emit_record(int i, int sp, int accuracy, float t
     rec.B[i] = make_float4(3.0f * quad.x, 3.0f * quad.y, 3.0f * quad.z, 1.5f * (quad.x + quad.z));
 }
 
+// One thread per node: the walk record of every branching node (binary nodes
+// folded into their parent emit nothing).  Topology comes from the climb
+// records: one 16-byte load per node, its parent and its children.
 static __global__ void k_records(int n, Segs segs, int accuracy, float theta, float G,
                                  const int* __restrict__ box_ord, const uint64_t* __restrict__ skeys,
                                  TreePtrs t, NodeSums ns, Records rec) {
@@ -710,11 +718,11 @@ static __global__ void k_records(int n, Segs segs, int accuracy, float theta, fl
     if (i >= n) return;
     const int sp = t.split[i];
     if (sp < 0) return;  // unused slot
-    const int pa = t.parent[i];
-    if (pa >= 0 && merged_into(sp, t.split[pa])) return;  // folded into its parent
+    const int4 T = t.climb[i];
+    if (T.z >= 0 && merged_into(sp, t.climb[T.z].w >> 1)) return;  // folded into its parent
     const float4 a = ns.s0[i], b = ns.s1[i];
     const float4 q = accuracy ? make_float4(b.y, b.z, b.w, 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
-    emit_record(i, sp, accuracy, theta, G, box_ord, seg_of(segs, i), skeys, t, a.x, a.w, b.x, q,
+    emit_record(i, sp, T, accuracy, theta, G, box_ord, seg_of(segs, i), skeys, t, a.x, a.w, b.x, q,
                 rec);
 }
 
