@@ -40,6 +40,11 @@ __device__ __forceinline__ int f2ord(float f) {
 }
 __device__ __forceinline__ float ord2f(int i) { return __int_as_float(i >= 0 ? i : (i ^ 0x7fffffff)); }
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialisation may start while its predecessor drains; this waits until the
+// predecessor's writes are visible.  A no-op for an ordinary launch.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 __device__ __forceinline__ unsigned lanemask_lt() {
     unsigned m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -106,6 +111,7 @@ static __global__ void __launch_bounds__(THREADS) k_bbox(const float* __restrict
                                                   const int* __restrict__ chunk_begin,
                                                   const int* __restrict__ chunk_end,
                                                   int* __restrict__ box_ord, int* __restrict__ status) {
+    pdl_wait();
     const int c = blockIdx.x;
     const int seg = chunk_seg[c], beg = chunk_begin[c], end = chunk_end[c];
     float l = 0.0f, r = 0.0f, b = 0.0f, t = 0.0f;
@@ -195,6 +201,7 @@ __device__ __forceinline__ uint64_t quad_key(float px, float py, Box bx) {
 static __global__ void k_keys(const float* __restrict__ x, const float* __restrict__ y, int n, Segs segs,
                        const int* __restrict__ box_ord, uint64_t* __restrict__ keys,
                        uint32_t* __restrict__ vals) {
+    pdl_wait();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     Box bx = load_box(box_ord, seg_of(segs, i));
@@ -225,6 +232,7 @@ static __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint64
                                                              int shift, int use_seg,
                                                              const int* __restrict__ seg_of_pos,
                                                              uint32_t* __restrict__ hist, int tiles) {
+    pdl_wait();
     constexpr int W = kSortThreads / 32;
     __shared__ uint32_t s_h[W][256];
     for (int i = threadIdx.x; i < W * 256; i += kSortThreads) (&s_h[0][0])[i] = 0u;
@@ -252,6 +260,7 @@ static __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint64
 // block d turns column d of hist into exclusive offsets; totals[d] = column sum
 static __global__ void __launch_bounds__(kSortThreads) k_radix_scan(uint32_t* __restrict__ hist, int tiles,
                                                              uint32_t* __restrict__ totals) {
+    pdl_wait();
     __shared__ uint32_t s_tmp[kSortThreads / 32];
     uint32_t* col = hist + (size_t)blockIdx.x * tiles;
     uint32_t running = 0;
@@ -274,6 +283,7 @@ static __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(
     const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
     uint32_t* __restrict__ vout, int n, int shift, int use_seg, const int* __restrict__ seg_of_pos,
     const uint32_t* __restrict__ hist, const uint32_t* __restrict__ totals, int tiles) {
+    pdl_wait();
     constexpr int W = kSortThreads / 32;
     constexpr int WCHUNK = 32 * kSortItems;
     __shared__ uint32_t s_wh[W][256];
@@ -357,6 +367,7 @@ struct BodyPtrs {
 };
 
 static __global__ void k_gather(int n, const uint32_t* __restrict__ perm, BodyPtrs src, BodyPtrs dst) {
+    pdl_wait();
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     uint32_t i = perm[j];
@@ -398,6 +409,7 @@ constexpr int kMomentsThreads = 1 << kMomentsLog2;
 // Karras (2012) radix-tree construction, one thread per internal node.
 static __global__ void k_build(const uint64_t* __restrict__ k, int n, Segs segs, TreePtrs t,
                         int* __restrict__ status) {
+    pdl_wait();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int s = seg_of(segs, i);
@@ -573,6 +585,7 @@ static __global__ void __launch_bounds__(kMomentsThreads) k_moments(int n, int a
                                                      const int* __restrict__ leaf_parent,
                                                      int* __restrict__ counter, NodeSums ns,
                                                      int* __restrict__ status) {
+    pdl_wait();
     __shared__ int s_cnt[kMomentsThreads];
     const int c0 = blockIdx.x * kMomentsThreads;  // this block's leaves: [c0, c0 + kMomentsThreads)
     const int j = c0 + threadIdx.x;
@@ -714,6 +727,7 @@ __device__ __forceinline__ void emit_record(int i, int sp, int4 T, int accuracy,
 static __global__ void k_records(int n, Segs segs, int accuracy, float theta, float G,
                                  const int* __restrict__ box_ord, const uint64_t* __restrict__ skeys,
                                  TreePtrs t, NodeSums ns, Records rec) {
+    pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int sp = t.split[i];

@@ -61,6 +61,24 @@ T* carve(char*& cur, size_t count) {
     return p;
 }
 
+// Launch with programmatic stream serialisation: the kernel may begin while the
+// previous kernel on the stream drains (it calls pdl_wait before reading).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), int grid, int block, size_t smem,
+                       cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 template <typename T>
 size_t span(size_t count) {
     return (sizeof(T) * count + 255) & ~size_t(255);
@@ -111,15 +129,16 @@ static cudaError_t launch_acc(const StepArgs& a, cudaStream_t st, int part) {
         const size_t smb = (size_t)warps * acc_warp_bytes(sb);
         int gb = std::min(a.walk_grid_acc, (a.groups2.ngroups + warps - 1) / warps);
         if (gb < 1) gb = 1;
-        k_walk_acc<false, true, false, 2><<<gb, warps * 32, smb, st>>>(
-            sb, a.segs, a.groups2, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt,
-            a.alpha, a.out, a.status, a.inter, a.work + 1, a.fresh, a.max_stack);
+        return launch_pdl(k_walk_acc<false, true, false, 2>, gb, warps * 32, smb, st, sb, a.segs,
+                          a.groups2, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt,
+                          a.ddt, a.alpha, a.out, a.status, a.inter, a.work + 1, a.fresh,
+                          a.max_stack, (double*)nullptr);
     } else {
-        k_walk_acc<MIXED, false, false, BPL><<<grid, warps * 32, smem, st>>>(
-            sh, a.segs, gr, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt,
-            a.alpha, a.out, a.status, a.inter, a.work + 2, a.fresh, a.max_stack);
+        return launch_pdl(k_walk_acc<MIXED, false, false, BPL>, grid, warps * 32, smem, st, sh,
+                          a.segs, gr, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt,
+                          a.ddt, a.alpha, a.out, a.status, a.inter, a.work + 2, a.fresh,
+                          a.max_stack, (double*)nullptr);
     }
-    return cudaGetLastError();
 }
 
 // part 0: the accuracy modes' bootstrap pass (nothing in REFERENCE mode);
@@ -129,10 +148,9 @@ cudaError_t launch_walk(const StepArgs& a, cudaStream_t st, int part) {
         if (part == 0) return cudaSuccess;
         int grid = std::min(a.walk_grid_ref, (a.groups.ngroups + kWalkWarps - 1) / kWalkWarps);
         if (grid < 1) grid = 1;
-        k_walk_ref<kWalkWarps, kRefStack><<<grid, kWalkWarps * 32, 0, st>>>(
-            a.segs, a.groups, a.in, a.recA, a.recC, a.eps2, a.dt, a.ddt, a.out, a.status, a.inter,
-            a.work);
-        return cudaGetLastError();
+        return launch_pdl(k_walk_ref<kWalkWarps, kRefStack>, grid, kWalkWarps * 32, 0, st, a.segs,
+                          a.groups, a.in, a.recA, a.recC, a.eps2, a.dt, a.ddt, a.out, a.status,
+                          a.inter, a.work);
     }
     if (a.bpl == 2)
         return a.mode == BH_MODE_MIXED ? launch_acc<true, 2>(a, st, part)
@@ -282,12 +300,11 @@ int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev)
 
     BodyPtrs cur = s->st[0];
     CK(mark(0));
-    k_bbox<kBboxThreads><<<s->nchunks, kBboxThreads, 0, st>>>(cur.x, cur.y, s->chunk_seg,
-                                                              s->chunk_begin, s->chunk_end,
-                                                              s->box_ord, s->status);
+    CK(launch_pdl(k_bbox<kBboxThreads>, s->nchunks, kBboxThreads, 0, st, cur.x, cur.y,
+                  s->chunk_seg, s->chunk_begin, s->chunk_end, s->box_ord, s->status));
     const int tb = 256, nb = (n + tb - 1) / tb;
     CK(mark(1));
-    k_keys<<<nb, tb, 0, st>>>(cur.x, cur.y, n, segs, s->box_ord, s->keys, s->vals);
+    CK(launch_pdl(k_keys, nb, tb, 0, st, cur.x, cur.y, n, segs, s->box_ord, s->keys, s->vals));
     CK(mark(2));
 
     // LSD radix sort: 8 passes over the key, then the system index
@@ -297,12 +314,11 @@ int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev)
     for (int ps = 0; ps < passes; ++ps) {
         int use_seg = ps >= 8;
         int shift = use_seg ? 8 * (ps - 8) : 8 * ps;
-        k_radix_hist<<<s->tiles, kSortThreads, 0, st>>>(ka, va, n, shift, use_seg, s->seg_of_pos,
-                                                        s->hist, s->tiles);
-        k_radix_scan<<<256, kSortThreads, 0, st>>>(s->hist, s->tiles, s->totals);
-        k_radix_scatter<<<s->tiles, kSortThreads, 0, st>>>(ka, va, kb, vb, n, shift, use_seg,
-                                                           s->seg_of_pos, s->hist, s->totals,
-                                                           s->tiles);
+        CK(launch_pdl(k_radix_hist, s->tiles, kSortThreads, 0, st, ka, va, n, shift, use_seg,
+                      s->seg_of_pos, s->hist, s->tiles));
+        CK(launch_pdl(k_radix_scan, 256, kSortThreads, 0, st, s->hist, s->tiles, s->totals));
+        CK(launch_pdl(k_radix_scatter, s->tiles, kSortThreads, 0, st, ka, va, kb, vb, n, shift,
+                      use_seg, s->seg_of_pos, s->hist, s->totals, s->tiles));
         std::swap(ka, kb);
         std::swap(va, vb);
     }
@@ -316,15 +332,15 @@ int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev)
         dst.xlo = dst.ylo = nullptr;
     }
     if (!accuracy) src.amag = dst.amag = nullptr;
-    k_gather<<<nb, tb, 0, st>>>(n, va, src, dst);
+    CK(launch_pdl(k_gather, nb, tb, 0, st, n, va, src, dst));
     CK(mark(4));
-    k_build<<<nb, tb, 0, st>>>(ka, n, segs, s->tree, s->status);
+    CK(launch_pdl(k_build, nb, tb, 0, st, ka, n, segs, s->tree, s->status));
     CK(mark(5));
-    k_moments<<<(n + kMomentsThreads - 1) / kMomentsThreads, kMomentsThreads, 0, st>>>(
-        n, accuracy ? 1 : 0, dst.x, dst.y, dst.m, s->tree.climb, s->tree.leaf_parent, s->counter,
-        s->sums, s->status);
-    k_records<<<nb, tb, 0, st>>>(n, segs, accuracy ? 1 : 0, s->p.theta, s->p.gravity, s->box_ord,
-                                 ka, s->tree, s->sums, s->rec);
+    CK(launch_pdl(k_moments, (n + kMomentsThreads - 1) / kMomentsThreads, kMomentsThreads, 0, st, n,
+                  accuracy ? 1 : 0, dst.x, dst.y, dst.m, s->tree.climb, s->tree.leaf_parent,
+                  s->counter, s->sums, s->status));
+    CK(launch_pdl(k_records, nb, tb, 0, st, n, segs, accuracy ? 1 : 0, s->p.theta, s->p.gravity,
+                  s->box_ord, ka, s->tree, s->sums, s->rec));
     CK(cudaGetLastError());
     CK(mark(6));
     return BH_OK;

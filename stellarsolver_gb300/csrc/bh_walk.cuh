@@ -87,6 +87,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_walk_ref(Segs segs, Groups gr, W
                                                          int* __restrict__ status,
                                                          unsigned long long* __restrict__ inter_total,
                                                          int* __restrict__ work) {
+    pdl_wait();
     __shared__ int s_stack[WARPS][STACK];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     int* stack = s_stack[warp];
@@ -373,6 +374,7 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
                                                          int* __restrict__ fresh,
                                                          int* __restrict__ max_stack,
                                                          double* __restrict__ pot = nullptr) {
+    pdl_wait();
     static_assert(BPL == 1 || BPL == 2, "one or two bodies per lane");
     if (ESTIMATE) {
         if (*(volatile int*)fresh == 0) return;

@@ -26,6 +26,8 @@ def main():
     ap.add_argument("--bpl", type=int, default=0, help="bodies per lane of the accuracy walk")
     ap.add_argument("--block", type=int, default=0, help="walk threads per block")
     ap.add_argument("--phases", action="store_true", help="also print event-timed phase ms")
+    ap.add_argument("--graph-ms", type=int, default=0, metavar="K",
+                    help="also time K steps replayed as a CUDA graph (host clock, synchronised)")
     ap.add_argument("--error", action="store_true",
                     help="also print the force error against the FP64 direct sum (4096 bodies)")
     ap.add_argument("--graph", action="store_true")
@@ -56,6 +58,16 @@ def main():
             s.step(1)
             s.sync()
         st = s.stats()
+        if a.graph_ms:
+            import time
+            s.set_params(mode=a.mode, theta=0.5, eps2=1e-4, timestep=1e-4, leaf_bucket=a.bucket,
+                         use_graph=True, bodies_per_lane=a.bpl, block_size=a.block)
+            s.step(3)
+            s.sync()
+            t0 = time.perf_counter()
+            s.step(a.graph_ms)
+            s.sync()
+            print(f"graph step ms: {1e3 * (time.perf_counter() - t0) / a.graph_ms:.4f}")
         if a.phases:
             ms = np.zeros(bh.PHASES_N, np.float32)
             for _ in range(5):
