@@ -1142,17 +1142,52 @@ int bh_measure_fp32_peak(int device, double* tflops) {
 }
 
 // Per-system FP64 sums: out[4k..4k+3] += kinetic, potential (0.5 m phi), px, py.
-__global__ void k_energy_reduce(int n, Segs segs, const float* __restrict__ m,
-                                const float* __restrict__ vx, const float* __restrict__ vy,
-                                const double* __restrict__ pot, double* __restrict__ out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double mi = m[i], u = vx[i], v = vy[i];
-    double* o = out + 4 * seg_of(segs, i);
-    atomicAdd(o + 0, 0.5 * mi * (u * u + v * v));
-    atomicAdd(o + 1, 0.5 * mi * pot[i]);
-    atomicAdd(o + 2, mi * u);
-    atomicAdd(o + 3, mi * v);
+// Reduced over the block first (one atomic per block and value) when the
+// block's positions belong to one system, as systems are contiguous ranges.
+__global__ void __launch_bounds__(256) k_energy_reduce(int n, Segs segs,
+                                                       const float* __restrict__ m,
+                                                       const float* __restrict__ vx,
+                                                       const float* __restrict__ vy,
+                                                       const double* __restrict__ pot,
+                                                       double* __restrict__ out) {
+    __shared__ double s_part[8][4];
+    const int b0 = blockIdx.x * blockDim.x;
+    const int i = b0 + threadIdx.x;
+    double e[4] = {0.0, 0.0, 0.0, 0.0};
+    int sg = 0;
+    if (i < n) {
+        const double mi = m[i], u = vx[i], v = vy[i];
+        e[0] = 0.5 * mi * (u * u + v * v);
+        e[1] = 0.5 * mi * pot[i];
+        e[2] = mi * u;
+        e[3] = mi * v;
+        sg = seg_of(segs, i);
+    }
+    const int last = min(n, b0 + (int)blockDim.x) - 1;
+    if (seg_of(segs, b0) != seg_of(segs, last)) {  // a block across two systems
+        if (i < n)
+            for (int k = 0; k < 4; ++k) atomicAdd(out + 4 * sg + k, e[k]);
+        return;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) e[k] += __shfl_down_sync(kFull, e[k], o);
+        if (lane == 0) s_part[warp][k] = e[k];
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        const int s0 = seg_of(segs, b0);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            double v = lane < nw ? s_part[lane][k] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFull, v, o);
+            if (lane == 0) atomicAdd(out + 4 * s0 + k, v);
+        }
+    }
 }
 
 // The diagnostics pass on `st`, no synchronisation: the tree of the current
