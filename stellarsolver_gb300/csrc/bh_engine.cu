@@ -206,6 +206,8 @@ struct bh_system {
                            // [6..8]: scratch of bh_energy
     double* diag = nullptr;  // bh_energy: 4 sums per system
     int* fresh = nullptr;  // 1 after bh_set_state: bootstrap |a_old| in the next step
+    bool fresh_host = false;  // the host's record of *fresh: the bootstrap pass is launched
+                              // only in steps that follow bh_set_state
     int seg_passes = 0;
 
     int walk_grid_ref = 0, walk_grid_acc = 0;
@@ -224,17 +226,19 @@ struct bh_system {
     cudaGraphExec_t egraph_exec = nullptr;
 
     cudaStream_t cap_stream = nullptr;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t graph_exec = nullptr;
+    cudaGraph_t graph[2] = {nullptr, nullptr};  // one step without / with the bootstrap pass
+    cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
 };
 
 namespace {
 
 void drop_graph(bh_system* s) {
-    if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
-    if (s->graph) cudaGraphDestroy(s->graph);
-    s->graph_exec = nullptr;
-    s->graph = nullptr;
+    for (int b = 0; b < 2; ++b) {
+        if (s->graph_exec[b]) cudaGraphExecDestroy(s->graph_exec[b]);
+        if (s->graph[b]) cudaGraphDestroy(s->graph[b]);
+        s->graph_exec[b] = nullptr;
+        s->graph[b] = nullptr;
+    }
     if (s->egraph_exec) cudaGraphExecDestroy(s->egraph_exec);
     if (s->egraph) cudaGraphDestroy(s->egraph);
     s->egraph_exec = nullptr;
@@ -348,12 +352,16 @@ int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev)
 
 // One step: the front half, then the bootstrap pass (accuracy modes, fresh
 // state only) and the walk fused with the integration (phases 6-7).
-int enqueue_step(bh_system* s, cudaStream_t st, cudaEvent_t* ev = nullptr) {
+// boot < 0: the bootstrap pass is launched iff bh_set_state came since the last
+// step (the host's record, cleared here); 0 / 1: left out / launched (graph capture).
+int enqueue_step(bh_system* s, cudaStream_t st, cudaEvent_t* ev = nullptr, int boot = -1) {
     auto mark = [&](int k) -> cudaError_t { return ev ? cudaEventRecord(ev[k], st) : cudaSuccess; };
+    const bool with_boot = boot < 0 ? s->fresh_host : boot > 0;
+    if (boot < 0) s->fresh_host = false;
     int rc = enqueue_front(s, st, s->p.mode != BH_MODE_REFERENCE, ev);
     if (rc != BH_OK) return rc;
     StepArgs a = step_args(s);
-    CK(launch_walk(a, st, 0));
+    if (with_boot) CK(launch_walk(a, st, 0));
     CK(mark(7));
     CK(launch_walk(a, st, 1));
     CK(mark(8));
@@ -433,11 +441,10 @@ __global__ void k_direct_reduce(int ns, int chunks, const double* __restrict__ p
     out[t] = G * acc;
 }
 
-int build_graph(bh_system* s) {
-    drop_graph(s);
+int build_graph(bh_system* s, int boot) {
     if (!s->cap_stream) CK(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
     CK(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal));
-    int st = enqueue_step(s, s->cap_stream);
+    int st = enqueue_step(s, s->cap_stream, nullptr, boot);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(s->cap_stream, &g);
     if (st != BH_OK) {
@@ -445,8 +452,8 @@ int build_graph(bh_system* s) {
         return st;
     }
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
-    s->graph = g;
-    CK(cudaGraphInstantiate(&s->graph_exec, g, 0));
+    s->graph[boot] = g;
+    CK(cudaGraphInstantiate(&s->graph_exec[boot], g, 0));
     return BH_OK;
 }
 
@@ -754,6 +761,7 @@ int bh_set_state(bh_system* s, const float* x, const float* y, const float* vx, 
     CK(cudaGetLastError());
     s->have_state = true;
     s->caller_order = true;
+    s->fresh_host = true;
     return BH_OK;
 }
 
@@ -779,6 +787,7 @@ int bh_set_accel(bh_system* s, const float* ax, const float* ay, void* stream) {
     k_amag<<<(s->n + 255) / 256, 256, 0, st>>>(s->n, t.x, t.y, s->st[0].amag, s->ax, s->ay);
     CK(cudaGetLastError());
     CK(cudaMemsetAsync(s->fresh, 0, sizeof(int), st));
+    s->fresh_host = false;
     return BH_OK;
 }
 
@@ -838,19 +847,21 @@ int bh_step(bh_system* s, int steps, void* stream) {
     CK(cudaSetDevice(s->device));
     cudaStream_t st = (cudaStream_t)stream;
     if (s->p.use_graph) {
-        if (!s->graph_exec) {
-            // the capture stream must see the state that `stream` produced
-            cudaEvent_t ev;
-            CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-            CK(cudaEventRecord(ev, st));
-            if (!s->cap_stream) CK(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
-            CK(cudaStreamWaitEvent(s->cap_stream, ev, 0));
-            cudaEventDestroy(ev);
-            int rc = build_graph(s);
-            if (rc != BH_OK) return rc;
-        }
         for (int k = 0; k < steps; ++k) {
-            CK(cudaGraphLaunch(s->graph_exec, st));
+            const int gi = s->fresh_host ? 1 : 0;  // with the bootstrap pass after bh_set_state
+            if (!s->graph_exec[gi]) {
+                // the capture stream must see the state that `stream` produced
+                cudaEvent_t ev;
+                CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+                CK(cudaEventRecord(ev, st));
+                if (!s->cap_stream) CK(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
+                CK(cudaStreamWaitEvent(s->cap_stream, ev, 0));
+                cudaEventDestroy(ev);
+                int rc = build_graph(s, gi);
+                if (rc != BH_OK) return rc;
+            }
+            CK(cudaGraphLaunch(s->graph_exec[gi], st));
+            s->fresh_host = false;
             s->caller_order = false;
             if (s->energy_every > 0 && ++s->energy_steps % s->energy_every == 0) {
                 if (!s->egraph_exec) {
@@ -1328,6 +1339,7 @@ int bh_autotune(bh_system* s, void* stream, bh_params* chosen) {
     CK(cudaMalloc(&bk, N * 9 * sizeof(float) + sizeof(int)));
     BodyPtrs& c = s->st[0];
     float* arrs[8] = {c.x, c.y, c.vx, c.vy, c.m, c.xlo, c.ylo, c.amag};
+    const bool orig_fresh = s->fresh_host;
     auto save = [&]() -> int {
         for (int k = 0; k < 8; ++k)
             CK(cudaMemcpyAsync(bk + k * N, arrs[k], N * sizeof(float), cudaMemcpyDeviceToDevice, st));
@@ -1341,6 +1353,7 @@ int bh_autotune(bh_system* s, void* stream, bh_params* chosen) {
         CK(cudaMemcpyAsync(c.id, bk + 8 * N, N * sizeof(int), cudaMemcpyDeviceToDevice, st));
         CK(cudaMemcpyAsync(s->fresh, bk + 9 * N, sizeof(int), cudaMemcpyDeviceToDevice, st));
         CK(cudaMemsetAsync(s->status, 0, sizeof(int), st));
+        s->fresh_host = orig_fresh;
         return BH_OK;
     };
     const bh_params orig = s->p;
