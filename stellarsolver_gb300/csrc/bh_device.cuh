@@ -176,26 +176,64 @@ static __global__ void __launch_bounds__(THREADS) k_bbox(const float* __restrict
     }
 }
 
+// ------------------------------------------------------------------ bodies
+
+struct BodyPtrs {
+    float *x, *y, *vx, *vy, *m, *xlo, *ylo;  // xlo/ylo may be null
+    int* id;
+    float* amag;  // |a| of the previous step (accuracy modes; may be null)
+};
+
+// Body i of src becomes body j of dst (the reorder into key order).
+__device__ __forceinline__ void gather_body(int j, uint32_t i, const BodyPtrs& src,
+                                            const BodyPtrs& dst) {
+    dst.x[j] = src.x[i];
+    dst.y[j] = src.y[i];
+    dst.vx[j] = src.vx[i];
+    dst.vy[j] = src.vy[i];
+    dst.m[j] = src.m[i];
+    dst.id[j] = src.id[i];
+    if (src.xlo) {
+        dst.xlo[j] = src.xlo[i];
+        dst.ylo[j] = src.ylo[i];
+    }
+    if (src.amag) dst.amag[j] = src.amag[i];
+}
+
 // ------------------------------------------------------------------ (b1) keys
 
 // Level by level: mid = (lo+hi)*0.5 in float, digit bit 0 = x < mid_x,
 // bit 1 = y < mid_y, the body's half becomes the interval (kernels.cu:144-157,
 // 165-177).  Explicit _rn intrinsics: no contraction may change a midpoint.
+// The x and y intervals are bisected together in packed FP32x2 arithmetic
+// (per component the same IEEE operations); the x and y bits are collected
+// separately and interleaved at the end.
+__device__ __forceinline__ uint64_t spread_even_bits(uint32_t v) {
+    uint64_t x = v;
+    x = (x | (x << 16)) & 0x0000ffff0000ffffull;
+    x = (x | (x << 8)) & 0x00ff00ff00ff00ffull;
+    x = (x | (x << 4)) & 0x0f0f0f0f0f0f0f0full;
+    x = (x | (x << 2)) & 0x3333333333333333ull;
+    x = (x | (x << 1)) & 0x5555555555555555ull;
+    return x;
+}
+
 __device__ __forceinline__ uint64_t quad_key(float px, float py, Box bx) {
-    float l = bx.l, r = bx.r, b = bx.b, t = bx.t;
-    uint64_t key = 0;
+    float2 lo = make_float2(bx.l, bx.b), hi = make_float2(bx.r, bx.t);
+    const float2 half = make_float2(0.5f, 0.5f);
+    uint32_t kx = 0, ky = 0;
 #pragma unroll 8
     for (int level = 0; level < 32; ++level) {
-        float mx = __fmul_rn(__fadd_rn(l, r), 0.5f);
-        float my = __fmul_rn(__fadd_rn(b, t), 0.5f);
-        bool xl = px < mx, yl = py < my;
-        r = xl ? mx : r;
-        l = xl ? l : mx;
-        t = yl ? my : t;
-        b = yl ? b : my;
-        key = (key << 2) | (uint64_t)((xl ? 1u : 0u) | (yl ? 2u : 0u));
+        const float2 mid = __fmul2_rn(__fadd2_rn(lo, hi), half);
+        const bool xl = px < mid.x, yl = py < mid.y;
+        hi.x = xl ? mid.x : hi.x;
+        lo.x = xl ? lo.x : mid.x;
+        hi.y = yl ? mid.y : hi.y;
+        lo.y = yl ? lo.y : mid.y;
+        kx = (kx << 1) | (xl ? 1u : 0u);
+        ky = (ky << 1) | (yl ? 1u : 0u);
     }
-    return key;
+    return spread_even_bits(kx) | (spread_even_bits(ky) << 1);
 }
 
 static __global__ void k_keys(const float* __restrict__ x, const float* __restrict__ y, int n, Segs segs,
@@ -207,6 +245,23 @@ static __global__ void k_keys(const float* __restrict__ x, const float* __restri
     Box bx = load_box(box_ord, seg_of(segs, i));
     keys[i] = quad_key(x[i], y[i], bx);
     vals[i] = (uint32_t)i;
+}
+
+// k_keys for the engine's step: also clears the moments arrival counters of
+// these positions and (block 0) the step's first `nzero` scheduling and
+// statistics words.
+static __global__ void k_keys_step(const float* __restrict__ x, const float* __restrict__ y, int n,
+                                   Segs segs, const int* __restrict__ box_ord,
+                                   uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                   int* __restrict__ counter, int* __restrict__ zero, int nzero) {
+    pdl_wait();
+    if (blockIdx.x == 0 && threadIdx.x < nzero) zero[threadIdx.x] = 0;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Box bx = load_box(box_ord, seg_of(segs, i));
+    keys[i] = quad_key(x[i], y[i], bx);
+    vals[i] = (uint32_t)i;
+    counter[i] = 0;
 }
 
 // ------------------------------------------------------------------ (b2) radix sort
@@ -360,28 +415,11 @@ static __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(
 
 // ------------------------------------------------------------------ (d) reorder
 
-struct BodyPtrs {
-    float *x, *y, *vx, *vy, *m, *xlo, *ylo;  // xlo/ylo may be null
-    int* id;
-    float* amag;  // |a| of the previous step (accuracy modes; may be null)
-};
-
 static __global__ void k_gather(int n, const uint32_t* __restrict__ perm, BodyPtrs src, BodyPtrs dst) {
     pdl_wait();
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
-    uint32_t i = perm[j];
-    dst.x[j] = src.x[i];
-    dst.y[j] = src.y[i];
-    dst.vx[j] = src.vx[i];
-    dst.vy[j] = src.vy[i];
-    dst.m[j] = src.m[i];
-    dst.id[j] = src.id[i];
-    if (src.xlo) {
-        dst.xlo[j] = src.xlo[i];
-        dst.ylo[j] = src.ylo[i];
-    }
-    if (src.amag) dst.amag[j] = src.amag[i];
+    gather_body(j, perm[j], src, dst);
 }
 
 // ------------------------------------------------------------------ (b3) tree

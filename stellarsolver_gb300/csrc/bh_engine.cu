@@ -53,6 +53,11 @@ constexpr int kBboxChunk = 8192;
 
 int walk_grid_cap(int device_sms, int blocks_per_sm) { return device_sms * std::max(1, blocks_per_sm); }
 
+// Per-step words: 2 x u64 interaction counts, then bh_system::work (9 ints);
+// the counts and work[0..5] are cleared at the start of every step.
+constexpr int kStepWords = 16;
+constexpr int kStepZero = 4 + 6;
+
 template <typename T>
 T* carve(char*& cur, size_t count) {
     T* p = reinterpret_cast<T*>(cur);
@@ -298,9 +303,6 @@ int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev)
     const bool mixed = s->p.mode == BH_MODE_MIXED;
     Segs segs{s->nseg, s->seg_off, s->nseg > 1 ? s->seg_of_pos : nullptr};
     CK(cudaMemsetAsync(s->box_ord, 0, sizeof(int) * 4 * s->nseg, st));  // origin box
-    CK(cudaMemsetAsync(s->counter, 0, sizeof(int) * n, st));
-    CK(cudaMemsetAsync(s->inter, 0, 2 * sizeof(unsigned long long), st));
-    CK(cudaMemsetAsync(s->work, 0, 6 * sizeof(int), st));
 
     BodyPtrs cur = s->st[0];
     CK(mark(0));
@@ -308,7 +310,9 @@ int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev)
                   s->chunk_seg, s->chunk_begin, s->chunk_end, s->box_ord, s->status));
     const int tb = 256, nb = (n + tb - 1) / tb;
     CK(mark(1));
-    CK(launch_pdl(k_keys, nb, tb, 0, st, cur.x, cur.y, n, segs, s->box_ord, s->keys, s->vals));
+    // keys and positions; the moments counters and the step's words cleared
+    CK(launch_pdl(k_keys_step, nb, tb, 0, st, cur.x, cur.y, n, segs, s->box_ord, s->keys, s->vals,
+                  s->counter, reinterpret_cast<int*>(s->inter), kStepZero));
     CK(mark(2));
 
     // LSD radix sort: 8 passes over the key, then the system index
@@ -562,7 +566,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     bytes += 8 * span<int>(N) + span<int4>(N);                  // tree arrays, counter, climb
     bytes += 2 * span<float4>(N);                               // node sums
     bytes += 2 * span<float4>(N) + 2 * span<int4>(N);           // walk records
-    bytes += 2 * span<float>(N) + span<int>(1) + span<unsigned long long>(2) + span<int>(9) +
+    bytes += 2 * span<float>(N) + span<int>(1) + span<int>(kStepWords) +
              span<double>(4 * (size_t)nseg) + span<int>(1);
     cudaError_t e = cudaMalloc(&s->arena, bytes);
     if (e != cudaSuccess) {
@@ -616,8 +620,13 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     s->ax = carve<float>(c, N);
     s->ay = carve<float>(c, N);
     s->status = carve<int>(c, 1);
-    s->inter = carve<unsigned long long>(c, 2);  // all interactions, body-cell ones
-    s->work = carve<int>(c, 9);
+    {
+        // inter (2 x u64: all interactions, body-cell ones), then work: the first
+        // kStepZero words are cleared by every step's key kernel
+        int* w = carve<int>(c, kStepWords);
+        s->inter = reinterpret_cast<unsigned long long*>(w);
+        s->work = w + 4;
+    }
     s->diag = carve<double>(c, 4 * (size_t)nseg);
     s->fresh = carve<int>(c, 1);
 
