@@ -49,7 +49,7 @@ extern "C" {
  *   iff min over the group's bodies |COM - p| > l/theta + |COM - cell centre|
  *   (l = larger cell side) and G M l^3 / d^5 <= alpha |a_old| (previous
  *   step's |a|; the first step after bh_set_state bootstraps it with a
- *   geometric-only pass at opening angle max(theta, 1) with monopole cells);
+ *   geometric-only pass at opening angle max(theta, 1.25) with monopole cells);
  *   leaf buckets; G applied.
  * MIXED: PLAIN plus compensated (Kahan) force sums and positions kept as
  *   hi + lo float pairs. */

@@ -121,7 +121,7 @@ def test_momentum_nearly_conserved(bh):
 @pytest.mark.parametrize("bpl", [1, 2])
 def test_walk_matches_cpu_restatement(bh, oracle, bpl):
     """The GPU PLAIN walk against oracle.walk_acc (same tree, same rule: the
-    bootstrap pass at opening angle 1 with monopole cells in 64-body groups,
+    bootstrap pass at opening angle 1.25 with monopole cells in 64-body groups,
     then the relative rule with alpha = 0.01).  Moments are
     summed with different float rounding, so a borderline node may be opened on
     one side only: interaction counts agree to 0.5 %, forces to 2e-4 of RMS."""
@@ -145,7 +145,7 @@ def test_walk_matches_cpu_restatement(bh, oracle, bpl):
     sk = k[operm]
     t = oracle.Tree(sk)
     sx, sy, sm = x[operm], y[operm], m[operm]
-    a0x, a0y, _ = oracle.walk_acc(sx, sy, sm, sk, t, box, 1.0, eps2, quadrupole=False,
+    a0x, a0y, _ = oracle.walk_acc(sx, sy, sm, sk, t, box, 1.25, eps2, quadrupole=False,
                                   group=64)  # bootstrap: always 64-body groups
     ox, oy, ointer = oracle.walk_acc(sx, sy, sm, sk, t, box, 0.5, eps2, alpha=0.01,
                                      aold=np.hypot(a0x, a0y), group=32 * bpl)
