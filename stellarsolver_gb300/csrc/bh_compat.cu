@@ -660,10 +660,11 @@ void compat_BuildQuadTree(float* x, float* y, float* mass, int* count, int* star
     uint32_t *va = w->vals, *vb = w->vals_alt;
     const int tiles = (n + kSortTile - 1) / kSortTile;
     for (int ps = 0; ps < 8; ++ps) {
-        k_radix_hist<<<tiles, kSortThreads, 0, st>>>(ka, va, n, 8 * ps, 0, nullptr, w->hist, tiles);
-        k_radix_scan<<<256, kSortThreads, 0, st>>>(w->hist, tiles, w->totals);
+        k_radix_hist<<<tiles, kSortThreads, 0, st>>>(ka, va, n, 8 * ps, 0, nullptr, w->hist, tiles,
+                                                     nullptr);
+        k_radix_scan<<<256, kSortThreads, 0, st>>>(w->hist, tiles, w->totals, nullptr);
         k_radix_scatter<<<tiles, kSortThreads, 0, st>>>(ka, va, kb, vb, n, 8 * ps, 0, nullptr,
-                                                        w->hist, w->totals, tiles);
+                                                        w->hist, w->totals, tiles, nullptr);
         std::swap(ka, kb);
         std::swap(va, vb);
     }
@@ -890,10 +891,11 @@ extern "C" int BuildQuadTreeNoAlloc(float* x, float* y, float* mass, int* count,
     uint32_t *va = w.vals, *vb = w.vals_alt;
     const int tiles = w.tiles;
     for (int ps = 0; ps < 8; ++ps) {
-        k_radix_hist<<<tiles, kSortThreads, 0, st>>>(ka, va, n, 8 * ps, 0, nullptr, w.hist, tiles);
-        k_radix_scan<<<256, kSortThreads, 0, st>>>(w.hist, tiles, w.totals);
+        k_radix_hist<<<tiles, kSortThreads, 0, st>>>(ka, va, n, 8 * ps, 0, nullptr, w.hist, tiles,
+                                                     nullptr);
+        k_radix_scan<<<256, kSortThreads, 0, st>>>(w.hist, tiles, w.totals, nullptr);
         k_radix_scatter<<<tiles, kSortThreads, 0, st>>>(ka, va, kb, vb, n, 8 * ps, 0, nullptr,
-                                                        w.hist, w.totals, tiles);
+                                                        w.hist, w.totals, tiles, nullptr);
         std::swap(ka, kb);
         std::swap(va, vb);
     }

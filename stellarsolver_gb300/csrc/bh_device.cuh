@@ -248,14 +248,16 @@ static __global__ void k_keys(const float* __restrict__ x, const float* __restri
 }
 
 // k_keys for the engine's step: also clears the moments arrival counters of
-// these positions and (block 0) the step's first `nzero` scheduling and
-// statistics words.
+// these positions, the sort's run overflow flag and (block 0) the step's first
+// `nzero` scheduling and statistics words.
 static __global__ void k_keys_step(const float* __restrict__ x, const float* __restrict__ y, int n,
                                    Segs segs, const int* __restrict__ box_ord,
                                    uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
-                                   int* __restrict__ counter, int* __restrict__ zero, int nzero) {
+                                   int* __restrict__ counter, int* __restrict__ zero, int nzero,
+                                   int* __restrict__ sort_flag) {
     pdl_wait();
     if (blockIdx.x == 0 && threadIdx.x < nzero) zero[threadIdx.x] = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *sort_flag = 0;
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     Box bx = load_box(box_ord, seg_of(segs, i));
@@ -282,12 +284,16 @@ static_assert(kSortThreads == 256, "one thread per digit in the sort kernels");
 // per-tile digit counts, written digit-major: hist[d * tiles + tile].  Each
 // warp counts into its own shared sub-histogram with plain shared atomics
 // (twice as fast as aggregating equal digits with warp votes first).
+// The three pass kernels take `only_if`: when non-null they do nothing unless
+// *only_if is set (the fallback full sort of k_sort_fixup's overflow).
 static __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint64_t* __restrict__ keys,
                                                              const uint32_t* __restrict__ vals, int n,
                                                              int shift, int use_seg,
                                                              const int* __restrict__ seg_of_pos,
-                                                             uint32_t* __restrict__ hist, int tiles) {
+                                                             uint32_t* __restrict__ hist, int tiles,
+                                                             const int* __restrict__ only_if) {
     pdl_wait();
+    if (only_if && *only_if == 0) return;
     constexpr int W = kSortThreads / 32;
     __shared__ uint32_t s_h[W][256];
     for (int i = threadIdx.x; i < W * 256; i += kSortThreads) (&s_h[0][0])[i] = 0u;
@@ -314,8 +320,10 @@ static __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint64
 
 // block d turns column d of hist into exclusive offsets; totals[d] = column sum
 static __global__ void __launch_bounds__(kSortThreads) k_radix_scan(uint32_t* __restrict__ hist, int tiles,
-                                                             uint32_t* __restrict__ totals) {
+                                                             uint32_t* __restrict__ totals,
+                                                             const int* __restrict__ only_if) {
     pdl_wait();
+    if (only_if && *only_if == 0) return;
     __shared__ uint32_t s_tmp[kSortThreads / 32];
     uint32_t* col = hist + (size_t)blockIdx.x * tiles;
     uint32_t running = 0;
@@ -337,8 +345,10 @@ static __global__ void __launch_bounds__(kSortThreads) k_radix_scan(uint32_t* __
 static __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(
     const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
     uint32_t* __restrict__ vout, int n, int shift, int use_seg, const int* __restrict__ seg_of_pos,
-    const uint32_t* __restrict__ hist, const uint32_t* __restrict__ totals, int tiles) {
+    const uint32_t* __restrict__ hist, const uint32_t* __restrict__ totals, int tiles,
+    const int* __restrict__ only_if) {
     pdl_wait();
+    if (only_if && *only_if == 0) return;
     constexpr int W = kSortThreads / 32;
     constexpr int WCHUNK = 32 * kSortItems;
     __shared__ uint32_t s_wh[W][256];
@@ -411,6 +421,47 @@ static __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(
         kout[o] = kk;
         vout[o] = vv;
     }
+}
+
+// After stable passes over bits 32..63 of the key, elements with equal high
+// words form runs in input order; each run is put in whole-key order with
+// ties kept in input order, which gives the stable sort by the whole key.
+// Element i's place in its run is the number of run members before it in
+// that order.  A run longer than kFixupRun is not ordered: *overflow is set,
+// and (set_cond, graph replay) the conditional node that holds the full
+// sort is switched on; exactly one thread does either.
+constexpr int kFixupRun = 256;
+
+static __global__ void k_sort_fixup(int n, const uint64_t* __restrict__ kin,
+                                    const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
+                                    uint32_t* __restrict__ vout, int* __restrict__ overflow,
+                                    cudaGraphConditionalHandle cond, int set_cond) {
+    pdl_wait();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint64_t k = kin[i];
+    const uint32_t hi = (uint32_t)(k >> 32);
+    const bool left = i > 0 && (uint32_t)(kin[i - 1] >> 32) == hi;
+    const bool right = i + 1 < n && (uint32_t)(kin[i + 1] >> 32) == hi;
+    if (!left && !right) {
+        kout[i] = k;
+        vout[i] = vin[i];
+        return;
+    }
+    int a = i, b = i + 1;
+    while (a > 0 && (uint32_t)(kin[a - 1] >> 32) == hi && i - a < kFixupRun) --a;
+    while (b < n && (uint32_t)(kin[b] >> 32) == hi && b - i <= kFixupRun) ++b;
+    if (b - a > kFixupRun) {
+        if (atomicCAS(overflow, 0, 1) == 0 && set_cond) cudaGraphSetConditional(cond, 1u);
+        return;
+    }
+    int rank = 0;
+    for (int j = a; j < b; ++j) {
+        const uint64_t kj = kin[j];
+        rank += (kj < k || (kj == k && j < i)) ? 1 : 0;
+    }
+    kout[a + rank] = k;
+    vout[a + rank] = vin[i];
 }
 
 // ------------------------------------------------------------------ (d) reorder

@@ -53,9 +53,13 @@ constexpr int kBboxChunk = 8192;
 
 int walk_grid_cap(int device_sms, int blocks_per_sm) { return device_sms * std::max(1, blocks_per_sm); }
 
-// Per-step words: 2 x u64 interaction counts, then bh_system::work (9 ints);
-// the counts and work[0..5] are cleared at the start of every step.
+// Per-step words: 2 x u64 interaction counts, then bh_system::work (10 ints):
+//   work[0..2] walk scheduling, [3..5] walk statistics, [6..8] the energy pass,
+//   [9] the sort's run overflow flag.
+// A step's key kernel clears the counts and work[0..5] (kStepZero words) and
+// the flag; the energy pass's tree build clears only the flag.
 constexpr int kStepWords = 16;
+constexpr int kWorkSortOverflow = 9;
 constexpr int kStepZero = 4 + 6;
 
 template <typename T>
@@ -81,6 +85,18 @@ cudaError_t launch_pdl(void (*kernel)(KArgs...), int grid, int block, size_t sme
     at[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
+// The same launch without the attribute (the body of a conditional graph node).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_plain(void (*kernel)(KArgs...), int grid, int block, size_t smem,
+                         cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
     return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
 }
 
@@ -189,8 +205,8 @@ struct bh_system {
 
     // state: [0] current (key order of the last step), [1] scratch / gathered
     BodyPtrs st[2]{};
-    uint64_t *keys = nullptr, *keys_alt = nullptr;
-    uint32_t *vals = nullptr, *vals_alt = nullptr;
+    uint64_t *keys = nullptr, *keys_alt = nullptr, *keys3 = nullptr;  // keys3: third sort buffer
+    uint32_t *vals = nullptr, *vals_alt = nullptr, *vals3 = nullptr;
     uint64_t* kfinal = nullptr;  // sorted keys after the last pass
     uint32_t* vfinal = nullptr;  // permutation after the last pass
     uint32_t *hist = nullptr, *totals = nullptr;
@@ -231,6 +247,7 @@ struct bh_system {
     cudaGraphExec_t egraph_exec = nullptr;
 
     cudaStream_t cap_stream = nullptr;
+    cudaStream_t cond_stream = nullptr;  // captures the body of the sort's conditional node
     cudaGraph_t graph[2] = {nullptr, nullptr};  // one step without / with the bootstrap pass
     cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
 };
@@ -296,8 +313,10 @@ ssg::StepArgs step_args(bh_system* s) {
 
 // Box, keys, sort, reorder, tree, moments and walk records of the current
 // state (phases 0-5; the walk records in the accuracy layout when `accuracy`).
-// ev (optional): events recorded at the phase boundaries.
-int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev) {
+// ev (optional): events recorded at the phase boundaries.  keep_stats: leave
+// the last step's interaction counts and walk statistics (the energy pass).
+int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev,
+                  bool keep_stats = false) {
     const int n = s->n;
     auto mark = [&](int k) -> cudaError_t { return ev ? cudaEventRecord(ev[k], st) : cudaSuccess; };
     const bool mixed = s->p.mode == BH_MODE_MIXED;
@@ -312,21 +331,95 @@ int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev)
     CK(mark(1));
     // keys and positions; the moments counters and the step's words cleared
     CK(launch_pdl(k_keys_step, nb, tb, 0, st, cur.x, cur.y, n, segs, s->box_ord, s->keys, s->vals,
-                  s->counter, reinterpret_cast<int*>(s->inter), kStepZero));
+                  s->counter, reinterpret_cast<int*>(s->inter), keep_stats ? 0 : kStepZero,
+                  s->work + kWorkSortOverflow));
     CK(mark(2));
 
-    // LSD radix sort: 8 passes over the key, then the system index
-    uint64_t *ka = s->keys, *kb = s->keys_alt;
-    uint32_t *va = s->vals, *vb = s->vals_alt;
-    const int passes = 8 + s->seg_passes;
-    for (int ps = 0; ps < passes; ++ps) {
-        int use_seg = ps >= 8;
-        int shift = use_seg ? 8 * (ps - 8) : 8 * ps;
-        CK(launch_pdl(k_radix_hist, s->tiles, kSortThreads, 0, st, ka, va, n, shift, use_seg,
-                      s->seg_of_pos, s->hist, s->tiles));
-        CK(launch_pdl(k_radix_scan, 256, kSortThreads, 0, st, s->hist, s->tiles, s->totals));
-        CK(launch_pdl(k_radix_scatter, s->tiles, kSortThreads, 0, st, ka, va, kb, vb, n, shift,
-                      use_seg, s->seg_of_pos, s->hist, s->totals, s->tiles));
+    // Sort (stable, by key, then by system): LSD passes over the key's high 32
+    // bits, then k_sort_fixup orders each run of equal high words by the whole
+    // key.  A run longer than kFixupRun (bodies packed into a 2^-16 box cell)
+    // makes the step take the full 8-pass sort from the original keys: in a
+    // graph behind a conditional node that only the fixup switches on, in
+    // stream order as kernels that return at once unless the flag is set.
+    int* overflow = s->work + kWorkSortOverflow;
+    uint64_t *k0 = s->keys, *kA = s->keys_alt, *kB = s->keys3;
+    uint32_t *v0 = s->vals, *vA = s->vals_alt, *vB = s->vals3;
+    auto pass = [&](auto launch, cudaStream_t q, const uint64_t* ki, const uint32_t* vi, uint64_t* ko,
+                    uint32_t* vo, int shift, int use_seg, const int* only_if) -> cudaError_t {
+        cudaError_t e = launch(k_radix_hist, s->tiles, kSortThreads, 0, q, ki, vi, n, shift, use_seg,
+                               s->seg_of_pos, s->hist, s->tiles, only_if);
+        if (e == cudaSuccess)
+            e = launch(k_radix_scan, 256, kSortThreads, 0, q, s->hist, s->tiles, s->totals, only_if);
+        if (e == cudaSuccess)
+            e = launch(k_radix_scatter, s->tiles, kSortThreads, 0, q, ki, vi, ko, vo, n, shift, use_seg,
+                       s->seg_of_pos, s->hist, s->totals, s->tiles, only_if);
+        return e;
+    };
+    auto pdl = [](auto... a) { return launch_pdl(a...); };
+    auto plain = [](auto... a) { return launch_plain(a...); };
+    // the full sort: k0 -> kB -> kA -> ... -> kA (8 passes)
+    auto full_sort = [&](auto launch, cudaStream_t q, const int* only_if) -> cudaError_t {
+        const uint64_t* ki = k0;
+        const uint32_t* vi = v0;
+        for (int ps = 0; ps < 8; ++ps) {
+            uint64_t* ko = (ps & 1) ? kA : kB;
+            uint32_t* vo = (ps & 1) ? vA : vB;
+            cudaError_t e = pass(launch, q, ki, vi, ko, vo, 8 * ps, 0, only_if);
+            if (e != cudaSuccess) return e;
+            ki = ko;
+            vi = vo;
+        }
+        return cudaSuccess;
+    };
+    cudaStreamCaptureStatus cstat = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(st, &cstat));
+    const bool capturing = cstat == cudaStreamCaptureStatusActive;
+    cudaGraph_t cgraph = nullptr;
+    cudaGraphConditionalHandle cond = 0;
+    if (capturing) {
+        CK(cudaStreamGetCaptureInfo(st, &cstat, nullptr, &cgraph, nullptr, nullptr, nullptr));
+        CK(cudaGraphConditionalHandleCreate(&cond, cgraph, 0, cudaGraphCondAssignDefault));
+    }
+    // high words: k0 -> kA -> kB -> kA -> kB
+    {
+        const uint64_t* ki = k0;
+        const uint32_t* vi = v0;
+        for (int ps = 0; ps < 4; ++ps) {
+            uint64_t* ko = (ps & 1) ? kB : kA;
+            uint32_t* vo = (ps & 1) ? vB : vA;
+            CK(pass(pdl, st, ki, vi, ko, vo, 32 + 8 * ps, 0, nullptr));
+            ki = ko;
+            vi = vo;
+        }
+    }
+    CK(launch_pdl(k_sort_fixup, nb, tb, 0, st, n, kB, vB, kA, vA, overflow, cond, capturing ? 1 : 0));
+    if (capturing) {
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        CK(cudaStreamGetCaptureInfo(st, &cstat, nullptr, &cgraph, &deps, nullptr, &ndeps));
+        cudaGraphNodeParams cp{};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = cond;
+        cp.conditional.type = cudaGraphCondTypeIf;
+        cp.conditional.size = 1;
+        cudaGraphNode_t cnode = nullptr;
+        CK(cudaGraphAddNode(&cnode, cgraph, deps, nullptr, ndeps, &cp));
+        CK(cudaStreamUpdateCaptureDependencies(st, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+        if (!s->cond_stream) return BH_ERR_STATE;  // created before the capture began
+        CK(cudaStreamBeginCaptureToGraph(s->cond_stream, cp.conditional.phGraph_out[0], nullptr,
+                                         nullptr, 0, cudaStreamCaptureModeRelaxed));
+        cudaError_t e = full_sort(plain, s->cond_stream, nullptr);
+        cudaGraph_t body = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(s->cond_stream, &body);
+        if (e != cudaSuccess) return cuda_fail(e, "conditional sort body");
+        if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture (sort body)");
+    } else {
+        CK(full_sort(pdl, st, overflow));
+    }
+    uint64_t *ka = kA, *kb = kB;
+    uint32_t *va = vA, *vb = vB;
+    for (int ps = 0; ps < s->seg_passes; ++ps) {  // then the system index
+        CK(pass(pdl, st, ka, va, kb, vb, 8 * ps, 1, nullptr));
         std::swap(ka, kb);
         std::swap(va, vb);
     }
@@ -447,6 +540,7 @@ __global__ void k_direct_reduce(int ns, int chunks, const double* __restrict__ p
 
 int build_graph(bh_system* s, int boot) {
     if (!s->cap_stream) CK(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
+    if (!s->cond_stream) CK(cudaStreamCreateWithFlags(&s->cond_stream, cudaStreamNonBlocking));
     CK(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal));
     int st = enqueue_step(s, s->cap_stream, nullptr, boot);
     cudaGraph_t g = nullptr;
@@ -559,7 +653,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
 
     size_t bytes = 0;
     bytes += 2 * (8 * span<float>(N) + span<int>(N));
-    bytes += 2 * span<uint64_t>(N) + 2 * span<uint32_t>(N);
+    bytes += 3 * span<uint64_t>(N) + 3 * span<uint32_t>(N);
     bytes += span<uint32_t>((size_t)256 * s->tiles) + span<uint32_t>(256);
     bytes += span<int>(4 * (size_t)nseg) + 3 * span<int>(nseg + 1) + span<int>(N);
     bytes += 3 * span<int>(s->nchunks);
@@ -590,8 +684,10 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     }
     s->keys = carve<uint64_t>(c, N);
     s->keys_alt = carve<uint64_t>(c, N);
+    s->keys3 = carve<uint64_t>(c, N);
     s->vals = carve<uint32_t>(c, N);
     s->vals_alt = carve<uint32_t>(c, N);
+    s->vals3 = carve<uint32_t>(c, N);
     s->hist = carve<uint32_t>(c, (size_t)256 * s->tiles);
     s->totals = carve<uint32_t>(c, 256);
     s->box_ord = carve<int>(c, 4 * (size_t)nseg);
@@ -723,6 +819,7 @@ int bh_destroy(bh_system* s) {
     cudaSetDevice(s->device);
     drop_graph(s);
     if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
+    if (s->cond_stream) cudaStreamDestroy(s->cond_stream);
     cudaFree(s->image);
     cudaFree(s->elog);
     cudaFree(s->elog_count);
@@ -1214,7 +1311,7 @@ __global__ void __launch_bounds__(256) k_energy_reduce(int n, Segs segs,
 // positions, a potential walk (FP64 sums per body), then per-system sums of
 // kinetic and potential energy and momentum into s->diag.
 int enqueue_energy(bh_system* s, cudaStream_t st) {
-    int rc = enqueue_front(s, st, true, nullptr);  // tree of the current positions
+    int rc = enqueue_front(s, st, true, nullptr, true);  // tree of the current positions
     if (rc != BH_OK) return rc;
     StepArgs a = step_args(s);
     a.alpha = 0.0f;
@@ -1279,6 +1376,7 @@ int enqueue_energy_log(bh_system* s, cudaStream_t st) {
 
 int build_energy_graph(bh_system* s) {
     if (!s->cap_stream) CK(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
+    if (!s->cond_stream) CK(cudaStreamCreateWithFlags(&s->cond_stream, cudaStreamNonBlocking));
     CK(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal));
     int st = enqueue_energy_log(s, s->cap_stream);
     cudaGraph_t g = nullptr;

@@ -1,0 +1,88 @@
+"""The engine's sort on the GPU: stable passes over the key's high 32 bits,
+then each run of equal high words ordered by the whole key; a run longer than
+256 bodies (bodies packed into one 2^-16 cell of the box) sends the step to
+the full 8-pass sort, behind a conditional node in a graph replay and as
+kernels gated by a device flag in stream order.
+
+Every case compares the sort permutation and the sorted keys with the oracle's
+stable sort, bit for bit, in stream order and as a graph replay, and the tree
+built from them with bh_check."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def bh():
+    from stellarsolver_gb300 import bh as _bh
+
+    _bh.lib()
+    return _bh
+
+
+def clustered(n, packed, seed):
+    """n - packed bodies spread over a few units, plus `packed` bodies 1e-8
+    apart near (1e-3, 2e-3): one 2^-16 cell of the box, distinct keys at 32
+    levels."""
+    rng = np.random.default_rng(seed)
+    x = rng.standard_normal(n).astype(np.float32)
+    y = rng.standard_normal(n).astype(np.float32)
+    i = np.arange(packed)
+    x[:packed] = np.float32(1e-3) + (i * 1e-8).astype(np.float32)
+    y[:packed] = np.float32(2e-3) + ((i % 7) * 1e-8).astype(np.float32)
+    perm = rng.permutation(n)
+    x, y = x[perm], y[perm]
+    vx = np.zeros(n, np.float32)
+    m = np.full(n, 1.0 / n, np.float32)
+    return x, y, vx, vx.copy(), m
+
+
+@pytest.mark.parametrize("graph", [False, True])
+@pytest.mark.parametrize("packed", [0, 200, 600])
+def test_permutation_bit_exact(bh, oracle, graph, packed):
+    n = 8192
+    x, y, vx, vy, m = clustered(n, packed, 11 + packed)
+    box = oracle.bbox(x, y)
+    k = oracle.keys(x, y, box)
+    hi = k >> np.uint64(32)
+    _, runs = np.unique(hi, return_counts=True)
+    if packed == 600:
+        assert runs.max() > 256  # the case that needs the full sort
+    else:
+        assert runs.max() <= 256
+    operm, _ = oracle.sort_keys(k)
+    with bh.BarnesHutSystem(n, mode="plain", eps2=1e-4, timestep=0.0, use_graph=graph) as s:
+        s.set_state(x, y, vx, vy, m)
+        s.step(1)
+        s.sync()
+        assert s.stats()["status"] == 0
+        assert np.array_equal(s.debug("perm"), operm.astype(np.int32))
+        assert np.array_equal(s.debug("keys"), k[operm])
+        assert s.check() == 0
+        # a second step: with timestep 0 the bodies stay put, now in key order,
+        # so the sort of the sorted keys is the identity and the caller index
+        # of every position ("perm", composed over the steps) is unchanged
+        s.step(1)
+        s.sync()
+        assert np.array_equal(s.debug("perm"), operm.astype(np.int32))
+        assert np.array_equal(s.debug("keys"), k[operm])
+        assert s.check() == 0
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_full_sort_then_hybrid_again(bh, oracle, graph):
+    """A packed run in one step, none in the next: the flag and the
+    conditional node are reset by every step."""
+    n = 4096
+    x1, y1, vx, vy, m = clustered(n, 600, 5)
+    x2, y2, _, _, _ = clustered(n, 0, 6)
+    with bh.BarnesHutSystem(n, mode="mixed", eps2=1e-4, timestep=0.0, use_graph=graph) as s:
+        for x, y in ((x1, y1), (x2, y2), (x1, y1)):
+            s.set_state(x, y, vx, vy, m)
+            s.step(1)
+            s.sync()
+            box = oracle.bbox(x, y)
+            operm, _ = oracle.sort_keys(oracle.keys(x, y, box))
+            assert np.array_equal(s.debug("perm"), operm.astype(np.int32))
+            assert s.check() == 0
