@@ -21,13 +21,15 @@ def walk_flops(stats: dict) -> int:
     return FLOPS_P2P * (stats["interactions"] - cells) + FLOPS_P2M * cells
 
 
-def phase_bytes(n: int, mixed: bool, passes: int = 8) -> dict:
-    """Algorithmic bytes per launch of each HBM-bound phase (each array once)."""
+def phase_bytes(n: int, mixed: bool, passes: int = 4) -> dict:
+    """Algorithmic bytes per launch of each HBM-bound phase (each array once).
+    The sort: `passes` radix passes over the key's high word and the run
+    fixup, each one read and one write of (key, index)."""
     lo = 16 * n if mixed else 0
     return {
         "bbox": 8 * n,
         "keys": 20 * n,
-        "sort": 24 * n * passes,  # one read + one write of (key, index) per pass
+        "sort": 24 * n * (passes + 1),
         "reorder": 52 * n + lo,
         "build": 36 * n + 16 * n,  # keys and node arrays, climb records
         "moments": 12 * n + 64 * n + 108 * n,  # bodies, node sums, then walk records
