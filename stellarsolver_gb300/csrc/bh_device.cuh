@@ -338,6 +338,19 @@ static __global__ void __launch_bounds__(kSortThreads) k_radix_scan(uint32_t* __
     if (threadIdx.x == 0) totals[blockIdx.x] = running;
 }
 
+// Lanes of the warp holding the same 8-bit digit as this lane (valid lanes
+// only; an invalid lane gets a mask it does not use): one vote per digit bit.
+__device__ __forceinline__ unsigned digit_peers(uint32_t d, bool valid) {
+    unsigned peers = __ballot_sync(kFull, valid);
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        const bool bit = (d >> b) & 1u;
+        const unsigned v = __ballot_sync(kFull, bit);
+        peers &= bit ? v : ~v;
+    }
+    return peers;
+}
+
 // Stable scatter of one tile: warp w owns 256 consecutive elements, ranks are
 // (earlier rounds of the warp) + (lower lanes with the same digit); warps are
 // then offset by the counts of lower warps.  Elements are staged in shared
@@ -384,7 +397,7 @@ static __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(
         bool valid = idx < n;
         uint32_t d = valid ? radix_digit(k[r], v[r], shift, use_seg, seg_of_pos) : 0u;
         dg[r] = valid ? (int)d : -1;
-        unsigned peers = __match_any_sync(kFull, valid ? d : 256u + lane);
+        unsigned peers = digit_peers(d, valid);
         rank[r] = valid ? s_wh[warp][d] + (uint32_t)__popc(peers & lt) : 0u;
         __syncwarp();
         if (valid && (__ffs(peers) - 1) == lane) s_wh[warp][d] += (uint32_t)__popc(peers);
