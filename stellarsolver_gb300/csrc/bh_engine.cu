@@ -153,12 +153,12 @@ static cudaError_t launch_acc(const StepArgs& a, cudaStream_t st, int part) {
         return launch_pdl(k_walk_acc<false, true, false, 2>, gb, warps * 32, smb, st, sb, a.segs,
                           a.groups2, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt,
                           a.ddt, a.alpha, a.out, a.status, a.inter, a.work + 1, a.fresh,
-                          a.max_stack, (double*)nullptr);
+                          a.max_stack, (double*)nullptr, Frontier{});
     } else {
         return launch_pdl(k_walk_acc<MIXED, false, false, BPL>, grid, warps * 32, smem, st, sh,
                           a.segs, gr, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt,
                           a.ddt, a.alpha, a.out, a.status, a.inter, a.work + 2, a.fresh,
-                          a.max_stack, (double*)nullptr);
+                          a.max_stack, (double*)nullptr, a.frontier);
     }
 }
 
@@ -216,6 +216,8 @@ struct bh_system {
     int *chunk_seg = nullptr, *chunk_begin = nullptr, *chunk_end = nullptr;
     int nchunks = 0;
     int ngroups = 0, ngroups2 = 0;  // groups of 32 and of 64 bodies
+    int nsupers = 0;                // walk super-groups (frontiers), all systems
+    int* sup_off = nullptr;         // [nseg+1] first super-group of each system
     TreePtrs tree{};
     int* counter = nullptr;
     NodeSums sums{};
@@ -227,6 +229,8 @@ struct bh_system {
                            // [6..8]: scratch of bh_energy
     double* diag = nullptr;  // bh_energy: 4 sums per system
     int* fresh = nullptr;  // 1 after bh_set_state: bootstrap |a_old| in the next step
+    int* flist = nullptr;   // walk frontiers, kFrontierCap per super-group (one system only)
+    int* fcount = nullptr;  // frontier entries per super-group, -1: start at the root
     bool fresh_host = false;  // the host's record of *fresh: the bootstrap pass is launched
                               // only in steps that follow bh_set_state
     int seg_passes = 0;
@@ -308,6 +312,8 @@ ssg::StepArgs step_args(bh_system* s) {
     a.warps = normalized_warps(s->p.block_size);
     a.walk_grid_ref = s->walk_grid_ref;
     a.walk_grid_acc = s->walk_grid_acc;
+    // shared walk starts: super-groups of 512 bodies counted from each system's start
+    a.frontier = Frontier{s->flist, s->fcount, s->nseg > 1 ? s->sup_off : nullptr};
     return a;
 }
 
@@ -460,6 +466,12 @@ int enqueue_step(bh_system* s, cudaStream_t st, cudaEvent_t* ev = nullptr, int b
     StepArgs a = step_args(s);
     if (with_boot) CK(launch_walk(a, st, 0));
     CK(mark(7));
+    if (a.mode != BH_MODE_REFERENCE) {
+        constexpr int kFW = 8;  // warps (super-groups) per block
+        const int blocks = (s->nsupers + kFW - 1) / kFW;
+        CK(launch_pdl(k_frontier<kFW>, blocks, kFW * 32, 0, st, a.segs, s->nsupers, a.in.x, a.in.y,
+                      a.recA, a.recC, a.recD, a.bucket, s->flist, s->fcount, a.frontier.sup_off));
+    }
     CK(launch_walk(a, st, 1));
     CK(mark(8));
     return BH_OK;
@@ -637,7 +649,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     s->seg_passes = nseg == 1 ? 0 : (nseg <= 256 ? 1 : 2);
 
     // chunk table for the box reduction and group table for the walks
-    std::vector<int> cseg, cbeg, cend, goff(nseg + 1, 0), goff2(nseg + 1, 0);
+    std::vector<int> cseg, cbeg, cend, goff(nseg + 1, 0), goff2(nseg + 1, 0), soff(nseg + 1, 0);
     for (int sg = 0; sg < nseg; ++sg) {
         for (int b = s->h_off[sg]; b < s->h_off[sg + 1]; b += kBboxChunk) {
             cseg.push_back(sg);
@@ -646,10 +658,12 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
         }
         goff[sg + 1] = goff[sg] + (sizes[sg] + 31) / 32;
         goff2[sg + 1] = goff2[sg] + (sizes[sg] + 63) / 64;
+        soff[sg + 1] = soff[sg] + num_supers(sizes[sg]);
     }
     s->nchunks = (int)cseg.size();
     s->ngroups = goff[nseg];
     s->ngroups2 = goff2[nseg];
+    s->nsupers = soff[nseg];
 
     size_t bytes = 0;
     bytes += 2 * (8 * span<float>(N) + span<int>(N));
@@ -662,6 +676,8 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     bytes += 2 * span<float4>(N) + 2 * span<int4>(N);           // walk records
     bytes += 2 * span<float>(N) + span<int>(1) + span<int>(kStepWords) +
              span<double>(4 * (size_t)nseg) + span<int>(1);
+    bytes += span<int>((size_t)s->nsupers * kFrontierCap) + span<int>((size_t)s->nsupers) +
+             span<int>(nseg + 1);
     cudaError_t e = cudaMalloc(&s->arena, bytes);
     if (e != cudaSuccess) {
         cuda_fail(e, "cudaMalloc(arena)");
@@ -725,6 +741,9 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     }
     s->diag = carve<double>(c, 4 * (size_t)nseg);
     s->fresh = carve<int>(c, 1);
+    s->flist = carve<int>(c, (size_t)s->nsupers * kFrontierCap);
+    s->fcount = carve<int>(c, (size_t)s->nsupers);
+    s->sup_off = carve<int>(c, nseg + 1);
 
     std::vector<int> sop;
     if (nseg > 1) {
@@ -742,6 +761,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     up(s->seg_off, s->h_off.data(), sizeof(int) * (nseg + 1));
     up(s->gseg_off, goff.data(), sizeof(int) * (nseg + 1));
     up(s->gseg_off2, goff2.data(), sizeof(int) * (nseg + 1));
+    up(s->sup_off, soff.data(), sizeof(int) * (nseg + 1));
     if (nseg > 1) up(s->seg_of_pos, sop.data(), sizeof(int) * N);
     up(s->chunk_seg, cseg.data(), sizeof(int) * s->nchunks);
     up(s->chunk_begin, cbeg.data(), sizeof(int) * s->nchunks);
@@ -1327,11 +1347,11 @@ int enqueue_energy(bh_system* s, cudaStream_t st) {
     if (a.bpl == 2)
         k_walk_acc<false, false, true, 2><<<grid, a.warps * 32, smem, st>>>(
             sh, a.segs, gr, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt, 0.0f,
-            a.out, a.status, a.inter, counter, a.fresh, s->work + 7, pot);
+            a.out, a.status, a.inter, counter, a.fresh, s->work + 7, pot, Frontier{});
     else
         k_walk_acc<false, false, true, 1><<<grid, a.warps * 32, smem, st>>>(
             sh, a.segs, gr, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt, 0.0f,
-            a.out, a.status, a.inter, counter, a.fresh, s->work + 7, pot);
+            a.out, a.status, a.inter, counter, a.fresh, s->work + 7, pot, Frontier{});
     CK(cudaGetLastError());
     CK(cudaMemsetAsync(s->diag, 0, sizeof(double) * 4 * s->nseg, st));
     Segs segs{s->nseg, s->seg_off, s->nseg > 1 ? s->seg_of_pos : nullptr};

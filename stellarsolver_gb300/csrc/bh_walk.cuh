@@ -47,7 +47,8 @@ struct Groups {
 };
 
 __device__ __forceinline__ void group_range(const Segs& segs, const Groups& gr, int g, int* lo,
-                                            int* hi, int* gstart, int width = 32) {
+                                            int* hi, int* gstart, int width = 32,
+                                            int* seg = nullptr) {
     int s = 0;
     if (segs.nseg > 1) {
         int a = 0, b = segs.nseg;  // find s with gseg_off[s] <= g < gseg_off[s+1]
@@ -64,6 +65,7 @@ __device__ __forceinline__ void group_range(const Segs& segs, const Groups& gr, 
     *hi = segs.off[s + 1];
     int g0 = segs.nseg > 1 ? __ldg(gr.gseg_off + s) : 0;
     *gstart = *lo + width * (g - g0);
+    if (seg) *seg = s;
 }
 
 // ------------------------------------------------------------------ REFERENCE walk
@@ -347,6 +349,137 @@ __host__ __device__ __forceinline__ int acc_warp_bytes(AccShape sh) {
            ((acc_body_cap(sh.bucket) * 4 + 15) & ~15);
 }
 
+// ------------------------------------------------------------------ shared frontier
+//
+// Consecutive groups open the same nodes near the top of the tree.  For each
+// super-group of 2^kSuperLog2 consecutive bodies of one system (counted from
+// the system's first body, so a system gets the same frontiers alone and in a
+// batch), k_frontier
+// opens once every node that each of its groups would open, and keeps the
+// nodes where that stops: the frontier.  The main accuracy walk of a group
+// starts from its super-group's frontier instead of the root, and tests and
+// decides exactly the nodes it would have tested from the root.
+//
+// A node is opened for all groups when it is not a leaf bucket, all its
+// children are nodes, and the farthest corner of the super-group's box lies
+// within its opening radius: far^2 <= ropen^2.  Every distance a group's rule
+// can use (box lower bound, extreme-body bound, exact minimum) is a float
+// expression of the same form over coordinates inside that box, and is
+// monotone in them, so it is <= far^2 and the group does not accept the node.
+constexpr int kSuperLog2 = 9;         // 512 bodies per super-group
+constexpr int kFrontierCap = 512;     // frontier entries kept per super-group
+constexpr int kFrontierStack = 1024;  // traversal stack per warp of k_frontier
+
+struct Frontier {
+    const int* list = nullptr;     // [super-group][kFrontierCap]
+    const int* count = nullptr;    // [super-group]: frontier entries, -1: start from the root; null: off
+    const int* sup_off = nullptr;  // [nseg+1] first super-group of each system (null: one system)
+};
+
+__host__ __device__ __forceinline__ int num_supers(int n) {
+    return (n + (1 << kSuperLog2) - 1) >> kSuperLog2;
+}
+
+// One warp per super-group (positions x, y in key order; walk records of the
+// systems' trees; sup_off: first super-group of each system, null for one).
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_frontier(Segs segs, int nsupers,
+                                                         const float* __restrict__ x,
+                                                         const float* __restrict__ y,
+                                                         const float4* __restrict__ recA,
+                                                         const int4* __restrict__ recC,
+                                                         const int4* __restrict__ recD, int bucket,
+                                                         int* __restrict__ list,
+                                                         int* __restrict__ count,
+                                                         const int* __restrict__ sup_off) {
+    pdl_wait();
+    __shared__ int s_stack[WARPS][kFrontierStack];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int S = blockIdx.x * WARPS + warp;
+    if (S >= nsupers) return;
+    const unsigned lt = lanemask_lt();
+    int* stack = s_stack[warp];
+    int sg = 0;  // the system: sup_off[sg] <= S < sup_off[sg + 1]
+    if (segs.nseg > 1) {
+        int a = 0, b = segs.nseg;
+        while (b - a > 1) {
+            const int mid = (a + b) >> 1;
+            if (__ldg(sup_off + mid) <= S)
+                a = mid;
+            else
+                b = mid;
+        }
+        sg = a;
+    }
+    const int lo = segs.off[sg], hi = segs.off[sg + 1];
+    const int s0 = lo + ((S - (segs.nseg > 1 ? __ldg(sup_off + sg) : 0)) << kSuperLog2);
+    const int s1 = min(hi, s0 + (1 << kSuperLog2));
+    float bx0 = __int_as_float(0x7f800000), bx1 = -bx0, by0 = bx0, by1 = -bx0;
+    for (int i = s0 + lane; i < s1; i += 32) {
+        const float px = x[i], py = y[i];
+        bx0 = fminf(bx0, px);
+        bx1 = fmaxf(bx1, px);
+        by0 = fminf(by0, py);
+        by1 = fmaxf(by1, py);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        bx0 = fminf(bx0, __shfl_xor_sync(kFull, bx0, o));
+        bx1 = fmaxf(bx1, __shfl_xor_sync(kFull, bx1, o));
+        by0 = fminf(by0, __shfl_xor_sync(kFull, by0, o));
+        by1 = fmaxf(by1, __shfl_xor_sync(kFull, by1, o));
+    }
+    int* out = list + (size_t)S * kFrontierCap;
+    bool bad = hi - lo < 2;  // no tree: the walk has nothing to start from
+    int top = 0, nf = 0, rounds = 0;
+    if (!bad) {
+        if (lane == 0) stack[0] = lo;  // the system's root
+        top = 1;
+    }
+    while (top > 0 && !bad) {
+        const int k = min(32, top);
+        if (++rounds > kMaxWalkRounds || top + 3 * k > kFrontierStack) {
+            bad = true;  // not a valid tree, or too wide a frontier: walks start at the root
+            break;
+        }
+        __syncwarp();
+        const int node = lane < k ? stack[top - 1 - lane] : -1;
+        top -= k;
+        bool open = false;
+        int4 C = make_int4(kNoChild, kNoChild, kNoChild, kNoChild);
+        if (node >= 0) {
+            const float4 A = recA[node];
+            const int4 D = recD[node];
+            const float fx = fmaxf(fabsf(A.x - bx0), fabsf(A.x - bx1));
+            const float fy = fmaxf(fabsf(A.y - by0), fabsf(A.y - by1));
+            if (D.y > bucket && fmaf(fx, fx, fy * fy) <= A.w) {
+                C = recC[node];
+                open = (C.x >= 0 || C.x == kNoChild) && (C.y >= 0 || C.y == kNoChild) &&
+                       (C.z >= 0 || C.z == kNoChild) && (C.w >= 0 || C.w == kNoChild);
+            }
+        }
+        const int nn = open ? (C.x >= 0) + (C.y >= 0) + (C.z >= 0) + (C.w >= 0) : 0;
+        const unsigned fm = __ballot_sync(kFull, node >= 0 && !open);
+        int ntot;
+        const int noff = warp_excl_scan(nn, &ntot);
+        __syncwarp();  // every lane has read its stack slot before children overwrite it
+        if (open) {
+            int* w = stack + top + noff;
+            if (C.x >= 0) *w++ = C.x;
+            if (C.y >= 0) *w++ = C.y;
+            if (C.z >= 0) *w++ = C.z;
+            if (C.w >= 0) *w++ = C.w;
+        }
+        if (node >= 0 && !open) {
+            const int idx = nf + __popc(fm & lt);
+            if (idx < kFrontierCap) out[idx] = node;
+        }
+        top += ntot;
+        nf += __popc(fm);
+    }
+    if (lane == 0) count[S] = (bad || nf > kFrontierCap) ? -1 : nf;
+}
+
 // Below this many lanes the exact group distance is taken cooperatively
 // (each lane measures its own body, then a warp minimum) instead of by a
 // loop over the 32 bodies in every lane.
@@ -373,7 +506,8 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
                                                          int* __restrict__ work,
                                                          int* __restrict__ fresh,
                                                          int* __restrict__ max_stack,
-                                                         double* __restrict__ pot = nullptr) {
+                                                         double* __restrict__ pot,
+                                                         Frontier fr) {
     pdl_wait();
     static_assert(BPL == 1 || BPL == 2, "one or two bodies per lane");
     if (ESTIMATE) {
@@ -404,8 +538,8 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
     unsigned long long my_inter = 0, my_cinter = 0;
 
     for (int g = next_group(work); g < gr.ngroups; g = next_group(work)) {
-        int lo, hi, gstart;
-        group_range(segs, gr, g, &lo, &hi, &gstart, GW);
+        int lo, hi, gstart, sg;
+        group_range(segs, gr, g, &lo, &hi, &gstart, GW, &sg);
         const int cnt = min(GW, hi - gstart);
         // body b of this lane is position gstart + 32 b + lane; invalid ones
         // mirror the group's first body
@@ -488,8 +622,17 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
         bool overflow = false;
         int top = 0, ccnt = 0, bcnt = 0, peak = 0, rounds = 0, tested = 0;
         if (hi - lo >= 2) {
-            if (lane == 0) stack[0] = lo;
-            top = 1;
+            // the super-group's frontier (main pass), else the root
+            const int S = (fr.sup_off ? __ldg(fr.sup_off + sg) : 0) + ((gstart - lo) >> kSuperLog2);
+            const int fc = fr.count ? __ldg(fr.count + S) : -1;
+            if (fc > 0 && 2 * fc <= STACK) {
+                const int* fl = fr.list + (size_t)S * kFrontierCap;
+                for (int e = lane; e < fc; e += 32) stack[e] = __ldg(fl + e);
+                top = fc;
+            } else {
+                if (lane == 0) stack[0] = lo;
+                top = 1;
+            }
         }
         auto add_batch = [&](int b, float bx, float by) {
             if (MIXED) {
