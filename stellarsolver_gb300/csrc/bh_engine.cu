@@ -230,7 +230,7 @@ struct bh_system {
     double* diag = nullptr;  // bh_energy: 4 sums per system
     int* fresh = nullptr;  // 1 after bh_set_state: bootstrap |a_old| in the next step
     int* flist = nullptr;   // walk frontiers, kFrontierCap per super-group (one system only)
-    int* fcount = nullptr;  // frontier entries per super-group, -1: start at the root
+    int2* fcount = nullptr;  // per super-group: (nodes to test, accepted cells); -1: the root
     bool fresh_host = false;  // the host's record of *fresh: the bootstrap pass is launched
                               // only in steps that follow bh_set_state
     int seg_passes = 0;
@@ -470,7 +470,8 @@ int enqueue_step(bh_system* s, cudaStream_t st, cudaEvent_t* ev = nullptr, int b
         constexpr int kFW = 8;  // warps (super-groups) per block
         const int blocks = (s->nsupers + kFW - 1) / kFW;
         CK(launch_pdl(k_frontier<kFW>, blocks, kFW * 32, 0, st, a.segs, s->nsupers, a.in.x, a.in.y,
-                      a.recA, a.recC, a.recD, a.bucket, s->flist, s->fcount, a.frontier.sup_off));
+                      a.in.amag, a.recA, a.recC, a.recD, a.bucket, 32 * a.bpl, a.alpha, s->flist,
+                      s->fcount, a.frontier.sup_off));
     }
     CK(launch_walk(a, st, 1));
     CK(mark(8));
@@ -676,7 +677,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     bytes += 2 * span<float4>(N) + 2 * span<int4>(N);           // walk records
     bytes += 2 * span<float>(N) + span<int>(1) + span<int>(kStepWords) +
              span<double>(4 * (size_t)nseg) + span<int>(1);
-    bytes += span<int>((size_t)s->nsupers * kFrontierCap) + span<int>((size_t)s->nsupers) +
+    bytes += span<int>((size_t)s->nsupers * kFrontierCap) + span<int2>((size_t)s->nsupers) +
              span<int>(nseg + 1);
     cudaError_t e = cudaMalloc(&s->arena, bytes);
     if (e != cudaSuccess) {
@@ -742,7 +743,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     s->diag = carve<double>(c, 4 * (size_t)nseg);
     s->fresh = carve<int>(c, 1);
     s->flist = carve<int>(c, (size_t)s->nsupers * kFrontierCap);
-    s->fcount = carve<int>(c, (size_t)s->nsupers);
+    s->fcount = carve<int2>(c, (size_t)s->nsupers);
     s->sup_off = carve<int>(c, nseg + 1);
 
     std::vector<int> sop;

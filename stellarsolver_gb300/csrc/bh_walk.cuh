@@ -366,13 +366,20 @@ __host__ __device__ __forceinline__ int acc_warp_bytes(AccShape sh) {
 // can use (box lower bound, extreme-body bound, exact minimum) is a float
 // expression of the same form over coordinates inside that box, and is
 // monotone in them, so it is <= far^2 and the group does not accept the node.
+// A frontier node is accepted by all groups when the super-group box's
+// nearest point lies beyond its opening radius and the relative rule holds
+// there with the smallest group scale a_g of the super-group (taken 0.1 %
+// low, for the groups' own float sums); those cells go to every group's cell
+// list untested.  list[S] holds the nodes to test from the front and the
+// accepted cells from the back; count[S] = (nodes to test, accepted cells).
 constexpr int kSuperLog2 = 9;         // 512 bodies per super-group
 constexpr int kFrontierCap = 512;     // frontier entries kept per super-group
 constexpr int kFrontierStack = 1024;  // traversal stack per warp of k_frontier
 
 struct Frontier {
     const int* list = nullptr;     // [super-group][kFrontierCap]
-    const int* count = nullptr;    // [super-group]: frontier entries, -1: start from the root; null: off
+    const int2* count = nullptr;   // [super-group]: (nodes to test, accepted cells); x = -1: start
+                                   // from the root; null: off
     const int* sup_off = nullptr;  // [nseg+1] first super-group of each system (null: one system)
 };
 
@@ -380,17 +387,20 @@ __host__ __device__ __forceinline__ int num_supers(int n) {
     return (n + (1 << kSuperLog2) - 1) >> kSuperLog2;
 }
 
-// One warp per super-group (positions x, y in key order; walk records of the
-// systems' trees; sup_off: first super-group of each system, null for one).
+// One warp per super-group (positions x, y and |a_old| in key order; walk
+// records of the systems' trees; sup_off: first super-group of each system,
+// null for one; gw: bodies per walk group; alpha: the relative rule's).
 template <int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) k_frontier(Segs segs, int nsupers,
                                                          const float* __restrict__ x,
                                                          const float* __restrict__ y,
+                                                         const float* __restrict__ amag,
                                                          const float4* __restrict__ recA,
                                                          const int4* __restrict__ recC,
                                                          const int4* __restrict__ recD, int bucket,
+                                                         int gw, float alpha,
                                                          int* __restrict__ list,
-                                                         int* __restrict__ count,
+                                                         int2* __restrict__ count,
                                                          const int* __restrict__ sup_off) {
     pdl_wait();
     __shared__ int s_stack[WARPS][kFrontierStack];
@@ -477,7 +487,52 @@ __global__ void __launch_bounds__(WARPS * 32) k_frontier(Segs segs, int nsupers,
         top += ntot;
         nf += __popc(fm);
     }
-    if (lane == 0) count[S] = (bad || nf > kFrontierCap) ? -1 : nf;
+    if (bad || nf > kFrontierCap) {
+        if (lane == 0) count[S] = make_int2(-1, 0);
+        return;
+    }
+    // the smallest relative-rule scale over the super-group's groups
+    float aa = __int_as_float(0x7f800000);
+    if (alpha > 0.0f) {
+        for (int g0 = s0 + lane * gw; g0 < s1; g0 += 32 * gw) {
+            const int g1 = min(s1, g0 + gw);
+            float amin = __int_as_float(0x7f800000), asum = 0.0f;
+            for (int i = g0; i < g1; ++i) {
+                const float a = amag[i];
+                amin = fminf(amin, a);
+                asum += a;
+            }
+            aa = fminf(aa, alpha * fmaxf(amin, 0.1f * asum / (float)(g1 - g0)));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) aa = fminf(aa, __shfl_xor_sync(kFull, aa, o));
+        aa *= 0.999f;
+    }
+    // split the frontier: nodes to test to the front, accepted cells to the back
+    __syncwarp();
+    for (int e = lane; e < nf; e += 32) stack[e] = out[e];
+    __syncwarp();
+    int nt = 0, na = 0;
+    for (int base = 0; base < nf; base += 32) {
+        const int e = base + lane;
+        bool acc = false;
+        int node = -1;
+        if (e < nf) {
+            node = stack[e];
+            const float4 A = recA[node];
+            const float ddx = fmaxf(fmaxf(bx0 - A.x, A.x - bx1), 0.0f);
+            const float ddy = fmaxf(fmaxf(by0 - A.y, A.y - by1), 0.0f);
+            const float d2 = fmaf(ddx, ddx, ddy * ddy);
+            if (d2 > A.w)
+                acc = __int_as_float(recD[node].z) <= aa * kRuleMargin * d2 * d2 * sqrt_approx(d2);
+        }
+        const unsigned am = __ballot_sync(kFull, acc), tm = __ballot_sync(kFull, e < nf && !acc);
+        if (acc) out[kFrontierCap - 1 - (na + __popc(am & lt))] = node;
+        if (e < nf && !acc) out[nt + __popc(tm & lt)] = node;
+        na += __popc(am);
+        nt += __popc(tm);
+    }
+    if (lane == 0) count[S] = make_int2(nt, na);
 }
 
 // Below this many lanes the exact group distance is taken cooperatively
@@ -621,14 +676,17 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
         long long entries = 0, centries = 0;
         bool overflow = false;
         int top = 0, ccnt = 0, bcnt = 0, peak = 0, rounds = 0, tested = 0;
+        const int* fl = nullptr;  // the super-group's frontier, if the walk starts there
+        int nacc = 0;             // its cells that every group accepts
         if (hi - lo >= 2) {
             // the super-group's frontier (main pass), else the root
             const int S = (fr.sup_off ? __ldg(fr.sup_off + sg) : 0) + ((gstart - lo) >> kSuperLog2);
-            const int fc = fr.count ? __ldg(fr.count + S) : -1;
-            if (fc > 0 && 2 * fc <= STACK) {
-                const int* fl = fr.list + (size_t)S * kFrontierCap;
-                for (int e = lane; e < fc; e += 32) stack[e] = __ldg(fl + e);
-                top = fc;
+            const int2 fc = fr.count ? fr.count[S] : make_int2(-1, 0);
+            if (fc.x >= 0 && 2 * fc.x <= STACK) {
+                fl = fr.list + (size_t)S * kFrontierCap;
+                for (int e = lane; e < fc.x; e += 32) stack[e] = fl[e];
+                top = fc.x;
+                nacc = fc.y;
             } else {
                 if (lane == 0) stack[0] = lo;
                 top = 1;
@@ -825,6 +883,15 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
             bcnt -= k;
             entries += k;
         };
+        // cells every group of the super-group accepts: straight to the cell list
+        for (int base = 0; base < nacc; base += 32) {
+            const int k = min(32, nacc - base);
+            __syncwarp();
+            if (lane < k) clist[ccnt + lane] = fl[kFrontierCap - 1 - (base + lane)];
+            ccnt += k;
+            __syncwarp();
+            while (ccnt >= 32) flush_cells(32);
+        }
         while (top > 0) {
             if (rounds == kMaxWalkRounds) {  // far beyond any valid tree: report, do not loop
                 if (lane == 0) atomicOr(status, ST_TREE);
