@@ -182,6 +182,8 @@ struct BodyPtrs {
     float *x, *y, *vx, *vy, *m, *xlo, *ylo;  // xlo/ylo may be null
     int* id;
     float* amag;  // |a| of the previous step (accuracy modes; may be null)
+    int* gcost;   // interaction entries of the body's walk group in the previous step
+                  // (accuracy modes; may be null)
 };
 
 // Body i of src becomes body j of dst (the reorder into key order).
@@ -198,6 +200,7 @@ __device__ __forceinline__ void gather_body(int j, uint32_t i, const BodyPtrs& s
         dst.ylo[j] = src.ylo[i];
     }
     if (src.amag) dst.amag[j] = src.amag[i];
+    if (src.gcost) dst.gcost[j] = src.gcost[i];
 }
 
 // ------------------------------------------------------------------ (b1) keys
@@ -248,16 +251,25 @@ static __global__ void k_keys(const float* __restrict__ x, const float* __restri
 }
 
 // k_keys for the engine's step: also clears the moments arrival counters of
-// these positions, the sort's run overflow flag and (block 0) the step's first
-// `nzero` scheduling and statistics words.
+// these positions, the two per-step flags (flags[0..1]) and (block 0) the
+// step's first `nzero` scheduling and statistics words.  zero[0..1] holds the
+// last step's interaction count (entries x bodies, u64): before clearing it,
+// its mean per body, the mean walk-group cost, goes to *mean_cost.
 static __global__ void k_keys_step(const float* __restrict__ x, const float* __restrict__ y, int n,
                                    Segs segs, const int* __restrict__ box_ord,
                                    uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
                                    int* __restrict__ counter, int* __restrict__ zero, int nzero,
-                                   int* __restrict__ sort_flag) {
+                                   int* __restrict__ flags, int* __restrict__ mean_cost) {
     pdl_wait();
-    if (blockIdx.x == 0 && threadIdx.x < nzero) zero[threadIdx.x] = 0;
-    if (blockIdx.x == 0 && threadIdx.x == 0) *sort_flag = 0;
+    if (blockIdx.x == 0) {
+        if (nzero > 0 && threadIdx.x == 0) {
+            const unsigned long long last = *reinterpret_cast<const unsigned long long*>(zero);
+            *mean_cost = (int)min(last / (unsigned long long)n, (unsigned long long)INT_MAX);
+        }
+        __syncthreads();
+        if (threadIdx.x < nzero) zero[threadIdx.x] = 0;
+        if (threadIdx.x < 2) flags[threadIdx.x] = 0;
+    }
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     Box bx = load_box(box_ord, seg_of(segs, i));

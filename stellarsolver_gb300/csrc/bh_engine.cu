@@ -53,13 +53,17 @@ constexpr int kBboxChunk = 8192;
 
 int walk_grid_cap(int device_sms, int blocks_per_sm) { return device_sms * std::max(1, blocks_per_sm); }
 
-// Per-step words: 2 x u64 interaction counts, then bh_system::work (10 ints):
+// Per-step words: 2 x u64 interaction counts, then bh_system::work (12 ints):
 //   work[0..2] walk scheduling, [3..5] walk statistics, [6..8] the energy pass,
-//   [9] the sort's run overflow flag.
+//   [9] the sort's run overflow flag, [10] heavy walk groups listed,
+//   [11] the mean walk-group cost of the last step.
 // A step's key kernel clears the counts and work[0..5] (kStepZero words) and
-// the flag; the energy pass's tree build clears only the flag.
+// the two flags, after saving the mean cost; the energy pass's tree build
+// clears only the flags.
 constexpr int kStepWords = 16;
 constexpr int kWorkSortOverflow = 9;
+constexpr int kWorkHeavy = 10;
+constexpr int kWorkMeanCost = 11;
 constexpr int kStepZero = 4 + 6;
 
 template <typename T>
@@ -153,12 +157,12 @@ static cudaError_t launch_acc(const StepArgs& a, cudaStream_t st, int part) {
         return launch_pdl(k_walk_acc<false, true, false, 2>, gb, warps * 32, smb, st, sb, a.segs,
                           a.groups2, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt,
                           a.ddt, a.alpha, a.out, a.status, a.inter, a.work + 1, a.fresh,
-                          a.max_stack, (double*)nullptr, Frontier{});
+                          a.max_stack, (double*)nullptr, Frontier{}, Heavy{});
     } else {
         return launch_pdl(k_walk_acc<MIXED, false, false, BPL>, grid, warps * 32, smem, st, sh,
                           a.segs, gr, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt,
                           a.ddt, a.alpha, a.out, a.status, a.inter, a.work + 2, a.fresh,
-                          a.max_stack, (double*)nullptr, a.frontier);
+                          a.max_stack, (double*)nullptr, a.frontier, a.heavy);
     }
 }
 
@@ -229,7 +233,8 @@ struct bh_system {
                            // [6..8]: scratch of bh_energy
     double* diag = nullptr;  // bh_energy: 4 sums per system
     int* fresh = nullptr;  // 1 after bh_set_state: bootstrap |a_old| in the next step
-    int* flist = nullptr;   // walk frontiers, kFrontierCap per super-group (one system only)
+    int* flist = nullptr;   // walk frontiers, kFrontierCap per super-group
+    int* heavy = nullptr;   // heavy walk groups of the step (k_frontier)
     int2* fcount = nullptr;  // per super-group: (nodes to test, accepted cells); -1: the root
     bool fresh_host = false;  // the host's record of *fresh: the bootstrap pass is launched
                               // only in steps that follow bh_set_state
@@ -289,9 +294,9 @@ ssg::StepArgs step_args(bh_system* s) {
     const BodyPtrs& c = s->st[0];
     bool mixed = s->p.mode == BH_MODE_MIXED;
     a.in = WalkIn{g.x, g.y, g.vx, g.vy, g.m, mixed ? g.xlo : nullptr, mixed ? g.ylo : nullptr, g.id,
-                  g.amag};
+                  g.amag, g.gcost};
     a.out = WalkOut{c.x, c.y, c.vx, c.vy, c.m, mixed ? c.xlo : nullptr, mixed ? c.ylo : nullptr, c.id,
-                    s->ax, s->ay, c.amag};
+                    s->ax, s->ay, c.amag, c.gcost};
     a.recA = s->rec.A;
     a.recB = s->rec.B;
     a.recC = s->rec.C;
@@ -314,6 +319,7 @@ ssg::StepArgs step_args(bh_system* s) {
     a.walk_grid_acc = s->walk_grid_acc;
     // shared walk starts: super-groups of 512 bodies counted from each system's start
     a.frontier = Frontier{s->flist, s->fcount, s->nseg > 1 ? s->sup_off : nullptr};
+    a.heavy = Heavy{s->heavy, s->work + kWorkHeavy, s->work + kWorkMeanCost};
     return a;
 }
 
@@ -338,7 +344,7 @@ int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev,
     // keys and positions; the moments counters and the step's words cleared
     CK(launch_pdl(k_keys_step, nb, tb, 0, st, cur.x, cur.y, n, segs, s->box_ord, s->keys, s->vals,
                   s->counter, reinterpret_cast<int*>(s->inter), keep_stats ? 0 : kStepZero,
-                  s->work + kWorkSortOverflow));
+                  s->work + kWorkSortOverflow, s->work + kWorkMeanCost));
     CK(mark(2));
 
     // Sort (stable, by key, then by system): LSD passes over the key's high 32
@@ -438,7 +444,10 @@ int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev,
         src.xlo = src.ylo = nullptr;
         dst.xlo = dst.ylo = nullptr;
     }
-    if (!accuracy) src.amag = dst.amag = nullptr;
+    if (!accuracy) {
+        src.amag = dst.amag = nullptr;
+        src.gcost = dst.gcost = nullptr;
+    }
     CK(launch_pdl(k_gather, nb, tb, 0, st, n, va, src, dst));
     CK(mark(4));
     CK(launch_pdl(k_build, nb, tb, 0, st, ka, n, segs, s->tree, s->status));
@@ -471,7 +480,9 @@ int enqueue_step(bh_system* s, cudaStream_t st, cudaEvent_t* ev = nullptr, int b
         const int blocks = (s->nsupers + kFW - 1) / kFW;
         CK(launch_pdl(k_frontier<kFW>, blocks, kFW * 32, 0, st, a.segs, s->nsupers, a.in.x, a.in.y,
                       a.in.amag, a.recA, a.recC, a.recD, a.bucket, 32 * a.bpl, a.alpha, s->flist,
-                      s->fcount, a.frontier.sup_off));
+                      s->fcount, a.frontier.sup_off, a.in.gcost,
+                      s->nseg > 1 ? (a.bpl == 2 ? s->gseg_off2 : s->gseg_off) : nullptr,
+                      s->work + kWorkMeanCost, s->heavy, s->work + kWorkHeavy));
     }
     CK(launch_walk(a, st, 1));
     CK(mark(8));
@@ -571,7 +582,7 @@ int build_graph(bh_system* s, int boot) {
 // State of a freshly loaded system: caller order, zero position tails and
 // accelerations, status cleared, bootstrap pass requested.
 __global__ void k_state_init(int n, int* id, float* xlo, float* ylo, float* ax, float* ay,
-                             float* amag, int* status, int* fresh) {
+                             float* amag, int* gcost, int* status, int* fresh) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
         id[i] = i;
@@ -580,6 +591,7 @@ __global__ void k_state_init(int n, int* id, float* xlo, float* ylo, float* ax, 
         ax[i] = 0.0f;
         ay[i] = 0.0f;
         amag[i] = 0.0f;
+        gcost[i] = 0;
     }
     if (i == 0) {
         *status = 0;
@@ -667,7 +679,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     s->nsupers = soff[nseg];
 
     size_t bytes = 0;
-    bytes += 2 * (8 * span<float>(N) + span<int>(N));
+    bytes += 2 * (8 * span<float>(N) + 2 * span<int>(N));
     bytes += 3 * span<uint64_t>(N) + 3 * span<uint32_t>(N);
     bytes += span<uint32_t>((size_t)256 * s->tiles) + span<uint32_t>(256);
     bytes += span<int>(4 * (size_t)nseg) + 3 * span<int>(nseg + 1) + span<int>(N);
@@ -678,7 +690,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     bytes += 2 * span<float>(N) + span<int>(1) + span<int>(kStepWords) +
              span<double>(4 * (size_t)nseg) + span<int>(1);
     bytes += span<int>((size_t)s->nsupers * kFrontierCap) + span<int2>((size_t)s->nsupers) +
-             span<int>(nseg + 1);
+             span<int>(nseg + 1) + span<int>((size_t)s->ngroups);
     cudaError_t e = cudaMalloc(&s->arena, bytes);
     if (e != cudaSuccess) {
         cuda_fail(e, "cudaMalloc(arena)");
@@ -698,6 +710,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
         b.ylo = carve<float>(c, N);
         b.id = carve<int>(c, N);
         b.amag = carve<float>(c, N);
+        b.gcost = carve<int>(c, N);
     }
     s->keys = carve<uint64_t>(c, N);
     s->keys_alt = carve<uint64_t>(c, N);
@@ -745,6 +758,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     s->flist = carve<int>(c, (size_t)s->nsupers * kFrontierCap);
     s->fcount = carve<int2>(c, (size_t)s->nsupers);
     s->sup_off = carve<int>(c, nseg + 1);
+    s->heavy = carve<int>(c, (size_t)s->ngroups);
 
     std::vector<int> sop;
     if (nseg > 1) {
@@ -884,7 +898,7 @@ int bh_set_state(bh_system* s, const float* x, const float* y, const float* vx, 
     CK(cudaMemcpyAsync(c.vy, vy, b, cudaMemcpyDefault, st));
     CK(cudaMemcpyAsync(c.m, mass, b, cudaMemcpyDefault, st));
     k_state_init<<<(s->n + 255) / 256, 256, 0, st>>>(s->n, c.id, c.xlo, c.ylo, s->ax, s->ay,
-                                                     c.amag, s->status, s->fresh);
+                                                     c.amag, c.gcost, s->status, s->fresh);
     CK(cudaGetLastError());
     s->have_state = true;
     s->caller_order = true;
@@ -1348,11 +1362,11 @@ int enqueue_energy(bh_system* s, cudaStream_t st) {
     if (a.bpl == 2)
         k_walk_acc<false, false, true, 2><<<grid, a.warps * 32, smem, st>>>(
             sh, a.segs, gr, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt, 0.0f,
-            a.out, a.status, a.inter, counter, a.fresh, s->work + 7, pot, Frontier{});
+            a.out, a.status, a.inter, counter, a.fresh, s->work + 7, pot, Frontier{}, Heavy{});
     else
         k_walk_acc<false, false, true, 1><<<grid, a.warps * 32, smem, st>>>(
             sh, a.segs, gr, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt, 0.0f,
-            a.out, a.status, a.inter, counter, a.fresh, s->work + 7, pot, Frontier{});
+            a.out, a.status, a.inter, counter, a.fresh, s->work + 7, pot, Frontier{}, Heavy{});
     CK(cudaGetLastError());
     CK(cudaMemsetAsync(s->diag, 0, sizeof(double) * 4 * s->nseg, st));
     Segs segs{s->nseg, s->seg_off, s->nseg > 1 ? s->seg_of_pos : nullptr};

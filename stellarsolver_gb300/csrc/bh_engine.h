@@ -34,7 +34,8 @@ struct StepArgs {
     int bucket, stack, warps;  // accuracy-walk shape: leaf bucket, stack entries, warps/block
     int bpl;                   // accuracy walk: bodies per lane (1 or 2)
     int walk_grid_ref, walk_grid_acc;
-    Frontier frontier;  // shared walk starts (main accuracy pass of one system)
+    Frontier frontier;  // shared walk starts (main accuracy pass)
+    Heavy heavy;        // heavy walk groups first (main accuracy pass)
 };
 
 cudaError_t launch_walk(const StepArgs& a, cudaStream_t st, int part);

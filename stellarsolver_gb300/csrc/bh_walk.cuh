@@ -25,14 +25,29 @@ namespace ssg {
 struct WalkIn {
     const float *x, *y, *vx, *vy, *m, *xlo, *ylo;
     const int* id;
-    float* amag;  // |a| of the previous step; written by the bootstrap pass
+    float* amag;       // |a| of the previous step; written by the bootstrap pass
+    const int* gcost;  // the previous step's walk-group cost of each body (accuracy modes)
 };
 struct WalkOut {
     float *x, *y, *vx, *vy, *m, *xlo, *ylo;
     int* id;
     float *ax, *ay;
     float* amag;  // |a| of this step, for the next step's relative rule
+    int* gcost;   // this step's walk-group cost (interaction entries) of each body
 };
+
+// Heaviest groups first.  A group whose first body's previous-step group cost
+// is at least 1.5x the previous step's mean (mean > 0) is heavy: k_frontier
+// lists the heavy groups, and the main walk takes them before the others,
+// so that the longest groups do not start late and leave the SMs idle.
+struct Heavy {
+    const int* list = nullptr;   // heavy group indices, in any order
+    const int* count = nullptr;  // their number; null: no reordering
+    const int* mean = nullptr;   // the previous step's mean group cost
+};
+__device__ __forceinline__ bool heavy_group(const int* __restrict__ gcost, int gstart, int mean) {
+    return mean > 0 && 2ll * __ldg(gcost + gstart) >= 3ll * mean;
+}
 
 // Next group for this warp: dynamic scheduling, groups differ ~10x in cost.
 __device__ __forceinline__ int next_group(int* work) {
@@ -401,7 +416,12 @@ __global__ void __launch_bounds__(WARPS * 32) k_frontier(Segs segs, int nsupers,
                                                          int gw, float alpha,
                                                          int* __restrict__ list,
                                                          int2* __restrict__ count,
-                                                         const int* __restrict__ sup_off) {
+                                                         const int* __restrict__ sup_off,
+                                                         const int* __restrict__ gcost,
+                                                         const int* __restrict__ gseg_off,
+                                                         const int* __restrict__ mean_cost,
+                                                         int* __restrict__ heavy,
+                                                         int* __restrict__ nheavy) {
     pdl_wait();
     __shared__ int s_stack[WARPS][kFrontierStack];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -424,6 +444,19 @@ __global__ void __launch_bounds__(WARPS * 32) k_frontier(Segs segs, int nsupers,
     const int lo = segs.off[sg], hi = segs.off[sg + 1];
     const int s0 = lo + ((S - (segs.nseg > 1 ? __ldg(sup_off + sg) : 0)) << kSuperLog2);
     const int s1 = min(hi, s0 + (1 << kSuperLog2));
+    {
+        // this super-group's heavy walk groups (at most 32: gw >= 32 bodies)
+        const int mean = *mean_cost;
+        const int gs = s0 + lane * gw;
+        const bool h = gs < s1 && heavy_group(gcost, gs, mean);
+        const unsigned hm = __ballot_sync(kFull, h);
+        int base = 0;
+        if (lane == 0 && hm) base = atomicAdd(nheavy, __popc(hm));
+        base = __shfl_sync(kFull, base, 0);
+        if (h)
+            heavy[base + __popc(hm & lt)] =
+                (segs.nseg > 1 ? __ldg(gseg_off + sg) : 0) + (gs - lo) / gw;
+    }
     float bx0 = __int_as_float(0x7f800000), bx1 = -bx0, by0 = bx0, by1 = -bx0;
     for (int i = s0 + lane; i < s1; i += 32) {
         const float px = x[i], py = y[i];
@@ -562,7 +595,7 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
                                                          int* __restrict__ fresh,
                                                          int* __restrict__ max_stack,
                                                          double* __restrict__ pot,
-                                                         Frontier fr) {
+                                                         Frontier fr, Heavy hv) {
     pdl_wait();
     static_assert(BPL == 1 || BPL == 2, "one or two bodies per lane");
     if (ESTIMATE) {
@@ -592,9 +625,14 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
     int* blist = stack + ((STACK + 3) & ~3);
     unsigned long long my_inter = 0, my_cinter = 0;
 
-    for (int g = next_group(work); g < gr.ngroups; g = next_group(work)) {
+    // heavy groups first (hv.count set: the main pass), then the others in order
+    const int nh = hv.count ? *hv.count : 0;
+    const int mean = hv.mean ? *hv.mean : 0;
+    for (int c = next_group(work); c < nh + gr.ngroups; c = next_group(work)) {
+        const int g = c < nh ? hv.list[c] : c - nh;
         int lo, hi, gstart, sg;
         group_range(segs, gr, g, &lo, &hi, &gstart, GW, &sg);
+        if (c >= nh && nh > 0 && heavy_group(in.gcost, gstart, mean)) continue;  // done first
         const int cnt = min(GW, hi - gstart);
         // body b of this lane is position gstart + 32 b + lane; invalid ones
         // mirror the group's first body
@@ -1080,6 +1118,7 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
             out.ax[jb] = gax;
             out.ay[jb] = gay;
             out.amag[jb] = sqrtf(gax * gax + gay * gay);
+            out.gcost[jb] = (int)min(entries, 1ll << 30);  // next step's heavy-group estimate
         }
     }
     if (!ESTIMATE && !DIAG && lane == 0 && my_inter) {
