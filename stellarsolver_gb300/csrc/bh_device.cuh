@@ -252,23 +252,27 @@ static __global__ void k_keys(const float* __restrict__ x, const float* __restri
 
 // k_keys for the engine's step: also clears the moments arrival counters of
 // these positions, the two per-step flags (flags[0..1]) and (block 0) the
-// step's first `nzero` scheduling and statistics words.  zero[0..1] holds the
-// last step's interaction count (entries x bodies, u64): before clearing it,
-// its mean per body, the mean walk-group cost, goes to *mean_cost.
+// step's first `nzero` scheduling and statistics words.  With nzero > 0 (a
+// step, not the energy pass) each system's walk cost of the last step
+// (seg_cost, entries x bodies) becomes its mean walk-group cost (mean_cost)
+// and is cleared.
 static __global__ void k_keys_step(const float* __restrict__ x, const float* __restrict__ y, int n,
                                    Segs segs, const int* __restrict__ box_ord,
                                    uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
                                    int* __restrict__ counter, int* __restrict__ zero, int nzero,
-                                   int* __restrict__ flags, int* __restrict__ mean_cost) {
+                                   int* __restrict__ flags,
+                                   unsigned long long* __restrict__ seg_cost,
+                                   int* __restrict__ mean_cost) {
     pdl_wait();
     if (blockIdx.x == 0) {
-        if (nzero > 0 && threadIdx.x == 0) {
-            const unsigned long long last = *reinterpret_cast<const unsigned long long*>(zero);
-            *mean_cost = (int)min(last / (unsigned long long)n, (unsigned long long)INT_MAX);
-        }
-        __syncthreads();
         if (threadIdx.x < nzero) zero[threadIdx.x] = 0;
         if (threadIdx.x < 2) flags[threadIdx.x] = 0;
+    }
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nzero > 0 && t < segs.nseg) {
+        const unsigned long long size = (unsigned long long)(segs.off[t + 1] - segs.off[t]);
+        mean_cost[t] = (int)min(seg_cost[t] / size, (unsigned long long)INT_MAX);
+        seg_cost[t] = 0ull;
     }
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;

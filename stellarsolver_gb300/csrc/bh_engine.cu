@@ -53,17 +53,14 @@ constexpr int kBboxChunk = 8192;
 
 int walk_grid_cap(int device_sms, int blocks_per_sm) { return device_sms * std::max(1, blocks_per_sm); }
 
-// Per-step words: 2 x u64 interaction counts, then bh_system::work (12 ints):
+// Per-step words: 2 x u64 interaction counts, then bh_system::work (11 ints):
 //   work[0..2] walk scheduling, [3..5] walk statistics, [6..8] the energy pass,
-//   [9] the sort's run overflow flag, [10] heavy walk groups listed,
-//   [11] the mean walk-group cost of the last step.
+//   [9] the sort's run overflow flag, [10] heavy walk groups listed.
 // A step's key kernel clears the counts and work[0..5] (kStepZero words) and
-// the two flags, after saving the mean cost; the energy pass's tree build
-// clears only the flags.
+// the two flags; the energy pass's tree build clears only the flags.
 constexpr int kStepWords = 16;
 constexpr int kWorkSortOverflow = 9;
 constexpr int kWorkHeavy = 10;
-constexpr int kWorkMeanCost = 11;
 constexpr int kStepZero = 4 + 6;
 
 template <typename T>
@@ -235,6 +232,8 @@ struct bh_system {
     int* fresh = nullptr;  // 1 after bh_set_state: bootstrap |a_old| in the next step
     int* flist = nullptr;   // walk frontiers, kFrontierCap per super-group
     int* heavy = nullptr;   // heavy walk groups of the step (k_frontier)
+    unsigned long long* seg_cost = nullptr;  // [nseg] walk cost of each system, this step
+    int* mean_cost = nullptr;                // [nseg] mean walk-group cost, last step
     int2* fcount = nullptr;  // per super-group: (nodes to test, accepted cells); -1: the root
     bool fresh_host = false;  // the host's record of *fresh: the bootstrap pass is launched
                               // only in steps that follow bh_set_state
@@ -319,7 +318,7 @@ ssg::StepArgs step_args(bh_system* s) {
     a.walk_grid_acc = s->walk_grid_acc;
     // shared walk starts: super-groups of 512 bodies counted from each system's start
     a.frontier = Frontier{s->flist, s->fcount, s->nseg > 1 ? s->sup_off : nullptr};
-    a.heavy = Heavy{s->heavy, s->work + kWorkHeavy, s->work + kWorkMeanCost};
+    a.heavy = Heavy{s->heavy, s->work + kWorkHeavy, s->mean_cost, s->seg_cost};
     return a;
 }
 
@@ -344,7 +343,7 @@ int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev,
     // keys and positions; the moments counters and the step's words cleared
     CK(launch_pdl(k_keys_step, nb, tb, 0, st, cur.x, cur.y, n, segs, s->box_ord, s->keys, s->vals,
                   s->counter, reinterpret_cast<int*>(s->inter), keep_stats ? 0 : kStepZero,
-                  s->work + kWorkSortOverflow, s->work + kWorkMeanCost));
+                  s->work + kWorkSortOverflow, s->seg_cost, s->mean_cost));
     CK(mark(2));
 
     // Sort (stable, by key, then by system): LSD passes over the key's high 32
@@ -482,7 +481,7 @@ int enqueue_step(bh_system* s, cudaStream_t st, cudaEvent_t* ev = nullptr, int b
                       a.in.amag, a.recA, a.recC, a.recD, a.bucket, 32 * a.bpl, a.alpha, s->flist,
                       s->fcount, a.frontier.sup_off, a.in.gcost,
                       s->nseg > 1 ? (a.bpl == 2 ? s->gseg_off2 : s->gseg_off) : nullptr,
-                      s->work + kWorkMeanCost, s->heavy, s->work + kWorkHeavy));
+                      s->mean_cost, s->heavy, s->work + kWorkHeavy));
     }
     CK(launch_walk(a, st, 1));
     CK(mark(8));
@@ -690,7 +689,8 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     bytes += 2 * span<float>(N) + span<int>(1) + span<int>(kStepWords) +
              span<double>(4 * (size_t)nseg) + span<int>(1);
     bytes += span<int>((size_t)s->nsupers * kFrontierCap) + span<int2>((size_t)s->nsupers) +
-             span<int>(nseg + 1) + span<int>((size_t)s->ngroups);
+             span<int>(nseg + 1) + span<int>((size_t)s->ngroups) +
+             span<unsigned long long>(nseg) + span<int>(nseg);
     cudaError_t e = cudaMalloc(&s->arena, bytes);
     if (e != cudaSuccess) {
         cuda_fail(e, "cudaMalloc(arena)");
@@ -759,6 +759,8 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     s->fcount = carve<int2>(c, (size_t)s->nsupers);
     s->sup_off = carve<int>(c, nseg + 1);
     s->heavy = carve<int>(c, (size_t)s->ngroups);
+    s->seg_cost = carve<unsigned long long>(c, nseg);
+    s->mean_cost = carve<int>(c, nseg);
 
     std::vector<int> sop;
     if (nseg > 1) {
@@ -783,6 +785,8 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     up(s->chunk_end, cend.data(), sizeof(int) * s->nchunks);
     if (rc == BH_OK && cudaMemset(s->status, 0, sizeof(int)) != cudaSuccess) rc = BH_ERR_CUDA;
     if (rc == BH_OK && cudaMemset(s->fresh, 0, sizeof(int)) != cudaSuccess) rc = BH_ERR_CUDA;
+    if (rc == BH_OK && cudaMemset(s->seg_cost, 0, sizeof(unsigned long long) * nseg) != cudaSuccess)
+        rc = BH_ERR_CUDA;
     if (rc == BH_OK) {
         cudaError_t ea = init_walk_attributes();
         if (ea != cudaSuccess) rc = cuda_fail(ea, "cudaFuncSetAttribute(walk)");

@@ -37,13 +37,15 @@ struct WalkOut {
 };
 
 // Heaviest groups first.  A group whose first body's previous-step group cost
-// is at least 1.5x the previous step's mean (mean > 0) is heavy: k_frontier
-// lists the heavy groups, and the main walk takes them before the others,
-// so that the longest groups do not start late and leave the SMs idle.
+// is at least 1.5x its system's mean of the previous step (mean > 0) is
+// heavy: k_frontier lists the heavy groups, and the main walk takes them
+// before the others, so that the longest groups do not start late and leave
+// the SMs idle.
 struct Heavy {
-    const int* list = nullptr;   // heavy group indices, in any order
-    const int* count = nullptr;  // their number; null: no reordering
-    const int* mean = nullptr;   // the previous step's mean group cost
+    const int* list = nullptr;           // heavy group indices, in any order
+    const int* count = nullptr;          // their number; null: no reordering
+    const int* mean = nullptr;           // [nseg] each system's mean group cost, last step
+    unsigned long long* cost = nullptr;  // [nseg] this step's cost (entries x bodies)
 };
 __device__ __forceinline__ bool heavy_group(const int* __restrict__ gcost, int gstart, int mean) {
     return mean > 0 && 2ll * __ldg(gcost + gstart) >= 3ll * mean;
@@ -446,7 +448,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_frontier(Segs segs, int nsupers,
     const int s1 = min(hi, s0 + (1 << kSuperLog2));
     {
         // this super-group's heavy walk groups (at most 32: gw >= 32 bodies)
-        const int mean = *mean_cost;
+        const int mean = mean_cost[sg];
         const int gs = s0 + lane * gw;
         const bool h = gs < s1 && heavy_group(gcost, gs, mean);
         const unsigned hm = __ballot_sync(kFull, h);
@@ -627,12 +629,11 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
 
     // heavy groups first (hv.count set: the main pass), then the others in order
     const int nh = hv.count ? *hv.count : 0;
-    const int mean = hv.mean ? *hv.mean : 0;
     for (int c = next_group(work); c < nh + gr.ngroups; c = next_group(work)) {
         const int g = c < nh ? hv.list[c] : c - nh;
         int lo, hi, gstart, sg;
         group_range(segs, gr, g, &lo, &hi, &gstart, GW, &sg);
-        if (c >= nh && nh > 0 && heavy_group(in.gcost, gstart, mean)) continue;  // done first
+        if (c >= nh && nh > 0 && heavy_group(in.gcost, gstart, hv.mean[sg])) continue;  // done first
         const int cnt = min(GW, hi - gstart);
         // body b of this lane is position gstart + 32 b + lane; invalid ones
         // mirror the group's first body
@@ -1074,6 +1075,7 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
         if (!ESTIMATE && !DIAG) {
             my_inter += (unsigned long long)(entries * cnt);
             my_cinter += (unsigned long long)(centries * cnt);
+            if (hv.cost && lane == 0) atomicAdd(hv.cost + sg, (unsigned long long)(entries * cnt));
         }
 #pragma unroll
         for (int b = 0; b < BPL; ++b) {
