@@ -312,12 +312,13 @@ __device__ __forceinline__ void p2m_pair(const float4 xy, const float4 mh, const
     const float2 txx = make_float2(t01.x, t01.y), txy = make_float2(t01.z, t01.w);
     const float2 tdx = __ffma2_rn(txx, dx, __fmul2_rn(txy, dy));  // -(T d).x
     const float2 tdy = __ffma2_rn(txy, dx, __fmul2_rn(t11, dy));  // -(T d).y
-    const float2 dtd = __ffma2_rn(dx, tdx, __fmul2_rn(dy, tdy));  // -d.T.d
-    const float2 t = __ffma2_rn(__fmul2_rn(make_float2(-2.5f, -2.5f), dtd), r2,
-                                make_float2(mh.z, mh.w));         // 2.5 d.T.d / u - h
+    const float2 qx = __fmul2_rn(r2, tdx), qy = __fmul2_rn(r2, tdy);  // -(T d) / u
+    const float2 w = __ffma2_rn(dx, qx, __fmul2_rn(dy, qy));           // -d.T.d / u
+    const float2 t = __ffma2_rn(make_float2(-2.5f, -2.5f), w,
+                                make_float2(mh.z, mh.w));              // 2.5 d.T.d / u - h
     const float2 coef = __ffma2_rn(r2, t, make_float2(mh.x, mh.y));
-    const float2 fx = __ffma2_rn(coef, dx, __fmul2_rn(r2, tdx));
-    const float2 fy = __ffma2_rn(coef, dy, __fmul2_rn(r2, tdy));
+    const float2 fx = __ffma2_rn(coef, dx, qx);
+    const float2 fy = __ffma2_rn(coef, dy, qy);
     ax = __ffma2_rn(r3, fx, ax);
     ay = __ffma2_rn(r3, fy, ay);
 }
