@@ -157,6 +157,29 @@ def test_walk_matches_cpu_restatement(bh, oracle, bpl):
     assert np.median(d) <= 1e-6 * rms, np.median(d) / rms
 
 
+@pytest.mark.parametrize("mode", ["plain", "mixed"])
+def test_graph_replay_is_bitwise_identical(bh, mode):
+    """Six steps as graph replays and in stream order give identical states and
+    interaction counts.  From the second step on, the walk starts from shared
+    frontiers and takes the heavy groups first; the sort's fallback is a
+    conditional node in the graph and flag-gated kernels in stream order.
+    None of this may change a result."""
+    from stellarsolver_gb300 import models
+
+    x, y, vx, vy, m = models.plummer(1 << 16, 77)
+    outs = []
+    for graph in (False, True):
+        with bh.BarnesHutSystem(len(x), mode=mode, theta=0.5, eps2=1e-4, timestep=1e-4,
+                                use_graph=graph) as s:
+            s.set_state(x, y, vx, vy, m)
+            s.step(6)
+            s.sync()
+            outs.append((s.get_state(), s.stats()["interactions"]))
+    assert outs[0][1] == outs[1][1]
+    for k in ("x", "y", "vx", "vy"):
+        assert np.array_equal(outs[0][0][k], outs[1][0][k]), k
+
+
 def test_set_accel_skips_bootstrap(bh):
     """Loading the previous accelerations gives the same step as the bootstrap."""
     from stellarsolver_gb300 import models
