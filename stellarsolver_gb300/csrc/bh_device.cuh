@@ -680,11 +680,25 @@ __device__ __forceinline__ ChildVals combine_node(int p, const ChildVals& a, con
 //
 // A block owns kMomentsThreads consecutive leaves.  A node whose body range
 // lies inside them is reached only by threads of that block: its arrival
-// counter lives in shared memory and block-scope fences order the child data.
+// counter lives in shared memory, taken with one block-scope acquire-release
+// atomic that orders the child data.
 // Only nodes that span two blocks' leaves use a global counter, taken with one
 // acquire-release atomic: its release publishes the node this thread wrote,
 // its acquire makes the sibling's sums visible to the loads that follow.  The
 // parent's climb record is loaded while the counter is taken.
+// Block-scope acquire-release add on a shared-memory counter: the one atomic
+// orders this thread's earlier global writes before the later reads of the
+// thread that arrives second, within one block.
+__device__ __forceinline__ int atomic_add_acq_rel_cta_shared(int* p, int v) {
+    int old;
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("atom.acq_rel.cta.shared::cta.add.s32 %0, [%1], %2;"
+                 : "=r"(old)
+                 : "r"(a), "r"(v)
+                 : "memory");
+    return old;
+}
+
 __device__ __forceinline__ int atomic_add_acq_rel_gpu(int* p, int v) {
     int old;
     asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;"
@@ -724,9 +738,7 @@ static __global__ void __launch_bounds__(kMomentsThreads) k_moments(int n, int a
         int4 TN = make_int4(0, 0, -1, 0);
         if (T.z >= 0) TN = climb[T.z];
         if (T.w & 1) {
-            __threadfence_block();
-            if (atomicAdd(s_cnt + (p - c0), 1) == 0) return;
-            __threadfence_block();
+            if (atomic_add_acq_rel_cta_shared(s_cnt + (p - c0), 1) == 0) return;
         } else {
             if (atomic_add_acq_rel_gpu(counter + p, 1) == 0) return;
         }
