@@ -11,11 +11,13 @@
 //              pushed on the warp's stack.  The interaction set is the
 //              reference's; only the summation order differs.
 // k_walk_acc   PLAIN / MIXED modes.  Lanes test up to 32 stack nodes at once
-//              against the group's bounding box (accept iff
-//              dist(COM, box)^2 > (bmax/theta)^2); accepted cells and the
-//              bodies of opened leaves go to shared-memory lists which are
-//              flushed 32 entries at a time as dense quadrupole / body-body
-//              interactions (every lane computes its body against every entry).
+//              against the group (geometric rule on the group's nearest body,
+//              relative rule on its |a_old|); accepted cells and the bodies of
+//              opened leaves go to shared-memory lists which are flushed 32
+//              entries at a time as dense quadrupole / body-body interactions
+//              (every lane computes its body against every entry).  The main
+//              pass starts each group from its super-group's shared frontier
+//              (k_frontier) and hands out the heaviest groups first.
 #pragma once
 
 #include "bh_device.cuh"
