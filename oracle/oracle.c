@@ -559,20 +559,12 @@ static void p2p_cpu(float bx, float by, float bm, float px, float py, float eps2
     *ay += f * dy;
 }
 
-int64_t orc_walk_acc(int n, const float* sx, const float* sy, const float* sm,
-                     const uint64_t* skeys, const int32_t* left, const int32_t* right,
-                     const int32_t* split, const int32_t* first, const int32_t* last,
-                     const int32_t* qchild, const float* box, float theta, float eps2, float G,
-                     int bucket, float alpha, const float* aold, int quadrupole, int group,
-                     float* sax, float* say) {
-    if (n < 2) {
-        for (int i = 0; i < n; ++i) sax[i] = say[i] = 0.0f;
-        return 0;
-    }
-    Mom* mom = (Mom*)malloc(sizeof(Mom) * (size_t)(n - 1));
-    acc_moments(0, left, right, sx, sy, sm, mom);
-    float* ropen2 = (float*)malloc(sizeof(float) * (size_t)(n - 1));
-    float* qerr = (float*)malloc(sizeof(float) * (size_t)(n - 1));
+/* Opening radius^2 and relative-rule numerator G M l^3 of every node: l the
+ * node's cell side (the larger box side halved per level), ropen = l / theta +
+ * |COM - cell centre| (the engine's k_records). */
+static void open_radii(int n, const Mom* mom, const uint64_t* skeys, const int32_t* split,
+                       const int32_t* first, const float* box, float theta, float G,
+                       float* ropen2, float* qerr) {
     for (int i = 0; i < n - 1; ++i) {
         int L = split[i] >> 1;
         if (L > 32) L = 32;
@@ -592,6 +584,23 @@ int64_t orc_walk_acc(int n, const float* sx, const float* sy, const float* sm,
         ropen2[i] = (float)(r * r);
         qerr[i] = (float)((double)G * mom[i].m * l * l * l);
     }
+}
+
+int64_t orc_walk_acc(int n, const float* sx, const float* sy, const float* sm,
+                     const uint64_t* skeys, const int32_t* left, const int32_t* right,
+                     const int32_t* split, const int32_t* first, const int32_t* last,
+                     const int32_t* qchild, const float* box, float theta, float eps2, float G,
+                     int bucket, float alpha, const float* aold, int quadrupole, int group,
+                     float* sax, float* say) {
+    if (n < 2) {
+        for (int i = 0; i < n; ++i) sax[i] = say[i] = 0.0f;
+        return 0;
+    }
+    Mom* mom = (Mom*)malloc(sizeof(Mom) * (size_t)(n - 1));
+    acc_moments(0, left, right, sx, sy, sm, mom);
+    float* ropen2 = (float*)malloc(sizeof(float) * (size_t)(n - 1));
+    float* qerr = (float*)malloc(sizeof(float) * (size_t)(n - 1));
+    open_radii(n, mom, skeys, split, first, box, theta, G, ropen2, qerr);
     const int relative = aold != NULL && alpha > 0.0f;
     if (group != 64) group = 32;  /* bodies per group: 32, or 64 (two per lane) */
     int groups = (n + group - 1) / group;
@@ -699,6 +708,232 @@ int64_t orc_walk_acc(int n, const float* sx, const float* sy, const float* sm,
     free(ropen2);
     free(qerr);
     return total;
+}
+
+/* ------------------------------------------------------------------ shared frontiers
+ * The engine's k_frontier (bh_walk.cuh) and the walk's frontier start,
+ * restated to check that a group starting from its super-group's frontier
+ * accepts exactly the cells, and interacts exactly the bodies, that it would
+ * from the root.  Decisions are orc_walk_acc's: group box, then the exact
+ * minimum over the group when the box is inconclusive; relative rule
+ * qerr <= aa d^4 sqrt(d). */
+typedef struct {
+    const Mom* mom;
+    const float *ropen2, *qerr;
+    const int32_t *first, *last, *qchild;
+    int bucket;
+} WalkCtx;
+
+static int cmp_i32(const void* a, const void* b) {
+    int32_t x = *(const int32_t*)a, y = *(const int32_t*)b;
+    return x < y ? -1 : (x > y);
+}
+
+/* One group's decisions from an initial stack: accepted nodes to acc[],
+ * directly interacted bodies to bod[] (both sorted); returns node tests. */
+static int64_t group_sets(const WalkCtx* c, const float* px, const float* py, int cnt, float aa,
+                          const int32_t* init, int ninit, int32_t** stack, int* cap,
+                          int32_t** acc, int* nacc, int* cacc, int32_t** bod, int* nbod,
+                          int* cbod) {
+    float gx0 = px[0], gx1 = px[0], gy0 = py[0], gy1 = py[0];
+    for (int k = 0; k < cnt; ++k) {
+        gx0 = fminf(gx0, px[k]);
+        gx1 = fmaxf(gx1, px[k]);
+        gy0 = fminf(gy0, py[k]);
+        gy1 = fmaxf(gy1, py[k]);
+    }
+    const float gdiag = sqrtf((gx1 - gx0) * (gx1 - gx0) + (gy1 - gy0) * (gy1 - gy0));
+    int top = 0;
+    int64_t tests = 0;
+    for (int q = 0; q < ninit; ++q) (*stack)[top++] = init[q];
+#define PUSH(arr, num, capv, val)                                              \
+    do {                                                                       \
+        if (*(num) == *(capv)) {                                               \
+            *(capv) *= 2;                                                      \
+            *(arr) = (int32_t*)realloc(*(arr), sizeof(int32_t) * (size_t)*(capv)); \
+        }                                                                      \
+        (*(arr))[(*(num))++] = (val);                                          \
+    } while (0)
+    while (top > 0) {
+        int32_t node = (*stack)[--top];
+        ++tests;
+        float cx = c->mom[node].cx, cy = c->mom[node].cy;
+        float ddx = fmaxf(fmaxf(gx0 - cx, cx - gx1), 0.0f);
+        float ddy = fmaxf(fmaxf(gy0 - cy, cy - gy1), 0.0f);
+        float d2 = ddx * ddx + ddy * ddy;
+        if (d2 <= c->ropen2[node]) {
+            float reach = sqrtf(d2) + gdiag;
+            if (reach * reach > c->ropen2[node]) {
+                d2 = INFINITY;
+                for (int k = 0; k < cnt; ++k) {
+                    float dx = px[k] - cx, dy = py[k] - cy;
+                    float q = dx * dx + dy * dy;
+                    d2 = q < d2 ? q : d2;
+                }
+            }
+        }
+        int accept = d2 > c->ropen2[node] && c->qerr[node] <= aa * d2 * d2 * sqrtf(d2);
+        if (accept) {
+            PUSH(acc, nacc, cacc, node);
+        } else if (c->last[node] - c->first[node] + 1 <= c->bucket) {
+            for (int b = c->first[node]; b <= c->last[node]; ++b) PUSH(bod, nbod, cbod, b);
+        } else {
+            for (int s4 = 0; s4 < 4; ++s4) {
+                int32_t ch = c->qchild[4 * (size_t)node + s4];
+                if (ch == INT32_MIN) continue;
+                if (ch >= 0) {
+                    if (top == *cap) {
+                        *cap *= 2;
+                        *stack = (int32_t*)realloc(*stack, sizeof(int32_t) * (size_t)*cap);
+                    }
+                    (*stack)[top++] = ch;
+                } else {
+                    PUSH(bod, nbod, cbod, ~ch);
+                }
+            }
+        }
+    }
+#undef PUSH
+    qsort(*acc, (size_t)*nacc, sizeof(int32_t), cmp_i32);
+    qsort(*bod, (size_t)*nbod, sizeof(int32_t), cmp_i32);
+    return tests;
+}
+
+void orc_frontier_check(int n, const float* sx, const float* sy, const float* sm,
+                        const uint64_t* skeys, const int32_t* left, const int32_t* right,
+                        const int32_t* split, const int32_t* first, const int32_t* last,
+                        const int32_t* qchild, const float* box, float theta, float G, int bucket,
+                        float alpha, const float* aold, int group, int super, int64_t* stats) {
+    for (int k = 0; k < 5; ++k) stats[k] = 0;
+    if (n < 2) return;
+    Mom* mom = (Mom*)malloc(sizeof(Mom) * (size_t)(n - 1));
+    acc_moments(0, left, right, sx, sy, sm, mom);
+    float* ropen2 = (float*)malloc(sizeof(float) * (size_t)(n - 1));
+    float* qerr = (float*)malloc(sizeof(float) * (size_t)(n - 1));
+    open_radii(n, mom, skeys, split, first, box, theta, G, ropen2, qerr);
+    const WalkCtx c = {mom, ropen2, qerr, first, last, qchild, bucket};
+    const int nsup = (n + super - 1) / super;
+    int64_t diff = 0, fnodes = 0, facc = 0, t_root = 0, t_front = 0;
+#pragma omp parallel reduction(+ : diff, fnodes, facc, t_root, t_front)
+    {
+        int cap = 4096, cacc0 = 1024, cbod0 = 1024, cacc1 = 1024, cbod1 = 1024;
+        int32_t* stack = (int32_t*)malloc(sizeof(int32_t) * (size_t)cap);
+        int32_t* fr = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+        int32_t* frs = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+        int32_t *acc0 = (int32_t*)malloc(4096), *bod0 = (int32_t*)malloc(4096);
+        int32_t *acc1 = (int32_t*)malloc(4096), *bod1 = (int32_t*)malloc(4096);
+#pragma omp for schedule(dynamic, 1)
+        for (int S = 0; S < nsup; ++S) {
+            const int s0 = S * super, s1 = s0 + super < n ? s0 + super : n;
+            float bx0 = sx[s0], bx1 = sx[s0], by0 = sy[s0], by1 = sy[s0];
+            for (int i = s0; i < s1; ++i) {
+                bx0 = fminf(bx0, sx[i]);
+                bx1 = fmaxf(bx1, sx[i]);
+                by0 = fminf(by0, sy[i]);
+                by1 = fmaxf(by1, sy[i]);
+            }
+            /* the frontier: open what every group opens */
+            int top = 0, nf = 0;
+            frs[top++] = 0;
+            while (top > 0) {
+                int32_t node = frs[--top];
+                float cx = mom[node].cx, cy = mom[node].cy;
+                float fx = fmaxf(fabsf(cx - bx0), fabsf(cx - bx1));
+                float fy = fmaxf(fabsf(cy - by0), fabsf(cy - by1));
+                int open = last[node] - first[node] + 1 > bucket && fx * fx + fy * fy <= ropen2[node];
+                for (int s4 = 0; open && s4 < 4; ++s4) {
+                    int32_t ch = qchild[4 * (size_t)node + s4];
+                    if (ch != INT32_MIN && ch < 0) open = 0;  /* a body child */
+                }
+                if (open) {
+                    for (int s4 = 0; s4 < 4; ++s4) {
+                        int32_t ch = qchild[4 * (size_t)node + s4];
+                        if (ch >= 0) frs[top++] = ch;
+                    }
+                } else {
+                    fr[nf++] = node;
+                }
+            }
+            /* the smallest group scale of the super-group, 0.1 % low */
+            float aa = INFINITY;
+            if (aold && alpha > 0.0f) {
+                for (int g0 = s0; g0 < s1; g0 += group) {
+                    int cnt = s1 - g0 < group ? s1 - g0 : group;
+                    float amin = INFINITY, asum = 0.0f;
+                    for (int k = 0; k < cnt; ++k) {
+                        amin = fminf(amin, aold[g0 + k]);
+                        asum += aold[g0 + k];
+                    }
+                    float a = alpha * fmaxf(amin, 0.1f * asum / (float)cnt);
+                    aa = fminf(aa, a);
+                }
+                aa *= 0.999f;
+            }
+            /* frontier cells every group accepts */
+            int ntest = 0, nacc = 0;
+            int32_t* accepted = frs;  /* reuse: the traversal stack is empty now */
+            for (int q = 0; q < nf; ++q) {
+                int32_t node = fr[q];
+                float cx = mom[node].cx, cy = mom[node].cy;
+                float ddx = fmaxf(fmaxf(bx0 - cx, cx - bx1), 0.0f);
+                float ddy = fmaxf(fmaxf(by0 - cy, cy - by1), 0.0f);
+                float d2 = ddx * ddx + ddy * ddy;
+                if (d2 > ropen2[node] && qerr[node] <= aa * d2 * d2 * sqrtf(d2))
+                    accepted[nacc++] = node;
+                else
+                    fr[ntest++] = node;
+            }
+            fnodes += ntest;
+            facc += nacc;
+            /* each group: root start against frontier start */
+            for (int g0 = s0; g0 < s1; g0 += group) {
+                int cnt = s1 - g0 < group ? s1 - g0 : group;
+                float ga = INFINITY;
+                if (aold && alpha > 0.0f) {
+                    float amin = INFINITY, amean = 0.0f;
+                    for (int k = 0; k < cnt; ++k) {
+                        amin = fminf(amin, aold[g0 + k]);
+                        amean += aold[g0 + k];
+                    }
+                    amean /= (float)cnt;
+                    ga = alpha * fmaxf(amin, 0.1f * amean);
+                }
+                int na0 = 0, nb0 = 0, na1 = 0, nb1 = 0;
+                int32_t root = 0;
+                t_root += group_sets(&c, sx + g0, sy + g0, cnt, ga, &root, 1, &stack, &cap, &acc0,
+                                     &na0, &cacc0, &bod0, &nb0, &cbod0);
+                t_front += group_sets(&c, sx + g0, sy + g0, cnt, ga, fr, ntest, &stack, &cap,
+                                      &acc1, &na1, &cacc1, &bod1, &nb1, &cbod1);
+                /* the untested accepted cells join the frontier start's cells */
+                if (na1 + nacc > cacc1) {
+                    cacc1 = na1 + nacc;
+                    acc1 = (int32_t*)realloc(acc1, sizeof(int32_t) * (size_t)cacc1);
+                }
+                memcpy(acc1 + na1, accepted, sizeof(int32_t) * (size_t)nacc);
+                na1 += nacc;
+                qsort(acc1, (size_t)na1, sizeof(int32_t), cmp_i32);
+                if (na0 != na1 || nb0 != nb1 ||
+                    memcmp(acc0, acc1, sizeof(int32_t) * (size_t)na0) != 0 ||
+                    memcmp(bod0, bod1, sizeof(int32_t) * (size_t)nb0) != 0)
+                    ++diff;
+            }
+        }
+        free(stack);
+        free(fr);
+        free(frs);
+        free(acc0);
+        free(bod0);
+        free(acc1);
+        free(bod1);
+    }
+    stats[0] = diff;
+    stats[1] = fnodes;
+    stats[2] = facc;
+    stats[3] = t_root;
+    stats[4] = t_front;
+    free(mom);
+    free(ropen2);
+    free(qerr);
 }
 
 /* ------------------------------------------------------------------ tree invariants

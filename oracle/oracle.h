@@ -107,6 +107,23 @@ int64_t orc_walk_acc(int n, const float* sx, const float* sy, const float* sm,
                      int bucket, float alpha, const float* aold, int quadrupole, int group,
                      float* sax, float* say);
 
+/* The engine's shared walk frontiers (k_frontier in bh_walk.cuh) checked on
+ * the CPU, for one system: per super-group of `super` consecutive bodies the
+ * nodes every group of it opens (not a leaf bucket, only node children, the
+ * super-group box's farthest corner within the opening radius) are opened
+ * once; frontier nodes every group accepts (the box's nearest point beyond the
+ * radius, the relative rule at the smallest group scale taken 0.1 % low) go
+ * to the groups untested.  Each group's accepted cells and direct bodies are
+ * then compared between the root start and the frontier start, with the
+ * decisions of orc_walk_acc.  stats[0] = groups whose sets differ (0 is the
+ * claim), [1] = frontier nodes, [2] = accepted frontier cells, [3] = node
+ * tests from the root, [4] = node tests from the frontiers. */
+void orc_frontier_check(int n, const float* sx, const float* sy, const float* sm,
+                        const uint64_t* skeys, const int32_t* left, const int32_t* right,
+                        const int32_t* split, const int32_t* first, const int32_t* last,
+                        const int32_t* qchild, const float* box, float theta, float G, int bucket,
+                        float alpha, const float* aold, int group, int super, int64_t* stats);
+
 /* Tree invariants (the engine's bh_check, restated for one system; the
  * reference's debug.cpp:23-174 on a binary radix tree): returns the mask of
  * failing checks, bits as BH_CHECK_* in include/stellar_bh.h.  Node arrays have

@@ -58,6 +58,8 @@ def lib() -> ctypes.CDLL:
         L.orc_check_tree.restype = ctypes.c_uint
         L.orc_render.argtypes = [i32, vp, vp, i32, i32, f32, f32, f32, f32, vp]
         L.orc_render.restype = None
+        L.orc_frontier_check.argtypes = [i32] + [vp] * 11 + [f32, f32, i32, f32, vp, i32, i32, vp]
+        L.orc_frontier_check.restype = None
         L.orc_num_threads.restype = i32
         _lib = L
     return _lib
@@ -163,6 +165,25 @@ def walk_acc(sx, sy, sm, skeys, tree: Tree, box, theta, eps2, G=1.0, bucket=8, a
                                _p(_f32(aold)) if aold is not None else None,
                                1 if quadrupole else 0, int(group), _p(sax), _p(say))
     return sax, say, int(inter)
+
+
+def frontier_check(sx, sy, sm, skeys, tree: Tree, box, theta, G=1.0, bucket=8, alpha=0.0,
+                   aold=None, group=32, super_=512) -> dict:
+    """The engine's shared walk frontiers checked on the CPU (orc_frontier_check):
+    groups whose accepted cells or direct bodies differ between the root start
+    and the frontier start (0 expected), frontier sizes and node tests."""
+    n = len(sx)
+    sx, sy, sm = _f32(sx), _f32(sy), _f32(sm)
+    out = np.zeros(5, np.int64)
+    lib().orc_frontier_check(n, _p(sx), _p(sy), _p(sm),
+                             _p(np.ascontiguousarray(skeys, dtype=np.uint64)), _p(tree.left),
+                             _p(tree.right), _p(tree.split), _p(tree.first), _p(tree.last),
+                             _p(tree.qchild), _p(_f32(box)), theta, G, bucket, alpha,
+                             _p(_f32(aold)) if aold is not None else None, int(group),
+                             int(super_), _p(out))
+    return dict(differing_groups=int(out[0]), frontier_nodes=int(out[1]),
+                accepted_cells=int(out[2]), tests_from_root=int(out[3]),
+                tests_from_frontier=int(out[4]))
 
 
 def check_tree(skeys, tree: Tree, sm, node_m, ids, box, left=None, right=None, parent=None,
