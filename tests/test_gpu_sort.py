@@ -86,3 +86,30 @@ def test_full_sort_then_hybrid_again(bh, oracle, graph):
             operm, _ = oracle.sort_keys(oracle.keys(x, y, box))
             assert np.array_equal(s.debug("perm"), operm.astype(np.int32))
             assert s.check() == 0
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_batch_with_a_packed_system_equals_systems_alone(bh, graph):
+    """A batch where one system packs 600 bodies into one cell takes the full
+    sort for the whole batch; every system still gets exactly the results it
+    gets alone."""
+    sizes = [3000, 4096, 1500]
+    systems = [clustered(sizes[0], 0, 21), clustered(sizes[1], 600, 22), clustered(sizes[2], 0, 23)]
+    kw = dict(mode="mixed", theta=0.5, eps2=1e-4, timestep=1e-4, use_graph=graph)
+    cat = [np.concatenate([s[k] for s in systems]) for k in range(5)]
+    with bh.BarnesHutSystem(sizes=sizes, **kw) as b:
+        off = b.offsets()
+        b.set_state(*cat)
+        b.step(3)
+        b.sync()
+        assert b.stats()["status"] == 0
+        got = b.get_state()
+    for k, (x, y, vx, vy, m) in enumerate(systems):
+        with bh.BarnesHutSystem(len(x), **kw) as s:
+            s.set_state(x, y, vx, vy, m)
+            s.step(3)
+            s.sync()
+            ref = s.get_state()
+        sl = slice(off[k], off[k + 1])
+        for key in ("x", "y", "vx", "vy"):
+            assert np.array_equal(got[key][sl].view(np.uint32), ref[key].view(np.uint32)), (k, key)
