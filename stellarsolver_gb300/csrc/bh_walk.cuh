@@ -374,11 +374,12 @@ __host__ __device__ __forceinline__ int acc_warp_bytes(AccShape sh) {
 // Consecutive groups open the same nodes near the top of the tree.  For each
 // super-group of 2^kSuperLog2 consecutive bodies of one system (counted from
 // the system's first body, so a system gets the same frontiers alone and in a
-// batch), k_frontier
-// opens once every node that each of its groups would open, and keeps the
-// nodes where that stops: the frontier.  The main accuracy walk of a group
-// starts from its super-group's frontier instead of the root, and tests and
-// decides exactly the nodes it would have tested from the root.
+// batch), k_frontier opens once every node that each of its groups would
+// open, and keeps the nodes where that stops: the frontier.  The main accuracy
+// walk of a group starts from its super-group's frontier instead of the root,
+// and tests and decides exactly the nodes it would have tested from the root
+// (orc_frontier_check restates this on the CPU).  k_frontier also lists the
+// super-group's heavy walk groups (Heavy).
 //
 // A node is opened for all groups when it is not a leaf bucket, all its
 // children are nodes, and the farthest corner of the super-group's box lies
