@@ -118,19 +118,20 @@ def test_momentum_nearly_conserved(bh):
     assert np.abs(p1 - p0).max() <= 1e-4 * scale
 
 
-@pytest.mark.parametrize("bpl", [1, 2])
-def test_walk_matches_cpu_restatement(bh, oracle, bpl):
+@pytest.mark.parametrize("theta,bpl,n", [(0.5, 1, 1 << 16), (0.5, 2, 1 << 16), (0.15, 1, 1 << 14)])
+def test_walk_matches_cpu_restatement(bh, oracle, theta, bpl, n):
     """The GPU PLAIN walk against oracle.walk_acc (same tree, same rule: the
     bootstrap pass at opening angle 1.25 with monopole cells in 64-body groups,
     then the relative rule with alpha = 0.01).  Moments are
     summed with different float rounding, so a borderline node may be opened on
-    one side only: interaction counts agree to 0.5 %, forces to 2e-4 of RMS."""
+    one side only: interaction counts agree to 0.5 %, forces to 2e-4 of RMS.
+    At theta = 0.15 most super-groups' frontiers are too wide to keep, and
+    their groups start at the root."""
     from stellarsolver_gb300 import models
 
-    n = 1 << 16
     x, y, vx, vy, m = models.plummer(n, 0x5EED3000)
     eps2 = 1e-4
-    with bh.BarnesHutSystem(n, mode="plain", theta=0.5, eps2=eps2, timestep=0.0,
+    with bh.BarnesHutSystem(n, mode="plain", theta=theta, eps2=eps2, timestep=0.0,
                             bodies_per_lane=bpl) as s:
         s.set_state(x, y, vx, vy, m)
         s.step(1)
@@ -147,7 +148,7 @@ def test_walk_matches_cpu_restatement(bh, oracle, bpl):
     sx, sy, sm = x[operm], y[operm], m[operm]
     a0x, a0y, _ = oracle.walk_acc(sx, sy, sm, sk, t, box, 1.25, eps2, quadrupole=False,
                                   group=64)  # bootstrap: always 64-body groups
-    ox, oy, ointer = oracle.walk_acc(sx, sy, sm, sk, t, box, 0.5, eps2, alpha=0.01,
+    ox, oy, ointer = oracle.walk_acc(sx, sy, sm, sk, t, box, theta, eps2, alpha=0.01,
                                      aold=np.hypot(a0x, a0y), group=32 * bpl)
     gx, gy = acc[:n], acc[n:]
     rms = np.sqrt(np.mean(ox.astype(np.float64) ** 2 + oy.astype(np.float64) ** 2))
