@@ -21,16 +21,19 @@ def walk_flops(stats: dict) -> int:
     return FLOPS_P2P * (stats["interactions"] - cells) + FLOPS_P2M * cells
 
 
-def phase_bytes(n: int, mixed: bool, passes: int = 4) -> dict:
+def phase_bytes(n: int, mixed: bool, passes: int = 4, accuracy: bool = True) -> dict:
     """Algorithmic bytes per launch of each HBM-bound phase (each array once).
     The sort: `passes` radix passes over the key's high word and the run
-    fixup, each one read and one write of (key, index)."""
+    fixup, each one read and one write of (key, index).  The reorder moves
+    x, y, vx, vy, m, id (and the hi/lo tails in MIXED mode, |a_old| and the
+    walk-group cost in the accuracy modes) and reads the permutation."""
     lo = 16 * n if mixed else 0
+    acc = 16 * n if accuracy else 0
     return {
         "bbox": 8 * n,
         "keys": 20 * n,
         "sort": 24 * n * (passes + 1),
-        "reorder": 52 * n + lo,
+        "reorder": 52 * n + lo + acc,
         "build": 36 * n + 16 * n,  # keys and node arrays, climb records
         "moments": 12 * n + 64 * n + 108 * n,  # bodies, node sums, then walk records
     }
