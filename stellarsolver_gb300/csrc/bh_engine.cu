@@ -38,8 +38,7 @@ int cuda_fail(cudaError_t e, const char* what) {
 
 namespace {
 
-constexpr int kWalkWarps = 8;
-constexpr int kRefStack = 256;
+constexpr int kWalkWarps = 8;  // accuracy walk: default warps per block
 constexpr int kDefaultStack = 768;  // deepest measured: 670 (2D Plummer, N = 2^24)
 constexpr int kMaxStack = 2048;
 constexpr int kDefaultBucket = 8;
@@ -168,11 +167,10 @@ static cudaError_t launch_acc(const StepArgs& a, cudaStream_t st, int part) {
 cudaError_t launch_walk(const StepArgs& a, cudaStream_t st, int part) {
     if (a.mode == BH_MODE_REFERENCE) {
         if (part == 0) return cudaSuccess;
-        int grid = std::min(a.walk_grid_ref, (a.groups.ngroups + kWalkWarps - 1) / kWalkWarps);
+        int grid = std::min(a.walk_grid_ref, (a.groups.ngroups + kVoteWarps - 1) / kVoteWarps);
         if (grid < 1) grid = 1;
-        return launch_pdl(k_walk_ref<kWalkWarps, kRefStack>, grid, kWalkWarps * 32, 0, st, a.segs,
-                          a.groups, a.in, a.recA, a.recC, a.eps2, a.dt, a.ddt, a.out, a.status,
-                          a.inter, a.work);
+        return launch_pdl(k_walk_vote, grid, kVoteWarps * 32, 0, st, a.segs, a.groups, a.in, a.recA,
+                          a.recC, a.eps2, a.dt, a.ddt, a.out, a.status, a.inter, a.work);
     }
     if (a.bpl == 2)
         return a.mode == BH_MODE_MIXED ? launch_acc<true, 2>(a, st, part)
@@ -794,7 +792,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     if (rc == BH_OK) {
         int bref = 0, bacc = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &bref, k_walk_ref<kWalkWarps, kRefStack>, kWalkWarps * 32, 0);
+            &bref, k_walk_vote, kVoteWarps * 32, 0);
         // grid cap from the worst-case shape; the walks fetch groups dynamically
         const AccShape sh{kDefaultStack, kDefaultBucket, 1};
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bacc, k_walk_acc<true, false>,

@@ -5,11 +5,12 @@
 // (the reference's warp, kernels.cu:342-362) and keep the warp's traversal
 // state in shared memory.
 //
-// k_walk_ref   REFERENCE mode.  Node-serial: every lane evaluates the same
-//              node; a cell is approximated iff all lanes vote dp <= r
-//              (kernels.cu:395-406), bodies always interact, opened cells are
-//              pushed on the warp's stack.  The interaction set is the
-//              reference's; only the summation order differs.
+// k_walk_vote  REFERENCE mode.  A cell is approximated iff all lanes vote
+//              dp <= r (kernels.cu:395-406), i.e. iff dp <= min_b r_b over the
+//              group; bodies always interact.  Lanes decide up to 32 stack
+//              nodes at once and stage the interactions, 32 at a time.  The
+//              interaction set is the reference's; only the summation order
+//              differs.
 // k_walk_acc   PLAIN / MIXED modes.  Lanes test up to 32 stack nodes at once
 //              against the group (geometric rule on the group's nearest body,
 //              relative rule on its |a_old|); accepted cells and the bodies of
@@ -99,111 +100,6 @@ __device__ __forceinline__ float ref_r(float cx, float cy, float px, float py, f
 // Rounds of node tests one group may take.  A valid tree gives a group at most
 // one test per node, far below this; beyond it the tree is not a tree.
 constexpr int kMaxWalkRounds = 1 << 22;
-
-template <int WARPS, int STACK>
-__global__ void __launch_bounds__(WARPS * 32) k_walk_ref(Segs segs, Groups gr, WalkIn in,
-                                                         const float4* __restrict__ recA,
-                                                         const int4* __restrict__ recC, float eps2,
-                                                         float dt, float ddt, WalkOut out,
-                                                         int* __restrict__ status,
-                                                         unsigned long long* __restrict__ inter_total,
-                                                         int* __restrict__ work) {
-    pdl_wait();
-    __shared__ int s_stack[WARPS][STACK];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    int* stack = s_stack[warp];
-    unsigned long long my_inter = 0;
-    for (int g = next_group(work); g < gr.ngroups; g = next_group(work)) {
-        int lo, hi, gstart;
-        group_range(segs, gr, g, &lo, &hi, &gstart);
-        const int j = gstart + lane;
-        const bool valid = j < hi;
-        const int cnt = min(32, hi - gstart);
-        const float px = valid ? in.x[j] : 0.0f, py = valid ? in.y[j] : 0.0f;
-        float ax = 0.0f, ay = 0.0f;
-        long long inter = 0;
-        bool overflow = false;
-        if (hi - lo >= 2) {
-            int top = 0;
-            {
-                float4 A = recA[lo];  // the system's root
-                float dx, dy;
-                float r = ref_r(A.x, A.y, px, py, eps2, &dx, &dy);
-                if (__all_sync(kFull, !valid || A.w <= r)) {
-                    float ri = rsqrtf(r);
-                    float f = A.z * ri * ri * ri;
-                    ax = fmaf(f, dx, ax);
-                    ay = fmaf(f, dy, ay);
-                    inter += cnt;
-                } else {
-                    if (lane == 0) stack[0] = lo;
-                    top = 1;
-                }
-            }
-            int pops = 0;
-            while (top > 0 && !overflow) {
-                if (++pops > kMaxWalkRounds) {  // far beyond any valid tree
-                    if (lane == 0) atomicOr(status, ST_TREE);
-                    break;
-                }
-                __syncwarp();
-                const int node = stack[--top];
-                const int4 C = recC[node];
-                const int cs[4] = {C.x, C.y, C.z, C.w};
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int c = cs[q];
-                    if (c == kNoChild) continue;
-                    float cx, cy, cm, crit;
-                    if (c < 0) {
-                        cx = in.x[~c];
-                        cy = in.y[~c];
-                        cm = in.m[~c];
-                        crit = 0.0f;
-                    } else {
-                        float4 A = recA[c];
-                        cx = A.x;
-                        cy = A.y;
-                        cm = A.z;
-                        crit = A.w;
-                    }
-                    float dx, dy;
-                    float r = ref_r(cx, cy, px, py, eps2, &dx, &dy);
-                    bool accept = (c < 0) || __all_sync(kFull, !valid || crit <= r);
-                    if (accept) {
-                        float ri = rsqrtf(r);  // kernels.cu:407-411
-                        float f = cm * ri * ri * ri;
-                        ax = fmaf(f, dx, ax);
-                        ay = fmaf(f, dy, ay);
-                        inter += cnt;
-                    } else if (top < STACK) {
-                        __syncwarp();
-                        if (lane == 0) stack[top] = c;
-                        ++top;
-                    } else {
-                        overflow = true;
-                    }
-                }
-            }
-        }
-        if (overflow && lane == 0) atomicOr(status, ST_STACK);
-        my_inter += (unsigned long long)inter;
-        if (valid) {
-            // kernels.cu:529-533: v += dt*a; x += d*dt*v
-            float vx = __fadd_rn(in.vx[j], __fmul_rn(dt, ax));
-            float vy = __fadd_rn(in.vy[j], __fmul_rn(dt, ay));
-            out.x[j] = __fadd_rn(px, __fmul_rn(ddt, vx));
-            out.y[j] = __fadd_rn(py, __fmul_rn(ddt, vy));
-            out.vx[j] = vx;
-            out.vy[j] = vy;
-            out.m[j] = in.m[j];
-            out.id[j] = in.id[j];
-            out.ax[j] = ax;
-            out.ay[j] = ay;
-        }
-    }
-    if (lane == 0 && my_inter) atomicAdd(inter_total, my_inter);
-}
 
 // ------------------------------------------------------------------ accuracy walk
 
@@ -367,6 +263,218 @@ __host__ __device__ __forceinline__ int acc_body_cap(int bucket) {
 __host__ __device__ __forceinline__ int acc_warp_bytes(AccShape sh) {
     return 3 * 32 * 16 + 32 * 8 * sh.bpl + 16 + 64 * 4 + ((sh.stack * 4 + 15) & ~15) +
            ((acc_body_cap(sh.bucket) * 4 + 15) & ~15);
+}
+
+// ------------------------------------------------------------------ REFERENCE walk, batched
+//
+// k_walk_vote gives the reference's interaction set with the accuracy walk's
+// machinery.  The reference approximates a cell iff every lane of the warp
+// votes dp_L <= r_b, with r_b = fl(fl(fl(dx)^2 + fl(dy)^2) + eps2) for its
+// body b (kernels.cu:395-406): that is, iff dp_L <= min_b r_b.  Lanes test up
+// to 32 stack nodes at once and find that minimum as the accuracy walk finds
+// its group distance: r of the group box's nearest point is a lower bound
+// (every float step is monotone in |dx|, |dy|), r of the four extreme bodies an
+// upper bound, and only between the two is the minimum over the bodies taken.
+// Accepted cells and the bodies of opened cells are staged and evaluated 32 at
+// a time with the reference's arithmetic (kernels.cu:403-411); only the
+// summation order differs from the reference.
+constexpr int kVoteWarps = 4;
+constexpr int kVoteStack = 1024;
+
+__device__ __forceinline__ float ref_r_only(float cx, float cy, float px, float py, float eps2) {
+    float dx, dy;
+    return ref_r(cx, cy, px, py, eps2, &dx, &dy);
+}
+
+static __global__ void __launch_bounds__(kVoteWarps * 32) k_walk_vote(Segs segs, Groups gr, WalkIn in,
+                                                               const float4* __restrict__ recA,
+                                                               const int4* __restrict__ recC,
+                                                               float eps2, float dt, float ddt,
+                                                               WalkOut out,
+                                                               int* __restrict__ status,
+                                                               unsigned long long* __restrict__ inter_total,
+                                                               int* __restrict__ work) {
+    pdl_wait();
+    __shared__ int s_stack[kVoteWarps][kVoteStack];
+    __shared__ float4 s_stage[kVoteWarps][32];  // staged entries: x, y, m
+    __shared__ float2 s_gp[kVoteWarps][32];     // the group's positions
+    __shared__ int s_clist[kVoteWarps][64];
+    __shared__ int s_blist[kVoteWarps][32 + 128];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned lt = lanemask_lt();
+    int* stack = s_stack[warp];
+    float4* stage = s_stage[warp];
+    float2* gp = s_gp[warp];
+    int* clist = s_clist[warp];
+    int* blist = s_blist[warp];
+    unsigned long long my_inter = 0;
+    for (int g = next_group(work); g < gr.ngroups; g = next_group(work)) {
+        int lo, hi, gstart;
+        group_range(segs, gr, g, &lo, &hi, &gstart);
+        const int j = gstart + lane;
+        const bool valid = j < hi;
+        const int cnt = min(32, hi - gstart);
+        // invalid lanes mirror the group's first body (they vote with it)
+        const float px = in.x[valid ? j : gstart], py = in.y[valid ? j : gstart];
+        __syncwarp();
+        gp[lane] = make_float2(px, py);
+        float gx0 = px, gx1 = px, gy0 = py, gy1 = py;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            gx0 = fminf(gx0, __shfl_xor_sync(kFull, gx0, o));
+            gx1 = fmaxf(gx1, __shfl_xor_sync(kFull, gx1, o));
+            gy0 = fminf(gy0, __shfl_xor_sync(kFull, gy0, o));
+            gy1 = fmaxf(gy1, __shfl_xor_sync(kFull, gy1, o));
+        }
+        // the extreme bodies: y at min/max x, x at min/max y
+        float ext[4];
+        {
+            const float key[4] = {gx0, gx1, gy0, gy1};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const unsigned hit = __ballot_sync(kFull, (q < 2 ? px : py) == key[q]);
+                ext[q] = __shfl_sync(kFull, q < 2 ? py : px, __ffs(hit) - 1);
+            }
+        }
+        float ax = 0.0f, ay = 0.0f;
+        long long entries = 0;
+        bool overflow = false;
+        int top = 0, ccnt = 0, bcnt = 0, rounds = 0;
+        if (hi - lo >= 2) {
+            if (lane == 0) stack[0] = lo;  // the system's root
+            top = 1;
+        }
+        // k entries of staged (x, y, m), with the reference's arithmetic
+        auto interact = [&](int k) {
+            for (int e = 0; e < k; ++e) {
+                const float4 c = stage[e];
+                float dx, dy;
+                const float r = ref_r(c.x, c.y, px, py, eps2, &dx, &dy);
+                const float ri = rsqrtf(r);  // kernels.cu:407-411
+                const float f = c.z * ri * ri * ri;
+                ax = fmaf(f, dx, ax);
+                ay = fmaf(f, dy, ay);
+            }
+            entries += k;
+        };
+        auto flush_cells = [&](int k) {  // the last k entries of clist
+            __syncwarp();
+            if (lane < k) {
+                const float4 A = recA[clist[ccnt - k + lane]];
+                stage[lane] = make_float4(A.x, A.y, A.z, 0.0f);
+            }
+            __syncwarp();
+            interact(k);
+            ccnt -= k;
+        };
+        auto flush_bodies = [&](int k) {
+            __syncwarp();
+            if (lane < k) {
+                const int b = blist[bcnt - k + lane];
+                stage[lane] = make_float4(in.x[b], in.y[b], in.m[b], 0.0f);
+            }
+            __syncwarp();
+            interact(k);
+            bcnt -= k;
+        };
+        while (top > 0) {
+            if (rounds == kMaxWalkRounds) {  // far beyond any valid tree: report, do not loop
+                if (lane == 0) atomicOr(status, ST_TREE);
+                break;
+            }
+            int k = min(32, top);
+            if (top + 3 * k > kVoteStack) {  // pop k, push <= 4k
+                k = max((kVoteStack - top) / 3, 0);
+                if (k == 0) {
+                    overflow = true;
+                    break;
+                }
+            }
+            __syncwarp();
+            const int node = lane < k ? stack[top - 1 - lane] : -1;
+            top -= k;
+            ++rounds;
+            float4 A = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            bool acc = false, need = false;
+            if (node >= 0) {
+                A = recA[node];
+                // lower bound of min_b r_b: the box's nearest point
+                const float nx = fminf(fmaxf(A.x, gx0), gx1), ny = fminf(fmaxf(A.y, gy0), gy1);
+                const float rlo = ref_r_only(A.x, A.y, nx, ny, eps2);
+                if (A.w <= rlo) {
+                    acc = true;
+                } else {
+                    // upper bound: the extreme bodies; below dp some body votes to open
+                    float rhi = ref_r_only(A.x, A.y, gx0, ext[0], eps2);
+                    rhi = fminf(rhi, ref_r_only(A.x, A.y, gx1, ext[1], eps2));
+                    rhi = fminf(rhi, ref_r_only(A.x, A.y, ext[2], gy0, eps2));
+                    rhi = fminf(rhi, ref_r_only(A.x, A.y, ext[3], gy1, eps2));
+                    need = A.w <= rhi;
+                }
+            }
+            unsigned nm = __ballot_sync(kFull, need);
+            while (nm) {  // the exact minimum over the group's bodies, one node at a time
+                const int src = __ffs(nm) - 1;
+                nm &= nm - 1;
+                const float cx = __shfl_sync(kFull, A.x, src), cy = __shfl_sync(kFull, A.y, src);
+                float r = ref_r_only(cx, cy, px, py, eps2);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) r = fminf(r, __shfl_xor_sync(kFull, r, o));
+                if (lane == src) acc = A.w <= r;
+            }
+            const unsigned mc = __ballot_sync(kFull, acc);
+            if (acc) clist[ccnt + __popc(mc & lt)] = node;
+            ccnt += __popc(mc);
+            const bool open = node >= 0 && !acc;
+            int4 C = make_int4(kNoChild, kNoChild, kNoChild, kNoChild);
+            if (open) C = recC[node];
+            const int cs[4] = {C.x, C.y, C.z, C.w};
+            int nb = 0, nn = 0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                nb += (cs[q] != kNoChild && cs[q] < 0);
+                nn += (cs[q] >= 0);
+            }
+            int tot;
+            const int off = warp_excl_scan(nb | (nn << 16), &tot);
+            __syncwarp();  // every lane has read its stack slot before children overwrite it
+            if (open) {
+                int* bw = blist + bcnt + (off & 0xffff);
+                int* nw = stack + top + (off >> 16);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (cs[q] == kNoChild) continue;
+                    if (cs[q] < 0)
+                        *bw++ = ~cs[q];  // bodies always interact (kernels.cu:395-399)
+                    else
+                        *nw++ = cs[q];
+                }
+            }
+            bcnt += tot & 0xffff;
+            top += tot >> 16;
+            __syncwarp();
+            while (ccnt >= 32) flush_cells(32);
+            while (bcnt >= 32) flush_bodies(32);
+        }
+        if (ccnt > 0) flush_cells(ccnt);
+        if (bcnt > 0) flush_bodies(bcnt);
+        if (overflow && lane == 0) atomicOr(status, ST_STACK);
+        my_inter += (unsigned long long)(entries * cnt);
+        if (valid) {
+            // kernels.cu:529-533: v += dt*a; x += d*dt*v
+            float vx = __fadd_rn(in.vx[j], __fmul_rn(dt, ax));
+            float vy = __fadd_rn(in.vy[j], __fmul_rn(dt, ay));
+            out.x[j] = __fadd_rn(px, __fmul_rn(ddt, vx));
+            out.y[j] = __fadd_rn(py, __fmul_rn(ddt, vy));
+            out.vx[j] = vx;
+            out.vy[j] = vy;
+            out.m[j] = in.m[j];
+            out.id[j] = in.id[j];
+            out.ax[j] = ax;
+            out.ay[j] = ay;
+        }
+    }
+    if (lane == 0 && my_inter) atomicAdd(inter_total, my_inter);
 }
 
 // ------------------------------------------------------------------ shared frontier

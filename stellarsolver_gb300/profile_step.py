@@ -6,7 +6,7 @@ Creates one system on the 2D Plummer input, runs `--warmup` steps, then
 `--steps` steps, synchronising after each, and prints the per-step status.
 Kernel order per step: k_bbox, k_keys, (k_radix_hist, k_radix_scan,
 k_radix_scatter) x 8, k_gather, k_build, k_moments, k_records, then the walk
-(REFERENCE: k_walk_ref; PLAIN/MIXED: the bootstrap k_walk_acc, which exits at
+(REFERENCE: k_walk_vote; PLAIN/MIXED: the bootstrap k_walk_acc, which exits at
 once unless the state was just set, and the main k_walk_acc).
 """
 import argparse
