@@ -10,7 +10,8 @@ force walk fused with the integration.
           hi/lo positions) replayed as a CUDA graph, inputs resident in HBM,
           CUDA events per step, L2 flushed between timed steps.
   e2e     the same metric through the C ABI with host buffers: every step
-          copies the state in from pinned host memory, steps, and reads the
+          copies in from pinned host memory the state the reference's reset()
+          uploads (x, y, vx, vy, ax, ay, mass), steps, and reads the
           positions back.
   roofline  the force walk against the measured FP32 FMA peak (14 flops per
           body-body and 33 per body-cell interaction); per-phase HBM
@@ -317,8 +318,21 @@ def run_e2e(bh, torch, stream, sp, n, x, y, vx, vy, m, params, local, args):
                             leaf_bucket=params.leaf_bucket, block_size=params.block_size,
                             stack_depth=params.stack_depth, alpha=params.alpha,
                             bodies_per_lane=params.bodies_per_lane) as s:
+        # the accelerations of the uploaded state: one step from it, then
+        # bh_get_accel (the |a| that step computed at the uploaded positions)
+        pin["ax"] = torch.empty(n, dtype=torch.float32).pin_memory()
+        pin["ay"] = torch.empty(n, dtype=torch.float32).pin_memory()
+        ptr["ax"], ptr["ay"] = pin["ax"].data_ptr(), pin["ay"].data_ptr()
+        rc = lib.bh_set_state(s.handle, ptr["x"], ptr["y"], ptr["vx"], ptr["vy"], ptr["m"], sp)
+        rc |= lib.bh_step(s.handle, 1, sp)
+        rc |= lib.bh_get_accel(s.handle, ptr["ax"], ptr["ay"], sp)
+        s.sync(sp)
+        if rc:
+            raise RuntimeError(f"e2e C-ABI call failed: {rc}")
+
         def one():
             rc = lib.bh_set_state(s.handle, ptr["x"], ptr["y"], ptr["vx"], ptr["vy"], ptr["m"], sp)
+            rc |= lib.bh_set_accel(s.handle, ptr["ax"], ptr["ay"], sp)
             rc |= lib.bh_step(s.handle, 1, sp)
             rc |= lib.bh_get_state(s.handle, outx.data_ptr(), outy.data_ptr(), None, None, None, sp)
             if rc:
@@ -337,8 +351,9 @@ def run_e2e(bh, torch, stream, sp, n, x, y, vx, vy, m, params, local, args):
         secs = a.elapsed_time(b) / 1e3
         s.sync(sp)
     return {"value": round(args.steps / secs, 3), "unit": "steps/s",
-            "h2d_bytes_per_step": 20 * n, "d2h_bytes_per_step": 8 * n,
-            "path": "bh_set_state(pinned host) + bh_step + bh_get_state(x, y -> pinned host)"}
+            "h2d_bytes_per_step": 28 * n, "d2h_bytes_per_step": 8 * n,
+            "path": "bh_set_state + bh_set_accel (pinned host: the arrays of the reference's "
+                    "reset()) + bh_step + bh_get_state(x, y -> pinned host)"}
 
 
 def run_ensemble(bh, torch, stream, sp, local, world, rank, args):

@@ -121,16 +121,23 @@ int bh_num_bodies(const bh_system* s); /* getNumParticles() (BarnesHutParticleSy
 
 /* reset()'s host-to-device copy (BarnesHutParticleSystem.cpp:364-371).  Any
  * pointer may be host or device memory (cudaMemcpyDefault).  Accelerations
- * start at zero.  Asynchronous on `stream`, like cudaMemcpyAsync: pinned host
- * or device sources must stay unchanged until the stream has passed the call
- * (pageable host memory is staged before the call returns). */
+ * start at zero.  Asynchronous on `stream`, like cudaMemcpyAsync.  x and y
+ * are copied on `stream`; vx, vy and mass on the handle's own copy stream,
+ * overlapped with the next step's box, keys and sort, and ordered before the
+ * work of the next call on the handle (bh_step joins them just before the
+ * reorder), on that call's stream.  So pinned host or device sources must stay
+ * unchanged until `stream` has passed the next call on the handle, e.g.
+ * bh_step or bh_sync (pageable host memory is staged before the call
+ * returns). */
 int bh_set_state(bh_system* s, const float* x, const float* y, const float* vx,
                  const float* vy, const float* mass, void* stream);
 
 /* Accelerations of the state just loaded by bh_set_state (caller's order,
  * host or device pointers), like the reference's reset() upload of d_ax/d_ay
  * (BarnesHutParticleSystem.cpp:370-371).  PLAIN/MIXED use |a| as the scale of
- * the relative opening rule, so the next step skips the bootstrap pass. */
+ * the relative opening rule, so the next step skips the bootstrap pass.
+ * Copied on the handle's copy stream like bh_set_state's vx, vy and mass, with
+ * the same rule for the sources. */
 int bh_set_accel(bh_system* s, const float* ax, const float* ay, void* stream);
 
 /* Copy the current state out in the caller's order (any of the pointers may be

@@ -35,6 +35,12 @@ int cuda_fail(cudaError_t e, const char* what) {
         cudaError_t e_ = (call);                                     \
         if (e_ != cudaSuccess) return ssg::cuda_fail(e_, #call);     \
     } while (0)
+// the same for calls that return a status code
+#define RC(call)                                                     \
+    do {                                                             \
+        int rc_ = (call);                                            \
+        if (rc_ != BH_OK) return rc_;                                \
+    } while (0)
 
 namespace {
 
@@ -61,6 +67,11 @@ constexpr int kStepWords = 16;
 constexpr int kWorkSortOverflow = 9;
 constexpr int kWorkHeavy = 10;
 constexpr int kStepZero = 4 + 6;
+
+// Parts of a step: all of it, or split after the sort (bh_step joins the input
+// copies of bh_set_state in between).
+enum StepPart { kStepAll = 0, kStepPre = 1, kStepPost = 2 };
+constexpr int kGraphs = 5;
 
 template <typename T>
 T* carve(char*& cur, size_t count) {
@@ -254,14 +265,25 @@ struct bh_system {
 
     cudaStream_t cap_stream = nullptr;
     cudaStream_t cond_stream = nullptr;  // captures the body of the sort's conditional node
-    cudaGraph_t graph[2] = {nullptr, nullptr};  // one step without / with the bootstrap pass
-    cudaGraphExec_t graph_exec[2] = {nullptr, nullptr};
+    // Step graphs: [0] / [1] one step without / with the bootstrap pass; [2] the
+    // step up to the sort; [3] / [4] the rest, without / with the bootstrap pass
+    // (the first step after bh_set_state: the input copies join in between).
+    cudaGraph_t graph[kGraphs] = {};
+    cudaGraphExec_t graph_exec[kGraphs] = {};
+
+    // Input copies that no kernel before the reorder reads (vx, vy, mass; the
+    // accelerations of bh_set_accel) run on copy_stream, overlapped with the
+    // next step's box, keys and sort; in_event marks their end.
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t in_event = nullptr;
+    cudaEvent_t order_event = nullptr;  // `stream`'s work before a copy_stream copy
+    bool in_pending = false;            // copies on copy_stream that no step has joined yet
 };
 
 namespace {
 
 void drop_graph(bh_system* s) {
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < kGraphs; ++b) {
         if (s->graph_exec[b]) cudaGraphExecDestroy(s->graph_exec[b]);
         if (s->graph[b]) cudaGraphDestroy(s->graph[b]);
         s->graph_exec[b] = nullptr;
@@ -320,23 +342,21 @@ ssg::StepArgs step_args(bh_system* s) {
     return a;
 }
 
-// Box, keys, sort, reorder, tree, moments and walk records of the current
-// state (phases 0-5; the walk records in the accuracy layout when `accuracy`).
-// ev (optional): events recorded at the phase boundaries.  keep_stats: leave
-// the last step's interaction counts and walk statistics (the energy pass).
-int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev,
-                  bool keep_stats = false) {
+// Phases 0-3 of a step: box, keys, sort.  The sorted keys and permutation end
+// in keys_alt / vals_alt, or in keys3 / vals3 after an odd number of
+// system-index passes.
+int enqueue_sort(bh_system* s, cudaStream_t st, cudaEvent_t* ev, bool keep_stats) {
     const int n = s->n;
     auto mark = [&](int k) -> cudaError_t { return ev ? cudaEventRecord(ev[k], st) : cudaSuccess; };
-    const bool mixed = s->p.mode == BH_MODE_MIXED;
     Segs segs{s->nseg, s->seg_off, s->nseg > 1 ? s->seg_of_pos : nullptr};
+    const BodyPtrs& cur = s->st[0];
+    const int tb = 256, nb = (n + tb - 1) / tb;
+    uint64_t *k0 = s->keys, *kA = s->keys_alt, *kB = s->keys3;
+    uint32_t *v0 = s->vals, *vA = s->vals_alt, *vB = s->vals3;
     CK(cudaMemsetAsync(s->box_ord, 0, sizeof(int) * 4 * s->nseg, st));  // origin box
-
-    BodyPtrs cur = s->st[0];
     CK(mark(0));
     CK(launch_pdl(k_bbox<kBboxThreads>, s->nchunks, kBboxThreads, 0, st, cur.x, cur.y,
                   s->chunk_seg, s->chunk_begin, s->chunk_end, s->box_ord, s->status));
-    const int tb = 256, nb = (n + tb - 1) / tb;
     CK(mark(1));
     // keys and positions; the moments counters and the step's words cleared
     CK(launch_pdl(k_keys_step, nb, tb, 0, st, cur.x, cur.y, n, segs, s->box_ord, s->keys, s->vals,
@@ -351,8 +371,6 @@ int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev,
     // graph behind a conditional node that only the fixup switches on, in
     // stream order as kernels that return at once unless the flag is set.
     int* overflow = s->work + kWorkSortOverflow;
-    uint64_t *k0 = s->keys, *kA = s->keys_alt, *kB = s->keys3;
-    uint32_t *v0 = s->vals, *vA = s->vals_alt, *vB = s->vals3;
     auto pass = [&](auto launch, cudaStream_t q, const uint64_t* ki, const uint32_t* vi, uint64_t* ko,
                     uint32_t* vo, int shift, int use_seg, const int* only_if) -> cudaError_t {
         cudaError_t e = launch(k_radix_hist, s->tiles, kSortThreads, 0, q, ki, vi, n, shift, use_seg,
@@ -432,9 +450,34 @@ int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev,
         std::swap(ka, kb);
         std::swap(va, vb);
     }
+    CK(mark(3));
+    return BH_OK;
+}
+
+// Box, keys, sort, reorder, tree, moments and walk records of the current
+// state (phases 0-5; the walk records in the accuracy layout when `accuracy`).
+// ev (optional): events recorded at the phase boundaries.  keep_stats: leave
+// the last step's interaction counts and walk statistics (the energy pass).
+// part: kStepPre stops after the sort, kStepPost starts at the reorder.
+int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev,
+                  bool keep_stats = false, int part = kStepAll) {
+    const int n = s->n;
+    auto mark = [&](int k) -> cudaError_t { return ev ? cudaEventRecord(ev[k], st) : cudaSuccess; };
+    const bool mixed = s->p.mode == BH_MODE_MIXED;
+    Segs segs{s->nseg, s->seg_off, s->nseg > 1 ? s->seg_of_pos : nullptr};
+    const BodyPtrs& cur = s->st[0];
+    const int tb = 256, nb = (n + tb - 1) / tb;
+    if (part != kStepPost) {
+        int rc = enqueue_sort(s, st, ev, keep_stats);
+        if (rc != BH_OK) return rc;
+    }
+    // the sorted keys and permutation: in kA after the fixup, moved by each
+    // system-index pass
+    uint64_t* ka = (s->seg_passes & 1) ? s->keys3 : s->keys_alt;
+    uint32_t* va = (s->seg_passes & 1) ? s->vals3 : s->vals_alt;
     s->kfinal = ka;
     s->vfinal = va;
-    CK(mark(3));
+    if (part == kStepPre) return BH_OK;
 
     BodyPtrs src = cur, dst = s->st[1];
     if (!mixed) {
@@ -463,12 +506,13 @@ int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev,
 // state only) and the walk fused with the integration (phases 6-7).
 // boot < 0: the bootstrap pass is launched iff bh_set_state came since the last
 // step (the host's record, cleared here); 0 / 1: left out / launched (graph capture).
-int enqueue_step(bh_system* s, cudaStream_t st, cudaEvent_t* ev = nullptr, int boot = -1) {
+int enqueue_step(bh_system* s, cudaStream_t st, cudaEvent_t* ev = nullptr, int boot = -1,
+                 int part = kStepAll) {
     auto mark = [&](int k) -> cudaError_t { return ev ? cudaEventRecord(ev[k], st) : cudaSuccess; };
+    int rc = enqueue_front(s, st, s->p.mode != BH_MODE_REFERENCE, ev, false, part);
+    if (rc != BH_OK || part == kStepPre) return rc;
     const bool with_boot = boot < 0 ? s->fresh_host : boot > 0;
     if (boot < 0) s->fresh_host = false;
-    int rc = enqueue_front(s, st, s->p.mode != BH_MODE_REFERENCE, ev);
-    if (rc != BH_OK) return rc;
     StepArgs a = step_args(s);
     if (with_boot) CK(launch_walk(a, st, 0));
     CK(mark(7));
@@ -559,11 +603,42 @@ __global__ void k_direct_reduce(int ns, int chunks, const double* __restrict__ p
     out[t] = G * acc;
 }
 
-int build_graph(bh_system* s, int boot) {
+// The copy stream starts its next copy after the work enqueued on `st` so far.
+int copy_stream_after(bh_system* s, cudaStream_t st) {
+    if (!s->copy_stream) {
+        CK(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&s->in_event, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&s->order_event, cudaEventDisableTiming));
+    }
+    CK(cudaEventRecord(s->order_event, st));
+    CK(cudaStreamWaitEvent(s->copy_stream, s->order_event, 0));
+    return BH_OK;
+}
+
+// The input copies still on the copy stream come before `st`'s next work.
+int join_inputs(bh_system* s, cudaStream_t st) {
+    if (!s->in_pending) return BH_OK;
+    CK(cudaStreamWaitEvent(st, s->in_event, 0));
+    s->in_pending = false;
+    return BH_OK;
+}
+
+// The same for calls without a stream: the host waits for the copies.
+int settle_inputs(bh_system* s) {
+    if (!s->in_pending) return BH_OK;
+    CK(cudaStreamSynchronize(s->copy_stream));
+    s->in_pending = false;
+    return BH_OK;
+}
+
+// Capture of graph slot `slot` (see bh_system::graph).
+int build_graph(bh_system* s, int slot) {
     if (!s->cap_stream) CK(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
     if (!s->cond_stream) CK(cudaStreamCreateWithFlags(&s->cond_stream, cudaStreamNonBlocking));
+    const int part = slot < 2 ? kStepAll : slot == 2 ? kStepPre : kStepPost;
+    const int boot = (slot == 1 || slot == 4) ? 1 : 0;
     CK(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal));
-    int st = enqueue_step(s, s->cap_stream, nullptr, boot);
+    int st = enqueue_step(s, s->cap_stream, nullptr, boot, part);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(s->cap_stream, &g);
     if (st != BH_OK) {
@@ -571,15 +646,25 @@ int build_graph(bh_system* s, int boot) {
         return st;
     }
     if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
-    s->graph[boot] = g;
-    CK(cudaGraphInstantiate(&s->graph_exec[boot], g, 0));
+    s->graph[slot] = g;
+    CK(cudaGraphInstantiate(&s->graph_exec[slot], g, 0));
     return BH_OK;
 }
 
 // State of a freshly loaded system: caller order, zero position tails and
 // accelerations, status cleared, bootstrap pass requested.
+// The previous state's walk-group costs in caller order: kept[id[i]] = gcost[i].
+// They only order the walk's groups (heaviest first), never change a result,
+// so a state that continues the previous one keeps its schedule.
+__global__ void k_keep_cost(int n, const int* __restrict__ id, const int* __restrict__ gcost,
+                            int* __restrict__ kept) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) kept[id[i]] = gcost[i];
+}
+
+// kept: costs from k_keep_cost, or NULL for none (every group of equal weight)
 __global__ void k_state_init(int n, int* id, float* xlo, float* ylo, float* ax, float* ay,
-                             float* amag, int* gcost, int* status, int* fresh) {
+                             float* amag, int* gcost, const int* kept, int* status, int* fresh) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
         id[i] = i;
@@ -588,7 +673,7 @@ __global__ void k_state_init(int n, int* id, float* xlo, float* ylo, float* ax, 
         ax[i] = 0.0f;
         ay[i] = 0.0f;
         amag[i] = 0.0f;
-        gcost[i] = 0;
+        gcost[i] = kept ? kept[i] : 0;
     }
     if (i == 0) {
         *status = 0;
@@ -854,6 +939,12 @@ int bh_system_offset(const bh_system* s, int k) {
 int bh_destroy(bh_system* s) {
     if (!s) return BH_ERR_ARG;
     cudaSetDevice(s->device);
+    if (s->copy_stream) {
+        cudaStreamSynchronize(s->copy_stream);
+        cudaStreamDestroy(s->copy_stream);
+        cudaEventDestroy(s->in_event);
+        cudaEventDestroy(s->order_event);
+    }
     drop_graph(s);
     if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
     if (s->cond_stream) cudaStreamDestroy(s->cond_stream);
@@ -894,13 +985,26 @@ int bh_set_state(bh_system* s, const float* x, const float* y, const float* vx, 
     cudaStream_t st = (cudaStream_t)stream;
     const size_t b = sizeof(float) * s->n;
     const BodyPtrs& c = s->st[0];
+    // x and y on `stream`: the next step's box and keys read them.  vx, vy and
+    // mass, read first by the reorder, go on the copy stream and overlap the
+    // box, keys and sort; the next call on the handle joins them.
     CK(cudaMemcpyAsync(c.x, x, b, cudaMemcpyDefault, st));
     CK(cudaMemcpyAsync(c.y, y, b, cudaMemcpyDefault, st));
-    CK(cudaMemcpyAsync(c.vx, vx, b, cudaMemcpyDefault, st));
-    CK(cudaMemcpyAsync(c.vy, vy, b, cudaMemcpyDefault, st));
-    CK(cudaMemcpyAsync(c.m, mass, b, cudaMemcpyDefault, st));
+    RC(copy_stream_after(s, st));
+    CK(cudaMemcpyAsync(c.vx, vx, b, cudaMemcpyDefault, s->copy_stream));
+    CK(cudaMemcpyAsync(c.vy, vy, b, cudaMemcpyDefault, s->copy_stream));
+    CK(cudaMemcpyAsync(c.m, mass, b, cudaMemcpyDefault, s->copy_stream));
+    CK(cudaEventRecord(s->in_event, s->copy_stream));
+    s->in_pending = true;
+    // a handle that held a state keeps its bodies' walk-group costs (by caller index)
+    const int* kept = nullptr;
+    if (s->have_state && s->p.mode != BH_MODE_REFERENCE) {
+        k_keep_cost<<<(s->n + 255) / 256, 256, 0, st>>>(s->n, c.id, c.gcost, s->st[1].gcost);
+        CK(cudaGetLastError());
+        kept = s->st[1].gcost;
+    }
     k_state_init<<<(s->n + 255) / 256, 256, 0, st>>>(s->n, c.id, c.xlo, c.ylo, s->ax, s->ay,
-                                                     c.amag, c.gcost, s->status, s->fresh);
+                                                     c.amag, c.gcost, kept, s->status, s->fresh);
     CK(cudaGetLastError());
     s->have_state = true;
     s->caller_order = true;
@@ -908,8 +1012,10 @@ int bh_set_state(bh_system* s, const float* x, const float* y, const float* vx, 
     return BH_OK;
 }
 
-__global__ void k_amag(int n, const float* ax, const float* ay, float* amag, float* sax, float* say) {
+__global__ void k_amag(int n, const float* ax, const float* ay, float* amag, float* sax, float* say,
+                       int* fresh) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) *fresh = 0;  // |a| is known: no bootstrap pass in the next step
     if (i < n) {
         float a = ax[i], b = ay[i];
         amag[i] = sqrtf(a * a + b * b);
@@ -925,11 +1031,16 @@ int bh_set_accel(bh_system* s, const float* ax, const float* ay, void* stream) {
     cudaStream_t st = (cudaStream_t)stream;
     const size_t b = sizeof(float) * s->n;
     BodyPtrs& t = s->st[1];
-    CK(cudaMemcpyAsync(t.x, ax, b, cudaMemcpyDefault, st));
-    CK(cudaMemcpyAsync(t.y, ay, b, cudaMemcpyDefault, st));
-    k_amag<<<(s->n + 255) / 256, 256, 0, st>>>(s->n, t.x, t.y, s->st[0].amag, s->ax, s->ay);
+    // on the copy stream, after bh_set_state's state initialisation (`stream`),
+    // overlapped with the next step's box, keys and sort like vx, vy and mass
+    RC(copy_stream_after(s, st));
+    CK(cudaMemcpyAsync(t.x, ax, b, cudaMemcpyDefault, s->copy_stream));
+    CK(cudaMemcpyAsync(t.y, ay, b, cudaMemcpyDefault, s->copy_stream));
+    k_amag<<<(s->n + 255) / 256, 256, 0, s->copy_stream>>>(s->n, t.x, t.y, s->st[0].amag, s->ax,
+                                                           s->ay, s->fresh);
     CK(cudaGetLastError());
-    CK(cudaMemsetAsync(s->fresh, 0, sizeof(int), st));
+    CK(cudaEventRecord(s->in_event, s->copy_stream));
+    s->in_pending = true;
     s->fresh_host = false;
     return BH_OK;
 }
@@ -957,6 +1068,7 @@ int bh_get_state(bh_system* s, float* x, float* y, float* vx, float* vy, float* 
     if (!s) return BH_ERR_ARG;
     if (!s->have_state) return BH_ERR_STATE;
     CK(cudaSetDevice(s->device));
+    RC(join_inputs(s, (cudaStream_t)stream));
     cudaStream_t st = (cudaStream_t)stream;
     const BodyPtrs& c = s->st[0];
     int rc = scatter_out(s, c.x, c.y, c.vx, c.vy, x, y, vx, vy, st);
@@ -968,6 +1080,7 @@ int bh_get_accel(bh_system* s, float* ax, float* ay, void* stream) {
     if (!s) return BH_ERR_ARG;
     if (!s->have_state) return BH_ERR_STATE;
     CK(cudaSetDevice(s->device));
+    RC(join_inputs(s, (cudaStream_t)stream));
     return scatter_out(s, s->ax, s->ay, nullptr, nullptr, ax, ay, nullptr, nullptr,
                        (cudaStream_t)stream);
 }
@@ -977,6 +1090,7 @@ int bh_get_positions_hilo(bh_system* s, float* xhi, float* xlo, float* yhi, floa
     if (!s) return BH_ERR_ARG;
     if (!s->have_state) return BH_ERR_STATE;
     CK(cudaSetDevice(s->device));
+    RC(join_inputs(s, (cudaStream_t)stream));
     const BodyPtrs& c = s->st[0];
     return scatter_out(s, c.x, c.xlo, c.y, c.ylo, xhi, xlo, yhi, ylo, (cudaStream_t)stream);
 }
@@ -990,20 +1104,33 @@ int bh_step(bh_system* s, int steps, void* stream) {
     CK(cudaSetDevice(s->device));
     cudaStream_t st = (cudaStream_t)stream;
     if (s->p.use_graph) {
+        auto ensure = [&](int slot) -> int {
+            if (s->graph_exec[slot]) return BH_OK;
+            // the capture stream must see the state that `stream` produced
+            cudaEvent_t ev;
+            CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            CK(cudaEventRecord(ev, st));
+            if (!s->cap_stream) CK(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
+            CK(cudaStreamWaitEvent(s->cap_stream, ev, 0));
+            cudaEventDestroy(ev);
+            return build_graph(s, slot);
+        };
         for (int k = 0; k < steps; ++k) {
             const int gi = s->fresh_host ? 1 : 0;  // with the bootstrap pass after bh_set_state
-            if (!s->graph_exec[gi]) {
-                // the capture stream must see the state that `stream` produced
-                cudaEvent_t ev;
-                CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-                CK(cudaEventRecord(ev, st));
-                if (!s->cap_stream) CK(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
-                CK(cudaStreamWaitEvent(s->cap_stream, ev, 0));
-                cudaEventDestroy(ev);
-                int rc = build_graph(s, gi);
+            if (s->in_pending) {
+                // bh_set_state's copies run on: box, keys and sort first, then
+                // the join, then the rest of the step
+                int rc = ensure(2);
+                if (rc == BH_OK) rc = ensure(3 + gi);
                 if (rc != BH_OK) return rc;
+                CK(cudaGraphLaunch(s->graph_exec[2], st));
+                RC(join_inputs(s, st));
+                CK(cudaGraphLaunch(s->graph_exec[3 + gi], st));
+            } else {
+                int rc = ensure(gi);
+                if (rc != BH_OK) return rc;
+                CK(cudaGraphLaunch(s->graph_exec[gi], st));
             }
-            CK(cudaGraphLaunch(s->graph_exec[gi], st));
             s->fresh_host = false;
             s->caller_order = false;
             if (s->energy_every > 0 && ++s->energy_steps % s->energy_every == 0) {
@@ -1023,7 +1150,16 @@ int bh_step(bh_system* s, int steps, void* stream) {
         return BH_OK;
     }
     for (int k = 0; k < steps; ++k) {
-        int rc = enqueue_step(s, st);
+        int rc = BH_OK;
+        if (s->in_pending) {
+            const int boot = s->fresh_host ? 1 : 0;
+            s->fresh_host = false;
+            rc = enqueue_step(s, st, nullptr, boot, kStepPre);
+            if (rc == BH_OK) rc = join_inputs(s, st);
+            if (rc == BH_OK) rc = enqueue_step(s, st, nullptr, boot, kStepPost);
+        } else {
+            rc = enqueue_step(s, st);
+        }
         if (rc != BH_OK) return rc;
         s->caller_order = false;
         if (s->energy_every > 0 && ++s->energy_steps % s->energy_every == 0) {
@@ -1037,6 +1173,7 @@ int bh_step(bh_system* s, int steps, void* stream) {
 int bh_sync(bh_system* s, void* stream) {
     if (!s) return BH_ERR_ARG;
     CK(cudaSetDevice(s->device));
+    RC(join_inputs(s, (cudaStream_t)stream));
     CK(cudaStreamSynchronize((cudaStream_t)stream));
     int bits = 0;
     CK(cudaMemcpy(&bits, s->status, sizeof(int), cudaMemcpyDeviceToHost));
@@ -1047,6 +1184,7 @@ int bh_get_stats(bh_system* s, bh_stats* out, void* stream) {
     if (!s || !out) return BH_ERR_ARG;
     std::memset(out, 0, sizeof(*out));
     CK(cudaSetDevice(s->device));
+    RC(join_inputs(s, (cudaStream_t)stream));
     CK(cudaStreamSynchronize((cudaStream_t)stream));
     int bits = 0;
     unsigned long long inter[2] = {0, 0};
@@ -1098,6 +1236,7 @@ int bh_render(bh_system* s, int width, int height, float x0, float x1, float y0,
         return BH_ERR_ARG;
     if (!s->have_state) return BH_ERR_STATE;
     CK(cudaSetDevice(s->device));
+    RC(join_inputs(s, (cudaStream_t)stream));
     cudaStream_t st = (cudaStream_t)stream;
     const size_t pixels = (size_t)width * height;
     if (pixels > s->image_pixels) {
@@ -1122,6 +1261,7 @@ int bh_check(bh_system* s, void* stream, unsigned* failed) {
     if (!s || !failed) return BH_ERR_ARG;
     if (!s->have_state || s->caller_order || !s->kfinal) return BH_ERR_STATE;  // needs a step
     CK(cudaSetDevice(s->device));
+    RC(join_inputs(s, (cudaStream_t)stream));
     cudaStream_t st = (cudaStream_t)stream;
     const int n = s->n;
     // scratch: the key buffer the last sort did not end in, and the arrival counters
@@ -1149,6 +1289,7 @@ int bh_check(bh_system* s, void* stream, unsigned* failed) {
 int bh_get_debug(bh_system* s, const char* name, void* host_out, size_t bytes, void* stream) {
     if (!s || !name || !host_out) return BH_ERR_ARG;
     CK(cudaSetDevice(s->device));
+    RC(join_inputs(s, (cudaStream_t)stream));
     CK(cudaStreamSynchronize((cudaStream_t)stream));
     const size_t N = (size_t)s->n;
     const void* src = nullptr;
@@ -1203,6 +1344,7 @@ int bh_step_profiled(bh_system* s, void* stream, float* phase_ms) {
     if (!s || !phase_ms) return BH_ERR_ARG;
     if (!s->have_state) return BH_ERR_STATE;
     CK(cudaSetDevice(s->device));
+    RC(join_inputs(s, (cudaStream_t)stream));
     cudaStream_t st = (cudaStream_t)stream;
     cudaEvent_t ev[BH_NUM_PHASES + 1];
     for (auto& e : ev) CK(cudaEventCreate(&e));
@@ -1226,6 +1368,7 @@ int bh_direct_sum_f64(bh_system* s, int ns, const int* idx, double* ax, double* 
     for (int k = 0; k < ns; ++k)
         if (idx[k] < 0 || idx[k] >= s->n) return BH_ERR_ARG;
     CK(cudaSetDevice(s->device));
+    RC(settle_inputs(s));
     const BodyPtrs& c = s->st[0];
     BodyPtrs& t = s->st[1];
     bool mixed = s->p.mode == BH_MODE_MIXED;
@@ -1382,6 +1525,7 @@ int bh_energy(bh_system* s, void* stream, double* out) {
     if (!s || !out) return BH_ERR_ARG;
     if (!s->have_state) return BH_ERR_STATE;
     CK(cudaSetDevice(s->device));
+    RC(join_inputs(s, (cudaStream_t)stream));
     cudaStream_t st = (cudaStream_t)stream;
     int rc = enqueue_energy(s, st);
     if (rc != BH_OK) return rc;
@@ -1457,6 +1601,7 @@ int bh_get_energy_log(bh_system* s, double* out, int max_records, int* records, 
     *records = 0;
     if (!s->energy_every) return BH_OK;
     CK(cudaSetDevice(s->device));
+    RC(join_inputs(s, (cudaStream_t)stream));
     CK(cudaStreamSynchronize((cudaStream_t)stream));
     int count = 0;
     CK(cudaMemcpy(&count, s->elog_count, sizeof(int), cudaMemcpyDeviceToHost));
@@ -1476,6 +1621,7 @@ int bh_autotune(bh_system* s, void* stream, bh_params* chosen) {
     if (!s) return BH_ERR_ARG;
     if (!s->have_state) return BH_ERR_STATE;
     CK(cudaSetDevice(s->device));
+    RC(join_inputs(s, (cudaStream_t)stream));
     cudaStream_t st = (cudaStream_t)stream;
     const size_t N = (size_t)s->n;
     // back up the state the candidates will all start from

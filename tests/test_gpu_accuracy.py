@@ -237,6 +237,32 @@ def test_set_accel_skips_bootstrap(bh):
         assert np.allclose(st2[k], st2b[k], rtol=0, atol=1e-6 * np.abs(st2[k]).max()), k
 
 
+@pytest.mark.parametrize("mode", ["plain", "mixed"])
+def test_kept_group_costs_change_no_result(bh, mode):
+    """bh_set_state on a handle that has stepped keeps the bodies' walk-group
+    costs (by caller index) to schedule the heaviest groups first; the step
+    that follows is bit-identical to the same state's step on a new handle."""
+    from stellarsolver_gb300 import models
+
+    s0 = models.plummer(1 << 15, 31)
+    s1 = models.plummer(1 << 15, 32)
+    kw = dict(mode=mode, eps2=1e-4, timestep=1e-4)
+    with bh.BarnesHutSystem(len(s0[0]), **kw) as a:
+        a.set_state(*s0)
+        a.step(2)
+        a.set_state(*s1)
+        a.step(1)
+        a.sync()
+        ra = a.get_state()
+    with bh.BarnesHutSystem(len(s1[0]), **kw) as b:
+        b.set_state(*s1)
+        b.step(1)
+        b.sync()
+        rb = b.get_state()
+    for k in ("x", "y", "vx", "vy"):
+        assert np.array_equal(ra[k].view(np.uint32), rb[k].view(np.uint32)), k
+
+
 def test_energy_and_momentum_fp64(bh, oracle):
     """bh_energy against the exact FP64 O(N^2) sums: kinetic energy and momentum
     to 1e-12 (same float inputs, FP64 sums), potential to 1e-3 (tree walk,
