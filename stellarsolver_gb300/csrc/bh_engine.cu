@@ -664,7 +664,7 @@ __global__ void k_keep_cost(int n, const int* __restrict__ id, const int* __rest
 
 // kept: costs from k_keep_cost, or NULL for none (every group of equal weight)
 __global__ void k_state_init(int n, int* id, float* xlo, float* ylo, float* ax, float* ay,
-                             float* amag, int* gcost, const int* kept, int* status, int* fresh) {
+                             float* amag, int* gcost, const int* kept, int* fresh) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
         id[i] = i;
@@ -675,10 +675,7 @@ __global__ void k_state_init(int n, int* id, float* xlo, float* ylo, float* ax, 
         amag[i] = 0.0f;
         gcost[i] = kept ? kept[i] : 0;
     }
-    if (i == 0) {
-        *status = 0;
-        *fresh = 1;
-    }
+    if (i == 0) *fresh = 1;
 }
 
 // out[id[j]] = in[j] for up to four arrays
@@ -964,6 +961,7 @@ int bh_set_params(bh_system* s, const bh_params* p) {
     if (mode_change && s->have_state) {
         // lo words only exist in MIXED mode; start them at zero
         CK(cudaSetDevice(s->device));
+        RC(settle_inputs(s));
         CK(cudaMemset(s->st[0].xlo, 0, sizeof(float) * s->n));
         CK(cudaMemset(s->st[0].ylo, 0, sizeof(float) * s->n));
     }
@@ -985,27 +983,33 @@ int bh_set_state(bh_system* s, const float* x, const float* y, const float* vx, 
     cudaStream_t st = (cudaStream_t)stream;
     const size_t b = sizeof(float) * s->n;
     const BodyPtrs& c = s->st[0];
-    // x and y on `stream`: the next step's box and keys read them.  vx, vy and
-    // mass, read first by the reorder, go on the copy stream and overlap the
-    // box, keys and sort; the next call on the handle joins them.
+    // x and y on `stream`: the next step's box and keys read them.  What only
+    // the reorder reads first goes on the copy stream and overlaps the box,
+    // keys and sort; the next call on the handle joins it:
+    // - the initialisation of the other body arrays, while x and y are copied
+    //   (a handle that held a state keeps its bodies' walk-group costs, by
+    //   caller index);
+    // - then vx, vy and mass.
+    RC(copy_stream_after(s, st));
+    const int* kept = nullptr;
+    if (s->have_state && s->p.mode != BH_MODE_REFERENCE) {
+        k_keep_cost<<<(s->n + 255) / 256, 256, 0, s->copy_stream>>>(s->n, c.id, c.gcost,
+                                                                    s->st[1].gcost);
+        CK(cudaGetLastError());
+        kept = s->st[1].gcost;
+    }
+    k_state_init<<<(s->n + 255) / 256, 256, 0, s->copy_stream>>>(
+        s->n, c.id, c.xlo, c.ylo, s->ax, s->ay, c.amag, c.gcost, kept, s->fresh);
+    CK(cudaGetLastError());
+    CK(cudaMemsetAsync(s->status, 0, sizeof(int), st));
     CK(cudaMemcpyAsync(c.x, x, b, cudaMemcpyDefault, st));
     CK(cudaMemcpyAsync(c.y, y, b, cudaMemcpyDefault, st));
-    RC(copy_stream_after(s, st));
+    RC(copy_stream_after(s, st));  // the link is free again
     CK(cudaMemcpyAsync(c.vx, vx, b, cudaMemcpyDefault, s->copy_stream));
     CK(cudaMemcpyAsync(c.vy, vy, b, cudaMemcpyDefault, s->copy_stream));
     CK(cudaMemcpyAsync(c.m, mass, b, cudaMemcpyDefault, s->copy_stream));
     CK(cudaEventRecord(s->in_event, s->copy_stream));
     s->in_pending = true;
-    // a handle that held a state keeps its bodies' walk-group costs (by caller index)
-    const int* kept = nullptr;
-    if (s->have_state && s->p.mode != BH_MODE_REFERENCE) {
-        k_keep_cost<<<(s->n + 255) / 256, 256, 0, st>>>(s->n, c.id, c.gcost, s->st[1].gcost);
-        CK(cudaGetLastError());
-        kept = s->st[1].gcost;
-    }
-    k_state_init<<<(s->n + 255) / 256, 256, 0, st>>>(s->n, c.id, c.xlo, c.ylo, s->ax, s->ay,
-                                                     c.amag, c.gcost, kept, s->status, s->fresh);
-    CK(cudaGetLastError());
     s->have_state = true;
     s->caller_order = true;
     s->fresh_host = true;
