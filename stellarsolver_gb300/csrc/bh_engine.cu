@@ -54,7 +54,7 @@ constexpr int kMaxBucket = 32;
 constexpr int kMaxWalkSmem = 8 * (3 * 32 * 16 + 32 * 8 * 2 + 16 + 64 * 4 + kMaxStack * 4 +
                                   (32 + 32 * kMaxBucket) * 4);
 constexpr int kBboxThreads = 256;
-constexpr int kBboxChunk = 8192;
+constexpr int kBboxChunk = 2048;
 
 int walk_grid_cap(int device_sms, int blocks_per_sm) { return device_sms * std::max(1, blocks_per_sm); }
 
