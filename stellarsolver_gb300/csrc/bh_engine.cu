@@ -265,6 +265,9 @@ struct bh_system {
 
     cudaStream_t cap_stream = nullptr;
     cudaStream_t cond_stream = nullptr;  // captures the body of the sort's conditional node
+    // a graph branch beside the tree build: the reorder (captures only)
+    cudaStream_t fork_stream = nullptr;
+    cudaEvent_t fork_event = nullptr, join_event = nullptr;
     // Step graphs: [0] / [1] one step without / with the bootstrap pass; [2] the
     // step up to the sort; [3] / [4] the rest, without / with the bootstrap pass
     // (the first step after bh_set_state: the input copies join in between).
@@ -488,9 +491,23 @@ int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev,
         src.amag = dst.amag = nullptr;
         src.gcost = dst.gcost = nullptr;
     }
-    CK(launch_pdl(k_gather, nb, tb, 0, st, n, va, src, dst));
+    // The reorder and the tree build both start from the sort and write
+    // disjoint arrays; in a graph they are two branches that run side by side
+    // (the build is instruction-bound, the reorder waits on memory).
+    cudaStreamCaptureStatus cstat = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(st, &cstat));
+    const bool fork = cstat == cudaStreamCaptureStatusActive && s->fork_stream;
+    if (fork) {
+        CK(cudaEventRecord(s->fork_event, st));
+        CK(cudaStreamWaitEvent(s->fork_stream, s->fork_event, 0));
+        CK(launch_plain(k_gather, nb, tb, 0, s->fork_stream, n, va, src, dst));
+        CK(cudaEventRecord(s->join_event, s->fork_stream));
+    } else {
+        CK(launch_pdl(k_gather, nb, tb, 0, st, n, va, src, dst));
+    }
     CK(mark(4));
     CK(launch_pdl(k_build, nb, tb, 0, st, ka, n, segs, s->tree, s->status));
+    if (fork) CK(cudaStreamWaitEvent(st, s->join_event, 0));
     CK(mark(5));
     CK(launch_pdl(k_moments, (n + kMomentsThreads - 1) / kMomentsThreads, kMomentsThreads, 0, st, n,
                   accuracy ? 1 : 0, dst.x, dst.y, dst.m, s->tree.climb, s->tree.leaf_parent,
@@ -603,6 +620,15 @@ __global__ void k_direct_reduce(int ns, int chunks, const double* __restrict__ p
     out[t] = G * acc;
 }
 
+// The stream and events of the reorder's graph branch (created before a capture).
+int make_fork_stream(bh_system* s) {
+    if (s->fork_stream) return BH_OK;
+    CK(cudaStreamCreateWithFlags(&s->fork_stream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&s->fork_event, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&s->join_event, cudaEventDisableTiming));
+    return BH_OK;
+}
+
 // The copy stream starts its next copy after the work enqueued on `st` so far.
 int copy_stream_after(bh_system* s, cudaStream_t st) {
     if (!s->copy_stream) {
@@ -635,6 +661,7 @@ int settle_inputs(bh_system* s) {
 int build_graph(bh_system* s, int slot) {
     if (!s->cap_stream) CK(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
     if (!s->cond_stream) CK(cudaStreamCreateWithFlags(&s->cond_stream, cudaStreamNonBlocking));
+    RC(make_fork_stream(s));
     const int part = slot < 2 ? kStepAll : slot == 2 ? kStepPre : kStepPost;
     const int boot = (slot == 1 || slot == 4) ? 1 : 0;
     CK(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal));
@@ -945,6 +972,11 @@ int bh_destroy(bh_system* s) {
     drop_graph(s);
     if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
     if (s->cond_stream) cudaStreamDestroy(s->cond_stream);
+    if (s->fork_stream) {
+        cudaStreamDestroy(s->fork_stream);
+        cudaEventDestroy(s->fork_event);
+        cudaEventDestroy(s->join_event);
+    }
     cudaFree(s->image);
     cudaFree(s->elog);
     cudaFree(s->elog_count);
@@ -1562,6 +1594,7 @@ int enqueue_energy_log(bh_system* s, cudaStream_t st) {
 int build_energy_graph(bh_system* s) {
     if (!s->cap_stream) CK(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
     if (!s->cond_stream) CK(cudaStreamCreateWithFlags(&s->cond_stream, cudaStreamNonBlocking));
+    RC(make_fork_stream(s));
     CK(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal));
     int st = enqueue_energy_log(s, s->cap_stream);
     cudaGraph_t g = nullptr;
