@@ -605,12 +605,14 @@ __global__ void __launch_bounds__(WARPS * 32) k_frontier(Segs segs, int nsupers,
         bool open = false;
         int4 C = make_int4(kNoChild, kNoChild, kNoChild, kNoChild);
         if (node >= 0) {
+            // the children's record with the node's: one L2 round trip per round
             const float4 A = recA[node];
             const int4 D = recD[node];
+            const int4 Cn = recC[node];
             const float fx = fmaxf(fabsf(A.x - bx0), fabsf(A.x - bx1));
             const float fy = fmaxf(fabsf(A.y - by0), fabsf(A.y - by1));
             if (D.y > bucket && fmaf(fx, fx, fy * fy) <= A.w) {
-                C = recC[node];
+                C = Cn;
                 open = (C.x >= 0 || C.x == kNoChild) && (C.y >= 0 || C.y == kNoChild) &&
                        (C.z >= 0 || C.z == kNoChild) && (C.w >= 0 || C.w == kNoChild);
             }
