@@ -410,14 +410,15 @@ int enqueue_sort(bh_system* s, cudaStream_t st, cudaEvent_t* ev, bool keep_stats
         CK(cudaStreamGetCaptureInfo(st, &cstat, nullptr, &cgraph, nullptr, nullptr, nullptr));
         CK(cudaGraphConditionalHandleCreate(&cond, cgraph, 0, cudaGraphCondAssignDefault));
     }
-    // high words: k0 -> kA -> kB -> kA -> kB
+    // high words: k0 -> ... -> kB (the last pass writes kB, the fixup kA)
     {
         const uint64_t* ki = k0;
         const uint32_t* vi = v0;
-        for (int ps = 0; ps < 4; ++ps) {
-            uint64_t* ko = (ps & 1) ? kB : kA;
-            uint32_t* vo = (ps & 1) ? vB : vA;
-            CK(pass(pdl, st, ki, vi, ko, vo, 32 + 8 * ps, 0, nullptr));
+        for (int ps = 0; ps < kHighPasses; ++ps) {
+            const bool to_a = ((kHighPasses - 1 - ps) & 1) != 0;
+            uint64_t* ko = to_a ? kA : kB;
+            uint32_t* vo = to_a ? vA : vB;
+            CK(pass(pdl, st, ki, vi, ko, vo, kHighShift + 8 * ps, 0, nullptr));
             ki = ko;
             vi = vo;
         }

@@ -1,6 +1,6 @@
-"""The engine's sort on the GPU: stable passes over the key's high 32 bits,
-then each run of equal high words ordered by the whole key; a run longer than
-256 bodies (bodies packed into one 2^-16 cell of the box) sends the step to
+"""The engine's sort on the GPU: stable passes over the key's top 24 bits (the
+high word), then each run of equal high words ordered by the whole key; a run
+longer than 256 bodies (bodies packed into one 2^-12 cell of the box) sends the step to
 the full 8-pass sort, behind a conditional node in a graph replay and as
 kernels gated by a device flag in stream order.
 
@@ -23,7 +23,7 @@ def bh():
 
 def clustered(n, packed, seed):
     """n - packed bodies spread over a few units, plus `packed` bodies 1e-8
-    apart near (1e-3, 2e-3): one 2^-16 cell of the box, distinct keys at 32
+    apart near (1e-3, 2e-3): one 2^-12 cell of the box, distinct keys at 32
     levels."""
     rng = np.random.default_rng(seed)
     x = rng.standard_normal(n).astype(np.float32)
@@ -45,7 +45,7 @@ def test_permutation_bit_exact(bh, oracle, graph, packed):
     x, y, vx, vy, m = clustered(n, packed, 11 + packed)
     box = oracle.bbox(x, y)
     k = oracle.keys(x, y, box)
-    hi = k >> np.uint64(32)
+    hi = k >> np.uint64(40)  # the high word: the top 24 bits
     _, runs = np.unique(hi, return_counts=True)
     if packed == 600:
         assert runs.max() > 256  # the case that needs the full sort
