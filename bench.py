@@ -221,7 +221,8 @@ def run_engine(args):
     walk_flops = roofline.walk_flops(stats)
     achieved = walk_flops / (walk_ms * 1e-3) / 1e12
     traffic = recorded_traffic("walk")
-    pb = roofline.phase_bytes(n, args.mode == "mixed", accuracy=args.mode != "reference")
+    pb = roofline.phase_bytes(n, args.mode == "mixed", passes=roofline.high_passes(n),
+                              accuracy=args.mode != "reference")
     phases = {}
     for i, name in enumerate(bh.PHASES):
         ms = float(phase_ms[i])

@@ -452,20 +452,21 @@ static __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(
     }
 }
 
-// The sort's fast path: kHighPasses stable 8-bit passes over the key's top
-// bits (the high word: bits kHighShift..63, the first 12 quadtree levels),
-// then k_sort_fixup.  Elements with equal high words then form runs in input
-// order; each run is put in whole-key order with ties kept in input order,
-// which gives the stable sort by the whole key.  Element i's place in its run
-// is the number of run members before it in that order.  A run longer than
+// The sort's fast path: P stable 8-bit passes over the key's top 8P bits (the
+// high word, bits `shift` = 64 - 8P .. 63), then k_sort_fixup.  Elements with
+// equal high words then form runs in input order; each run is put in
+// whole-key order with ties kept in input order, which gives the stable sort
+// by the whole key.  Element i's place in its run is the number of run members
+// before it in that order, so the fixup's work grows with the run lengths: P
+// is 3 (runs of one 2^-12 box cell) for systems up to kShortSortMax bodies and
+// 4 (2^-16 cells) above, where the bodies per cell grow.  A run longer than
 // kFixupRun is not ordered: *overflow is set, and (set_cond, graph replay) the
 // conditional node that holds the full sort is switched on; exactly one
 // thread does either.
-constexpr int kHighPasses = 3;
-constexpr int kHighShift = 64 - 8 * kHighPasses;
+constexpr int kShortSortMax = 1 << 21;
 constexpr int kFixupRun = 256;
 
-static __global__ void k_sort_fixup(int n, const uint64_t* __restrict__ kin,
+static __global__ void k_sort_fixup(int n, int shift, const uint64_t* __restrict__ kin,
                                     const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
                                     uint32_t* __restrict__ vout, int* __restrict__ overflow,
                                     cudaGraphConditionalHandle cond, int set_cond) {
@@ -473,17 +474,17 @@ static __global__ void k_sort_fixup(int n, const uint64_t* __restrict__ kin,
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint64_t k = kin[i];
-    const uint32_t hi = (uint32_t)(k >> kHighShift);
-    const bool left = i > 0 && (uint32_t)(kin[i - 1] >> kHighShift) == hi;
-    const bool right = i + 1 < n && (uint32_t)(kin[i + 1] >> kHighShift) == hi;
+    const uint32_t hi = (uint32_t)(k >> shift);
+    const bool left = i > 0 && (uint32_t)(kin[i - 1] >> shift) == hi;
+    const bool right = i + 1 < n && (uint32_t)(kin[i + 1] >> shift) == hi;
     if (!left && !right) {
         kout[i] = k;
         vout[i] = vin[i];
         return;
     }
     int a = i, b = i + 1;
-    while (a > 0 && (uint32_t)(kin[a - 1] >> kHighShift) == hi && i - a < kFixupRun) --a;
-    while (b < n && (uint32_t)(kin[b] >> kHighShift) == hi && b - i <= kFixupRun) ++b;
+    while (a > 0 && (uint32_t)(kin[a - 1] >> shift) == hi && i - a < kFixupRun) --a;
+    while (b < n && (uint32_t)(kin[b] >> shift) == hi && b - i <= kFixupRun) ++b;
     if (b - a > kFixupRun) {
         if (atomicCAS(overflow, 0, 1) == 0 && set_cond) cudaGraphSetConditional(cond, 1u);
         return;

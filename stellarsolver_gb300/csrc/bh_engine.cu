@@ -247,6 +247,7 @@ struct bh_system {
     bool fresh_host = false;  // the host's record of *fresh: the bootstrap pass is launched
                               // only in steps that follow bh_set_state
     int seg_passes = 0;
+    int high_passes = 4;  // radix passes of the sort's fast path (k_sort_fixup)
 
     int walk_grid_ref = 0, walk_grid_acc = 0;
     bool have_state = false;
@@ -414,16 +415,17 @@ int enqueue_sort(bh_system* s, cudaStream_t st, cudaEvent_t* ev, bool keep_stats
     {
         const uint64_t* ki = k0;
         const uint32_t* vi = v0;
-        for (int ps = 0; ps < kHighPasses; ++ps) {
-            const bool to_a = ((kHighPasses - 1 - ps) & 1) != 0;
+        for (int ps = 0; ps < s->high_passes; ++ps) {
+            const bool to_a = ((s->high_passes - 1 - ps) & 1) != 0;
             uint64_t* ko = to_a ? kA : kB;
             uint32_t* vo = to_a ? vA : vB;
-            CK(pass(pdl, st, ki, vi, ko, vo, kHighShift + 8 * ps, 0, nullptr));
+            CK(pass(pdl, st, ki, vi, ko, vo, 64 - 8 * (s->high_passes - ps), 0, nullptr));
             ki = ko;
             vi = vo;
         }
     }
-    CK(launch_pdl(k_sort_fixup, nb, tb, 0, st, n, kB, vB, kA, vA, overflow, cond, capturing ? 1 : 0));
+    CK(launch_pdl(k_sort_fixup, nb, tb, 0, st, n, 64 - 8 * s->high_passes, kB, vB, kA, vA, overflow,
+                  cond, capturing ? 1 : 0));
     if (capturing) {
         const cudaGraphNode_t* deps = nullptr;
         size_t ndeps = 0;
@@ -767,6 +769,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     const size_t N = (size_t)s->n;
     s->tiles = (int)((N + kSortTile - 1) / kSortTile);
     s->seg_passes = nseg == 1 ? 0 : (nseg <= 256 ? 1 : 2);
+    s->high_passes = *std::max_element(sizes, sizes + nseg) <= kShortSortMax ? 3 : 4;
 
     // chunk table for the box reduction and group table for the walks
     std::vector<int> cseg, cbeg, cend, goff(nseg + 1, 0), goff2(nseg + 1, 0), soff(nseg + 1, 0);

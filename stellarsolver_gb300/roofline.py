@@ -21,10 +21,16 @@ def walk_flops(stats: dict) -> int:
     return FLOPS_P2P * (stats["interactions"] - cells) + FLOPS_P2M * cells
 
 
+def high_passes(largest_system: int) -> int:
+    """Radix passes of the sort's fast path: 3 (top 24 key bits) for systems
+    up to 2^21 bodies, 4 (top 32 bits) above."""
+    return 3 if largest_system <= 1 << 21 else 4
+
+
 def phase_bytes(n: int, mixed: bool, passes: int = 3, accuracy: bool = True) -> dict:
     """Algorithmic bytes per launch of each HBM-bound phase (each array once).
-    The sort: `passes` radix passes over the key's high word (its top 24
-    bits) and the run fixup, each one read and one write of (key, index).  The reorder moves
+    The sort: `passes` radix passes over the key's high word and the run
+    fixup, each one read and one write of (key, index).  The reorder moves
     x, y, vx, vy, m, id (and the hi/lo tails in MIXED mode, |a_old| and the
     walk-group cost in the accuracy modes) and reads the permutation."""
     lo = 16 * n if mixed else 0

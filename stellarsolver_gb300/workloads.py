@@ -124,7 +124,7 @@ def plummer24(args) -> dict:
                     s.step_profiled(phase_ms)
                 phase_ms /= 3
                 st = s.stats()
-            pb = roofline.phase_bytes(n, mode == "mixed")
+            pb = roofline.phase_bytes(n, mode == "mixed", passes=roofline.high_passes(n))
             phases = {}
             for i, name in enumerate(bh.PHASES):
                 ms = float(phase_ms[i])

@@ -1,6 +1,7 @@
 """The engine's sort on the GPU: stable passes over the key's top 24 bits (the
-high word), then each run of equal high words ordered by the whole key; a run
-longer than 256 bodies (bodies packed into one 2^-12 cell of the box) sends the step to
+high word; top 32 bits for systems over 2^21 bodies), then each run of equal
+high words ordered by the whole key; a run longer than 256 bodies (bodies
+packed into one 2^-12 cell of the box) sends the step to
 the full 8-pass sort, behind a conditional node in a graph replay and as
 kernels gated by a device flag in stream order.
 
@@ -113,3 +114,23 @@ def test_batch_with_a_packed_system_equals_systems_alone(bh, graph):
         sl = slice(off[k], off[k + 1])
         for key in ("x", "y", "vx", "vy"):
             assert np.array_equal(got[key][sl].view(np.uint32), ref[key].view(np.uint32)), (k, key)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_four_pass_sort_above_2e21_bodies(bh, oracle, graph):
+    """Systems over 2^21 bodies sort the top 32 key bits (4 passes) before the
+    fixup; 200 bodies in one 2^-16 cell stay within the fixup's runs."""
+    n = (1 << 21) + 1
+    x, y, vx, vy, m = clustered(n, 200, 41)
+    box = oracle.bbox(x, y)
+    k = oracle.keys(x, y, box)
+    _, runs = np.unique(k >> np.uint64(32), return_counts=True)
+    assert 200 <= runs.max() <= 256
+    operm, _ = oracle.sort_keys(k)
+    with bh.BarnesHutSystem(n, mode="plain", eps2=1e-4, timestep=0.0, use_graph=graph) as s:
+        s.set_state(x, y, vx, vy, m)
+        s.step(1)
+        s.sync()
+        assert s.stats()["status"] == 0
+        assert np.array_equal(s.debug("perm"), operm.astype(np.int32))
+        assert np.array_equal(s.debug("keys"), k[operm])
