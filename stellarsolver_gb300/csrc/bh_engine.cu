@@ -368,10 +368,11 @@ int enqueue_sort(bh_system* s, cudaStream_t st, cudaEvent_t* ev, bool keep_stats
                   s->work + kWorkSortOverflow, s->seg_cost, s->mean_cost));
     CK(mark(2));
 
-    // Sort (stable, by key, then by system): LSD passes over the key's high 32
-    // bits, then k_sort_fixup orders each run of equal high words by the whole
-    // key.  A run longer than kFixupRun (bodies packed into a 2^-16 box cell)
-    // makes the step take the full 8-pass sort from the original keys: in a
+    // Sort (stable, by key, then by system): LSD passes over the key's top
+    // 8 * high_passes bits (the high word), then k_sort_fixup orders each run
+    // of equal high words by the whole key.  A run longer than kFixupRun
+    // (bodies packed into one 2^-12 or 2^-16 box cell) makes the step take
+    // the full 8-pass sort from the original keys: in a
     // graph behind a conditional node that only the fixup switches on, in
     // stream order as kernels that return at once unless the flag is set.
     int* overflow = s->work + kWorkSortOverflow;
