@@ -482,17 +482,18 @@ static __global__ void k_sort_fixup(int n, int shift, const uint64_t* __restrict
         vout[i] = vin[i];
         return;
     }
-    int a = i, b = i + 1;
+    // the run's start, then one pass from it to the run's end that also ranks
+    int a = i;
     while (a > 0 && (uint32_t)(kin[a - 1] >> shift) == hi && i - a < kFixupRun) --a;
-    while (b < n && (uint32_t)(kin[b] >> shift) == hi && b - i <= kFixupRun) ++b;
-    if (b - a > kFixupRun) {
+    int rank = 0, j = a;
+    for (; j < n && j - a <= kFixupRun; ++j) {
+        const uint64_t kj = kin[j];
+        if ((uint32_t)(kj >> shift) != hi) break;
+        rank += (kj < k || (kj == k && j < i)) ? 1 : 0;
+    }
+    if (j - a > kFixupRun) {
         if (atomicCAS(overflow, 0, 1) == 0 && set_cond) cudaGraphSetConditional(cond, 1u);
         return;
-    }
-    int rank = 0;
-    for (int j = a; j < b; ++j) {
-        const uint64_t kj = kin[j];
-        rank += (kj < k || (kj == k && j < i)) ? 1 : 0;
     }
     kout[a + rank] = k;
     vout[a + rank] = vin[i];
