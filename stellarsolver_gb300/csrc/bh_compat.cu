@@ -912,7 +912,7 @@ extern "C" int BuildQuadTreeNoAlloc(float* x, float* y, float* mass, int* count,
                                         count, start, x, y, mass, index, w.status);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "BuildQuadTreeNoAlloc launch");
-    // wait for this build and return its device status (the scratch is shared:
+    // wait for this tree build and return its device status (the scratch is shared:
     // the next call may overwrite it as soon as this one returns)
     e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "BuildQuadTreeNoAlloc sync");
