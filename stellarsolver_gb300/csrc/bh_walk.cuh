@@ -918,7 +918,7 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
                             p2p<false>(A.x, A.y, A.z, px[b], py[b], eps2, bx[b], by[b]);
                     }
                 } else if (k == 32) {
-#pragma unroll 4
+#pragma unroll 8
                     for (int e = 0; e < 16; ++e) {
                         const float4 xy = cpair.xy[e], mh = cpair.mh[e], t01 = cpair.t01[e];
                         const float2 t11 = cpair.t11[e];
@@ -996,7 +996,7 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
                 }
                 if (eps2 > 0.0f) {
                     if (k == 32) {
-#pragma unroll 4
+#pragma unroll 8
                         for (int e = 0; e < 16; ++e) {
                             const float4 xy = bxy[e];
                             const float2 w = bm[e];
