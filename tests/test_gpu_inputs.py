@@ -88,3 +88,31 @@ def test_upload_then_read_back(bh):
         got = s.get_state()
     for key, a in zip(("x", "y", "vx", "vy", "m"), (x, y, vx, vy, m)):
         assert np.array_equal(got[key], a), key
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_overlapped_uploads_ensemble(bh, graph):
+    """The same for a batch of systems: the batched step after an overlapped
+    upload equals the one after a synchronised upload."""
+    torch = pytest.importorskip("torch")
+    from stellarsolver_gb300 import models
+
+    sizes = [3000, 40000, 1500]
+    systems = [models.plummer(n, 950 + k) for k, n in enumerate(sizes)]
+    cat = [np.concatenate([s[k] for s in systems]) for k in range(5)]
+    pin = [torch.from_numpy(a.copy()).pin_memory() for a in cat]
+    outs = []
+    for synchronise in (False, True):
+        with bh.BarnesHutSystem(sizes=sizes, mode="mixed", eps2=1e-4, timestep=1e-4,
+                                use_graph=graph) as b:
+            for _ in range(2):
+                b.set_state_ptrs(*[p.data_ptr() for p in pin])
+                if synchronise:
+                    b.sync()
+                b.step(2)
+                outs.append(b.get_state())
+                assert b.stats()["status"] == 0
+    half = len(outs) // 2
+    for a, c in zip(outs[:half], outs[half:]):
+        for key in ("x", "y", "vx", "vy"):
+            assert np.array_equal(a[key].view(np.uint32), c[key].view(np.uint32)), key
