@@ -1741,6 +1741,32 @@ int bh_autotune(bh_system* s, void* stream, bh_params* chosen) {
                 }
             }
         }
+        // The sort's fast path with the chosen walk: 3 or 4 high-word passes.
+        // The fixup's work grows with the bodies per 2^-12 cell, so the better
+        // count depends on the density, not only on N; the size rule's choice
+        // stays unless the other steps more than 1 % faster.
+        const int size_rule = s->high_passes;
+        float pass_ms[2] = {0.f, 0.f};
+        for (int hp = 3; hp <= 4 && rc == BH_OK; ++hp) {
+            bh_params cand = best;
+            cand.use_graph = 0;
+            s->p = cand;
+            s->high_passes = hp;
+            drop_graph(s);
+            rc = restore();
+            if (rc == BH_OK) rc = enqueue_step(s, st);
+            if (rc != BH_OK) break;
+            CK(cudaEventRecord(e0, st));
+            for (int k = 0; k < 2 && rc == BH_OK; ++k) rc = enqueue_step(s, st);
+            CK(cudaEventRecord(e1, st));
+            CK(cudaEventSynchronize(e1));
+            CK(cudaEventElapsedTime(&pass_ms[hp - 3], e0, e1));
+        }
+        s->high_passes = size_rule;
+        if (rc == BH_OK) {
+            const float keep = pass_ms[size_rule - 3], other = pass_ms[4 - size_rule];
+            if (other < 0.99f * keep) s->high_passes = 7 - size_rule;
+        }
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
     }

@@ -312,6 +312,9 @@ def test_autotune_keeps_results_and_accuracy(bh, oracle):
         s.step(1)
         s.sync()
         ax, ay = s.get_accel()
+        # the sort pass count the autotuner kept gives the oracle's permutation
+        operm, _ = oracle.sort_keys(oracle.keys(x, y, oracle.bbox(x, y)))
+        assert np.array_equal(s.debug("perm"), operm.astype(np.int32))
     rms, mx = force_error(oracle, x, y, m, ax, ay, 1e-4)
     assert rms <= 1e-3, (rms, mx)
 
