@@ -13,9 +13,11 @@ force walk fused with the integration.
           copies in from pinned host memory the state the reference's reset()
           uploads (x, y, vx, vy, ax, ay, mass), steps, and reads the
           positions back.
-  roofline  the force walk against the measured FP32 FMA peak (14 flops per
-          body-body and 33 per body-cell interaction); per-phase HBM
-          fractions beside it.
+  roofline  the force walk (k_walk_acc alone) against the measured FP32 FMA
+          peak, 14 flops per body-node interaction; the executed count with
+          quadrupole cells at 33 flops beside it, and per-phase HBM fractions.
+  reference_mode  the reference's own walk rule (monopole warp vote) on the
+          GPU, same workload: the like-for-like figure for the reference arm.
   ensemble  256 systems, N log-uniform in [2^10, 2^17]: the batched MIXED
           engine against one PLAIN handle per system.
 
@@ -219,10 +221,13 @@ def run_engine(args):
         sysm.step_profiled(phase_ms, sp)
     phase_ms /= prof_steps
     sysm.sync(sp)
-    walk_ms = float(phase_ms[bh.PHASES.index("walk")])
-    fp32_peak = bh.measure_fp32_peak(local)
-    walk_flops = roofline.walk_flops(stats)
+    walk_ms = float(phase_ms[bh.PHASES.index("walk")])  # k_walk_acc alone
+    peaks = bh.measure_fp32_peaks(local)
+    fp32_peak = max(peaks.values())
+    walk_flops = roofline.walk_flops(stats)  # 14 per interaction
+    walk_flops_mp = roofline.walk_flops_with_multipole(stats)
     achieved = walk_flops / (walk_ms * 1e-3) / 1e12
+    achieved_mp = walk_flops_mp / (walk_ms * 1e-3) / 1e12
     traffic = recorded_traffic("walk")
     pb = roofline.phase_bytes(n, args.mode == "mixed", passes=roofline.high_passes(n),
                               accuracy=args.mode != "reference")
@@ -239,6 +244,21 @@ def run_engine(args):
     # ---------------------------------------------------------------- e2e through the C ABI
     e2e = run_e2e(bh, torch, stream, sp, n, x, y, vx, vy, m, sysm.params, local, args)
     sysm.close()
+    # the reference's own rule on the GPU (REFERENCE mode: monopole warp-vote walk,
+    # the interaction set of kernels.cu:340-435), same workload, graph replay: the
+    # like-for-like figure beside the --impl reference arm
+    with bh.BarnesHutSystem(n, device=local, mode="reference", use_graph=True, **common) as s:
+        s.set_state(x, y, vx, vy, m)
+        for _ in range(args.warmup):
+            s.step(1, sp)
+        s.sync(sp)
+        ref_secs = timed_steps(s, args.steps)
+        ref_inter = s.stats(sp)["interactions"]
+    reference_mode = {"steps_per_s": round(args.steps / ref_secs, 3),
+                      "ms_per_step": round(1e3 * ref_secs / args.steps, 4),
+                      "interactions_per_step": ref_inter,
+                      "rule": "reference warp vote (monopole, kernels.cu:395-411), CUDA graph, "
+                              "L2 flushed before every timed step"}
     ens = None
     if not args.no_ensemble:
         ens = run_ensemble(bh, torch, stream, sp, local, world, rank, args)
@@ -264,6 +284,7 @@ def run_engine(args):
         "interactions_per_step": stats["interactions"],
         "cell_interactions_per_step": stats["cell_interactions"],
         "walk_flops_per_step": walk_flops,
+        "walk_flops_with_multipole_per_step": walk_flops_mp,
         "interactions_per_s": round(stats["interactions"] * value / world, 1) * world,
         "force_error_vs_fp64": errors,
         "plain_fp32": {"steps_per_s_graph": round(sides["plain_graph"], 3),
@@ -271,12 +292,21 @@ def run_engine(args):
                            round(sides["plain_single_system_nograph"], 3),
                        "interactions_per_step": inter["plain"]},
         "mixed_over_plain_single_system": round(value / world / sides["plain_single_system_nograph"], 3),
+        "reference_mode": reference_mode,
         "momentum_drift_rel": float(np.abs(p1 - p0).max() / pscale),
         "tree": {"cells": stats["cells"], "nodes": stats["nodes"], "max_depth": stats["max_depth"]},
         "roofline": {"bound": "fp32", "kernel": "k_walk_acc", "achieved": round(achieved, 3),
                      "peak": round(fp32_peak, 2), "unit": "TFLOP/s",
                      "frac": round(achieved / fp32_peak, 4),
-                     "peak_source": "measured FFMA probe (bh_measure_fp32_peak)",
+                     "flops_per_interaction": roofline.FLOPS_P2P,
+                     "walk_ms": round(walk_ms, 4),
+                     "rule": "achieved = 14 flops x interactions_per_step / walk_ms "
+                             "(k_walk_acc alone, CUDA events on its stream)",
+                     "achieved_with_multipole": round(achieved_mp, 3),
+                     "frac_with_multipole": round(achieved_mp / fp32_peak, 4),
+                     "peak_source": "measured in-process: max of FFMA and FFMA2 chain probes "
+                                    "(bh_measure_fp32_peaks)",
+                     "peak_probes": {k: round(v, 2) for k, v in peaks.items()},
                      "traffic": traffic, "phases": phases,
                      "hbm_peak_gbs": hbm_peak, "hbm_peak_source": hbm_kind},
         "e2e": e2e,
@@ -422,18 +452,24 @@ def run_ensemble(bh, torch, stream, sp, local, world, rank, args):
             "interactions_per_s": round(inter / t_batch, 1)}
 
 
+CPU_BASELINE_STEPS = 5
+
+
 def cpu_baseline(x, y, vx, vy, m):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as po
 
     po.lib()
+    state = (x, y, vx, vy)
     t0 = time.perf_counter()
-    po.step_ref(x, y, vx, vy, m, THETA, EPS * EPS, DT, 1.0)
+    for _ in range(CPU_BASELINE_STEPS):
+        state = po.step_ref(*state, m, THETA, EPS * EPS, DT, 1.0)[:4]
     secs = time.perf_counter() - t0
-    return {"value": round(1.0 / secs, 4), "unit": "steps/s", "cores": po.num_threads(),
-            "kind": "port",
-            "sample": f"1 full reference-rule step of the {WORKLOAD} workload (box, keys, sort, "
-                      "tree, centre of mass, warp-vote walk, update), OpenMP over all host threads"}
+    return {"value": round(CPU_BASELINE_STEPS / secs, 4), "unit": "steps/s",
+            "cores": po.num_threads(), "kind": "port",
+            "sample": f"{CPU_BASELINE_STEPS} consecutive full reference-rule steps of the "
+                      f"{WORKLOAD} workload (box, keys, sort, tree, centre of mass, warp-vote "
+                      "walk, update), OpenMP over all host threads"}
 
 
 def run_reference(args):

@@ -94,13 +94,19 @@ void bh_compat_release(void);
  * every GPU that loads the library holds until the process exits.
  *   - Same arguments and outputs as BuildQuadTree.  Returns a BH_* status:
  *     BH_ERR_CAPACITY for n > 65536 (see bh_last_error), else the build's
- *     device status.
- *   - Synchronous: waits on the compat stream before it returns.
+ *     device status.  A failure is also recorded for bh_compat_status().
+ *   - Synchronous: it waits on the compat stream and copies its status word
+ *     to the host before it returns, so it cannot be called while a stream is
+ *     being captured or a CUDA graph is being built.
  *   - The first call on a device resolves the array's device address
- *     (cudaGetSymbolAddress).  Make that first call before any stream capture.
+ *     (cudaGetSymbolAddress) once for that device.
  *   - All calls share the one array and it keeps the last call's contents.
  *     Calls that overlap on the GPU (other host threads, other streams) race;
- *     serialise them. */
+ *     serialise them.
+ *   - Only this tree build is free of allocation.  ComputeBoundingBox,
+ *     SortParticles and CalculateForces (and BuildQuadTree) still keep a
+ *     cudaMalloc'ed workspace per device, allocated on their first call and
+ *     grown when a larger layout needs it; bh_compat_release frees it. */
 int BuildQuadTreeNoAlloc(float *x, float *y, float *mass, int *count, int *start, int *child,
                          int *index, float *left, float *right, float *bottom, float *top, int n,
                          int m);

@@ -205,11 +205,13 @@ int bh_check(bh_system* s, void* stream, unsigned* failed);
 int bh_get_debug(bh_system* s, const char* name, void* host_out, size_t bytes, void* stream);
 
 /* Phases timed by bh_step_profiled, in order. */
-#define BH_NUM_PHASES 8 /* bbox, keys, sort, reorder, build, moments and walk records,
-                          bootstrap (accuracy modes, first step after bh_set_state), walk */
+#define BH_NUM_PHASES 9 /* bbox, keys, sort, reorder, build, moments and walk records,
+                          bootstrap (accuracy modes, first step after bh_set_state),
+                          frontier (accuracy modes: shared walk starts and heavy groups),
+                          walk (the force walk kernel alone) */
 
 /* One step (never graph-replayed) with CUDA events at the phase boundaries;
- * synchronises, then ADDS each phase's milliseconds to phase_ms[0..7].
+ * synchronises, then ADDS each phase's milliseconds to phase_ms[0..8].
  * No reference counterpart (the reference times the whole step only,
  * BarnesHutParticleSystem.cpp:303-321). */
 int bh_step_profiled(bh_system* s, void* stream, float* phase_ms);
@@ -239,10 +241,14 @@ int bh_set_energy_log(bh_system* s, int every, int capacity);
  * min(*records, capacity, max_records) of them, oldest first. */
 int bh_get_energy_log(bh_system* s, double* out, int max_records, int* records, void* stream);
 
-/* Measure the device's FP32 FMA throughput (TFLOP/s, 2 flops per FMA) with a
- * register-only kernel on every SM; the roofline denominator of the force
- * walk.  device -1 = current.  No reference counterpart. */
+/* Measure the device's FP32 FMA throughput (TFLOP/s, 2 flops per FMA) with
+ * register-only kernels on every SM, one of scalar FFMA chains and one of
+ * packed FP32x2 FFMA2 chains (the instruction the force walk issues); the
+ * larger is the roofline denominator of the force walk.  device -1 = current.
+ * No reference counterpart. */
 int bh_measure_fp32_peak(int device, double* tflops);
+/* The same probe, both figures: *scalar (FFMA) and *packed (FFMA2). */
+int bh_measure_fp32_peaks(int device, double* scalar, double* packed);
 
 /* The reference's initial conditions, number for number: the Model enum of
  * SimulationParameters.h:8-13 and the generators of

@@ -18,7 +18,8 @@ from . import build as _build
 MODES = {"reference": 0, "plain": 1, "mixed": 2}
 CHECK_BITS = {"count": 1, "child_sum": 2, "child_range": 4, "parent": 8, "keys_sorted": 16,
               "permutation": 32, "box": 64, "mass": 128}
-PHASES = ("bbox", "keys", "sort", "reorder", "build", "moments", "bootstrap", "walk")
+PHASES = ("bbox", "keys", "sort", "reorder", "build", "moments", "bootstrap", "frontier",
+          "walk")
 PHASES_N = len(PHASES)
 
 BH_OK = 0
@@ -98,6 +99,7 @@ def lib() -> ctypes.CDLL:
     L.bh_step_profiled.argtypes = [vp, vp, vp]
     L.bh_direct_sum_f64.argtypes = [vp, i32, vp, vp, vp]
     L.bh_measure_fp32_peak.argtypes = [i32, P(ctypes.c_double)]
+    L.bh_measure_fp32_peaks.argtypes = [i32, P(ctypes.c_double), P(ctypes.c_double)]
     L.bh_autotune.argtypes = [vp, vp, P(Params)]
     L.bh_energy.argtypes = [vp, vp, vp]
     L.bh_initial_conditions.argtypes = [i32, i32, ctypes.c_float] + [vp] * 5
@@ -147,10 +149,19 @@ def reference_initial_conditions(model: str, n: int, gravity: float = 1.0):
 
 
 def measure_fp32_peak(device: int = -1) -> float:
-    """Measured FP32 FMA throughput of the device in TFLOP/s."""
+    """Measured FP32 FMA throughput of the device in TFLOP/s (the larger of
+    the scalar FFMA and packed FFMA2 probes)."""
     v = ctypes.c_double(0.0)
     _check(lib().bh_measure_fp32_peak(device, ctypes.byref(v)), "bh_measure_fp32_peak")
     return float(v.value)
+
+
+def measure_fp32_peaks(device: int = -1) -> dict:
+    """Both FP32 FMA probes in TFLOP/s: scalar FFMA chains and packed FFMA2 chains."""
+    a, b = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    _check(lib().bh_measure_fp32_peaks(device, ctypes.byref(a), ctypes.byref(b)),
+           "bh_measure_fp32_peaks")
+    return {"ffma": float(a.value), "ffma2": float(b.value)}
 
 
 def make_params(mode="reference", theta=0.5, eps2=0.025, gravity=1.0, timestep=1e-3,
@@ -297,8 +308,9 @@ class BarnesHutSystem:
 
     def step_profiled(self, phase_ms: np.ndarray, stream=None):
         """One non-graph step with events at the phase boundaries; adds each
-        phase's milliseconds to phase_ms (float32[8]: bbox, keys, sort,
-        reorder, build, moments with the walk records, bootstrap, walk)."""
+        phase's milliseconds to phase_ms (float32[9]: bbox, keys, sort,
+        reorder, build, moments with the walk records, bootstrap, frontier,
+        walk)."""
         assert phase_ms.dtype == np.float32 and phase_ms.shape == (PHASES_N,)
         _check(lib().bh_step_profiled(self._h, stream, _p(phase_ms)), "bh_step_profiled")
 

@@ -9,11 +9,14 @@
 // SortParticles fills sorted[]/start[] by a level-by-level pass in one block;
 // CalculateForces is the warp-vote walk over child[] (kernels.cu:340-435).
 // Scratch buffers (keys, sort, tree, frontier queues) are kept per device and
-// grown on demand.
+// grown on demand.  Each device also keeps the last tree layout a builder
+// produced (its child[] pointer and m), which SortParticles and
+// CalculateForces use to bound their reads of child[].
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -63,27 +66,76 @@ struct Workspace {
     int *ncell, *cbase, *bsum, *total;
     int *qa, *qb;
     int* status;
-    // last reference layout seen: lets CalculateForces bound-check child[]
-    const int* child_ptr = nullptr;
-    int child_m = 0;
 };
+
+// One workspace per device.  Held by pointer, so a workspace keeps its address
+// when another device adds its own.
 std::mutex g_ws_mu;
-std::vector<Workspace> g_ws;
+std::vector<std::unique_ptr<Workspace>> g_ws;
+
+// The last tree layout built on each device (by BuildQuadTree or
+// BuildQuadTreeNoAlloc): SortParticles and CalculateForces read child[] up to
+// node m - 1 when they are given the same child array on the same device.
+constexpr int kMaxDevices = 64;
+struct Layout {
+    const int* child = nullptr;
+    int m = 0;
+};
+Layout g_layout[kMaxDevices];  // guarded by g_ws_mu
+int g_sms[kMaxDevices] = {};   // SM count per device, read once (guarded by g_ws_mu)
+
+int current_device() {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+    return dev;
+}
+
+void set_layout(const int* child, int m) {
+    const int dev = current_device();
+    if (dev < 0 || dev >= kMaxDevices) return;
+    std::lock_guard<std::mutex> lk(g_ws_mu);
+    g_layout[dev] = Layout{child, m};
+}
+
+// Nodes of child[] that the last build on this device covers, or the
+// reference's capacity 2n + 12000 (BarnesHutParticleSystem.cpp:33) for a
+// layout no build of this process produced.
+int layout_m(const int* child, int n) {
+    const int dev = current_device();
+    if (dev >= 0 && dev < kMaxDevices) {
+        std::lock_guard<std::mutex> lk(g_ws_mu);
+        if (g_layout[dev].child == child && g_layout[dev].m > 0) return g_layout[dev].m;
+    }
+    return 2 * n + 12000;
+}
+
+int device_sms() {
+    const int dev = current_device();
+    if (dev < 0) return 1;
+    std::lock_guard<std::mutex> lk(g_ws_mu);
+    if (dev < kMaxDevices && g_sms[dev] > 0) return g_sms[dev];
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+        sms = 1;
+    if (dev < kMaxDevices) g_sms[dev] = sms;
+    return sms;
+}
 
 size_t al(size_t b) { return (b + 255) & ~size_t(255); }
 
+// The current device's workspace with room for n bodies and m nodes, grown
+// (cudaFree + cudaMalloc) when it is smaller.
 Workspace* workspace(size_t n, size_t m) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    const int dev = current_device();
+    if (dev < 0) return nullptr;
     std::lock_guard<std::mutex> lk(g_ws_mu);
-    for (auto& w : g_ws)
-        if (w.device == dev && w.cap >= n && w.mcap >= m) return &w;
     Workspace* w = nullptr;
     for (auto& x : g_ws)
-        if (x.device == dev) w = &x;
+        if (x->device == dev) w = x.get();
+    if (w && w->cap >= n && w->mcap >= m) return w;
     if (!w) {
-        g_ws.emplace_back();
-        w = &g_ws.back();
+        g_ws.push_back(std::make_unique<Workspace>());
+        w = g_ws.back().get();
         w->device = dev;
     }
     if (w->base) cudaFree(w->base);
@@ -557,7 +609,45 @@ int fetch_status(Workspace* w) {
     return BH_OK;
 }
 
-Workspace* g_last_ws = nullptr;
+// BuildQuadTree's launch sequence on the scratch of w, which must hold n
+// bodies (shared by BuildQuadTree and BuildQuadTreeNoAlloc).  Keys of the
+// bodies in the caller's box, the 8-pass radix sort of the whole key, the
+// radix tree and its node sums, then the tree written out in the reference
+// layout (child, count, start, cell x/y/mass, *index).
+cudaError_t enqueue_build(Workspace& w, float* x, float* y, float* mass, int* count, int* start,
+                          int* child, int* index, float* left, float* right, float* bottom,
+                          float* top, int n, int m, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(w.counter, 0, sizeof(int) * n, st);  // moments' arrivals
+    if (e != cudaSuccess) return e;
+    const int nb = blocks_for(n, 256);
+    k_c_box_to_ord<<<1, 1, 0, st>>>(left, right, bottom, top, w.box_ord, w.seg_off, n);
+    Segs segs{1, w.seg_off, nullptr};
+    k_keys<<<nb, 256, 0, st>>>(x, y, n, segs, w.box_ord, w.keys, w.vals);
+    uint64_t *ka = w.keys, *kb = w.keys_alt;
+    uint32_t *va = w.vals, *vb = w.vals_alt;
+    const int tiles = (n + kSortTile - 1) / kSortTile;
+    for (int ps = 0; ps < 8; ++ps) {
+        k_radix_hist<<<tiles, kSortThreads, 0, st>>>(ka, va, n, 8 * ps, 0, nullptr, w.hist, tiles,
+                                                     nullptr);
+        k_radix_scan<<<256, kSortThreads, 0, st>>>(w.hist, tiles, w.totals, nullptr);
+        k_radix_scatter<<<tiles, kSortThreads, 0, st>>>(ka, va, kb, vb, n, 8 * ps, 0, nullptr,
+                                                        w.hist, w.totals, tiles, nullptr);
+        std::swap(ka, kb);
+        std::swap(va, vb);
+    }
+    k_c_gather3<<<nb, 256, 0, st>>>(n, va, x, y, mass, w.sx, w.sy, w.sm);
+    k_build<<<nb, 256, 0, st>>>(ka, n, segs, w.tree, w.status);
+    k_moments<<<(n + kMomentsThreads - 1) / kMomentsThreads, kMomentsThreads, 0, st>>>(
+        n, 0, w.sx, w.sy, w.sm, w.tree.climb, w.tree.leaf_parent, w.counter, w.sums, w.status);
+    k_c_ncells<<<nb, 256, 0, st>>>(n, w.tree.split, w.tree.parent, w.ncell);
+    const int sb = blocks_for(n, 1024);
+    k_c_scan_block<<<sb, 1024, 0, st>>>(w.ncell, w.cbase, w.bsum, n);
+    k_c_scan_top<<<1, 1024, 0, st>>>(w.bsum, sb, w.total);
+    k_c_scan_add<<<nb, 256, 0, st>>>(w.cbase, w.bsum, n);
+    k_c_materialize<<<nb, 256, 0, st>>>(n, m, w.tree, ka, va, w.cbase, w.total, w.sums, child,
+                                        count, start, x, y, mass, index, w.status);
+    return cudaGetLastError();
+}
 
 }  // namespace
 
@@ -577,12 +667,10 @@ void bh_compat_set_stream(void* stream) { g_set.stream = (cudaStream_t)stream; }
 int bh_compat_status(void) {
     cudaError_t e = cudaStreamSynchronize(g_set.stream);
     if (e != cudaSuccess) record(cuda_fail(e, "compat stream"));
+    const int cur = current_device();
     std::lock_guard<std::mutex> lk(g_ws_mu);
-    for (auto& w : g_ws) {
-        int cur = -1;
-        cudaGetDevice(&cur);
-        if (w.device == cur && w.base) record(fetch_status(&w));
-    }
+    for (auto& w : g_ws)
+        if (w->device == cur && w->base) record(fetch_status(w.get()));
     return t_status;
 }
 
@@ -591,9 +679,9 @@ void bh_compat_clear_status(void) { t_status = BH_OK; }
 void bh_compat_release(void) {
     std::lock_guard<std::mutex> lk(g_ws_mu);
     for (auto& w : g_ws)
-        if (w.base) cudaFree(w.base);
+        if (w->base) cudaFree(w->base);
     g_ws.clear();
-    g_last_ws = nullptr;
+    for (auto& l : g_layout) l = Layout{};
 }
 
 }  // extern "C"
@@ -648,40 +736,10 @@ void compat_BuildQuadTree(float* x, float* y, float* mass, int* count, int* star
         record(BH_ERR_NOMEM);
         return;
     }
-    g_last_ws = w;
-    w->child_ptr = child;
-    w->child_m = m;
-    cudaStream_t st = g_set.stream;
-    const int nb = blocks_for(n, 256);
-    k_c_box_to_ord<<<1, 1, 0, st>>>(left, right, bottom, top, w->box_ord, w->seg_off, n);
-    Segs segs{1, w->seg_off, nullptr};
-    k_keys<<<nb, 256, 0, st>>>(x, y, n, segs, w->box_ord, w->keys, w->vals);
-    uint64_t *ka = w->keys, *kb = w->keys_alt;
-    uint32_t *va = w->vals, *vb = w->vals_alt;
-    const int tiles = (n + kSortTile - 1) / kSortTile;
-    for (int ps = 0; ps < 8; ++ps) {
-        k_radix_hist<<<tiles, kSortThreads, 0, st>>>(ka, va, n, 8 * ps, 0, nullptr, w->hist, tiles,
-                                                     nullptr);
-        k_radix_scan<<<256, kSortThreads, 0, st>>>(w->hist, tiles, w->totals, nullptr);
-        k_radix_scatter<<<tiles, kSortThreads, 0, st>>>(ka, va, kb, vb, n, 8 * ps, 0, nullptr,
-                                                        w->hist, w->totals, tiles, nullptr);
-        std::swap(ka, kb);
-        std::swap(va, vb);
-    }
-    k_c_gather3<<<nb, 256, 0, st>>>(n, va, x, y, mass, w->sx, w->sy, w->sm);
-    k_build<<<nb, 256, 0, st>>>(ka, n, segs, w->tree, w->status);
-    record_cuda(cudaMemsetAsync(w->counter, 0, sizeof(int) * n, st), "BuildQuadTree memset");
-    k_moments<<<(n + kMomentsThreads - 1) / kMomentsThreads, kMomentsThreads, 0, st>>>(
-        n, 0, w->sx, w->sy, w->sm, w->tree.climb, w->tree.leaf_parent, w->counter, w->sums,
-        w->status);
-    k_c_ncells<<<nb, 256, 0, st>>>(n, w->tree.split, w->tree.parent, w->ncell);
-    const int sb = blocks_for(n, 1024);
-    k_c_scan_block<<<sb, 1024, 0, st>>>(w->ncell, w->cbase, w->bsum, n);
-    k_c_scan_top<<<1, 1024, 0, st>>>(w->bsum, sb, w->total);
-    k_c_scan_add<<<nb, 256, 0, st>>>(w->cbase, w->bsum, n);
-    k_c_materialize<<<nb, 256, 0, st>>>(n, m, w->tree, ka, va, w->cbase, w->total, w->sums, child,
-                                        count, start, x, y, mass, index, w->status);
-    record_cuda(cudaGetLastError(), "BuildQuadTree");
+    set_layout(child, m);
+    record_cuda(enqueue_build(*w, x, y, mass, count, start, child, index, left, right, bottom, top,
+                              n, m, g_set.stream),
+                "BuildQuadTree");
 }
 
 void compat_ComputeCentreOfMass(float* x, float* y, float* mass, int* index, int n) {
@@ -691,13 +749,13 @@ void compat_ComputeCentreOfMass(float* x, float* y, float* mass, int* index, int
 
 void compat_SortParticles(int* count, int* start, int* sorted, int* child, int* index, int n) {
     (void)index;
-    Workspace* w = g_last_ws;
-    int mlimit = (w && w->child_ptr == child) ? w->child_m : 0;
-    if (!w || mlimit == 0) {
-        // layout not produced by BuildQuadTree in this process: size the queues for 2n+12000
-        mlimit = 2 * n + 12000;
-        w = workspace(1, (size_t)mlimit);
+    if (n < 1) {
+        record(BH_ERR_ARG);
+        return;
     }
+    // queues for every cell of the layout, on the current device's workspace
+    const int mlimit = layout_m(child, n);
+    Workspace* w = workspace(1, (size_t)mlimit);
     if (!w) {
         record(BH_ERR_NOMEM);
         return;
@@ -712,15 +770,19 @@ void compat_CalculateForces(float* x, float* y, float* vx, float* vy, float* ax,
     (void)vx;
     (void)vy;
     (void)g;  // unused in the reference too (kernels.cu:340)
-    Workspace* w = g_last_ws;
-    int mlimit = (w && w->child_ptr == child) ? w->child_m : 2 * n + 12000;
-    if (!w) w = workspace(1, 1);
+    if (n < 1) {
+        record(BH_ERR_ARG);
+        return;
+    }
+    const int mlimit = layout_m(child, n);
+    Workspace* w = workspace(1, 1);  // the current device's status word
     if (!w) {
         record(BH_ERR_NOMEM);
         return;
     }
     constexpr int W = 8, S = 256;
-    int blocks = std::min(blocks_for((n + 31) / 32, W), 152 * 16);
+    // a grid-stride loop over the warp groups: at most 16 blocks per SM
+    int blocks = std::min(blocks_for((n + 31) / 32, W), 16 * device_sms());
     k_c_forces<W, S><<<blocks, W * 32, 0, g_set.stream>>>(x, y, mass, sorted, child, left, right, n,
                                                         mlimit, g_set.theta, g_set.eps2, ax, ay,
                                                         w->status);
@@ -794,14 +856,13 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 namespace {
 
-constexpr int kNoAllocMaxDevices = 64;
 std::mutex g_noalloc_mu;
-unsigned char* g_noalloc_addr[kNoAllocMaxDevices] = {};
+unsigned char* g_noalloc_addr[kMaxDevices] = {};
 
 // Device address of g_noalloc_scratch on the current device, resolved once per
 // device (the first call on a device does this set-up).
 unsigned char* noalloc_scratch(int dev, int* status) {
-    if (dev < 0 || dev >= kNoAllocMaxDevices) {
+    if (dev < 0 || dev >= kMaxDevices) {
         *status = BH_ERR_NO_DEVICE;
         return nullptr;
     }
@@ -857,71 +918,55 @@ void noalloc_layout(unsigned char* base, size_t n, Workspace* w) {
     w->tiles = tiles;
 }
 
+// Status of one BuildQuadTreeNoAlloc call, also recorded for bh_compat_status().
+int noalloc_result(int rc) {
+    record(rc);
+    return rc;
+}
+
 }  // namespace
 
 extern "C" int BuildQuadTreeNoAlloc(float* x, float* y, float* mass, int* count, int* start,
                                     int* child, int* index, float* left, float* right,
                                     float* bottom, float* top, int n, int m) {
-    if (n < 1 || m < n) return BH_ERR_ARG;
+    if (n < 1 || m < n) return noalloc_result(BH_ERR_ARG);
     if (n > kNoAllocMaxBodies) {
         g_last_error = "BuildQuadTreeNoAlloc: n = " + std::to_string(n) +
                        " exceeds the static scratch limit of " +
                        std::to_string(kNoAllocMaxBodies) + " bodies";
-        return BH_ERR_CAPACITY;
+        return noalloc_result(BH_ERR_CAPACITY);
     }
-    if (n == 1) return BH_OK;  // a lone body: no cells, *index stays n
+    if (n == 1) {  // a lone body: no cells, *index stays n
+        set_layout(child, m);
+        return BH_OK;
+    }
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (e != cudaSuccess) return noalloc_result(cuda_fail(e, "cudaGetDevice"));
     int st_code = BH_OK;
     unsigned char* base = noalloc_scratch(dev, &st_code);
-    if (!base) return st_code;
+    if (!base) return noalloc_result(st_code);
     Workspace w;
     noalloc_layout(base, (size_t)n, &w);
     cudaStream_t st = g_set.stream;
-    // the array keeps the previous call's contents: clear what must start at zero
+    // the array keeps the previous call's contents: clear the status word here
+    // (enqueue_build clears the arrival counters)
     e = cudaMemsetAsync(w.status, 0, sizeof(int), st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(w.counter, 0, sizeof(int) * n, st);
-    if (e != cudaSuccess) return cuda_fail(e, "BuildQuadTreeNoAlloc memset");
-    const int nb = blocks_for(n, 256);
-    k_c_box_to_ord<<<1, 1, 0, st>>>(left, right, bottom, top, w.box_ord, w.seg_off, n);
-    Segs segs{1, w.seg_off, nullptr};
-    k_keys<<<nb, 256, 0, st>>>(x, y, n, segs, w.box_ord, w.keys, w.vals);
-    uint64_t *ka = w.keys, *kb = w.keys_alt;
-    uint32_t *va = w.vals, *vb = w.vals_alt;
-    const int tiles = w.tiles;
-    for (int ps = 0; ps < 8; ++ps) {
-        k_radix_hist<<<tiles, kSortThreads, 0, st>>>(ka, va, n, 8 * ps, 0, nullptr, w.hist, tiles,
-                                                     nullptr);
-        k_radix_scan<<<256, kSortThreads, 0, st>>>(w.hist, tiles, w.totals, nullptr);
-        k_radix_scatter<<<tiles, kSortThreads, 0, st>>>(ka, va, kb, vb, n, 8 * ps, 0, nullptr,
-                                                        w.hist, w.totals, tiles, nullptr);
-        std::swap(ka, kb);
-        std::swap(va, vb);
-    }
-    k_c_gather3<<<nb, 256, 0, st>>>(n, va, x, y, mass, w.sx, w.sy, w.sm);
-    k_build<<<nb, 256, 0, st>>>(ka, n, segs, w.tree, w.status);
-    k_moments<<<(n + kMomentsThreads - 1) / kMomentsThreads, kMomentsThreads, 0, st>>>(
-        n, 0, w.sx, w.sy, w.sm, w.tree.climb, w.tree.leaf_parent, w.counter, w.sums, w.status);
-    k_c_ncells<<<nb, 256, 0, st>>>(n, w.tree.split, w.tree.parent, w.ncell);
-    const int sb = blocks_for(n, 1024);
-    k_c_scan_block<<<sb, 1024, 0, st>>>(w.ncell, w.cbase, w.bsum, n);
-    k_c_scan_top<<<1, 1024, 0, st>>>(w.bsum, sb, w.total);
-    k_c_scan_add<<<nb, 256, 0, st>>>(w.cbase, w.bsum, n);
-    k_c_materialize<<<nb, 256, 0, st>>>(n, m, w.tree, ka, va, w.cbase, w.total, w.sums, child,
-                                        count, start, x, y, mass, index, w.status);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail(e, "BuildQuadTreeNoAlloc launch");
+    if (e != cudaSuccess) return noalloc_result(cuda_fail(e, "BuildQuadTreeNoAlloc memset"));
+    e = enqueue_build(w, x, y, mass, count, start, child, index, left, right, bottom, top, n, m,
+                      st);
+    if (e != cudaSuccess) return noalloc_result(cuda_fail(e, "BuildQuadTreeNoAlloc launch"));
     // wait for this tree build and return its device status (the scratch is shared:
     // the next call may overwrite it as soon as this one returns)
     e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return cuda_fail(e, "BuildQuadTreeNoAlloc sync");
+    if (e != cudaSuccess) return noalloc_result(cuda_fail(e, "BuildQuadTreeNoAlloc sync"));
     int bits = 0;
     e = cudaMemcpy(&bits, w.status, sizeof(int), cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return cuda_fail(e, "BuildQuadTreeNoAlloc status");
-    if (bits & ST_DUP) return BH_ERR_DUPLICATE_KEYS;
-    if (bits & ST_CAPACITY) return BH_ERR_CAPACITY;
-    if (bits & ST_NONFINITE) return BH_ERR_NONFINITE;
-    if (bits & ST_TREE) return BH_ERR_TREE;
+    if (e != cudaSuccess) return noalloc_result(cuda_fail(e, "BuildQuadTreeNoAlloc status"));
+    if (bits & ST_DUP) return noalloc_result(BH_ERR_DUPLICATE_KEYS);
+    if (bits & ST_CAPACITY) return noalloc_result(BH_ERR_CAPACITY);
+    if (bits & ST_NONFINITE) return noalloc_result(BH_ERR_NONFINITE);
+    if (bits & ST_TREE) return noalloc_result(BH_ERR_TREE);
+    set_layout(child, m);  // SortParticles and CalculateForces read up to node m - 1
     return BH_OK;
 }

@@ -546,13 +546,15 @@ int enqueue_step(bh_system* s, cudaStream_t st, cudaEvent_t* ev = nullptr, int b
                       s->nseg > 1 ? (a.bpl == 2 ? s->gseg_off2 : s->gseg_off) : nullptr,
                       s->mean_cost, s->heavy, s->work + kWorkHeavy));
     }
-    CK(launch_walk(a, st, 1));
     CK(mark(8));
+    CK(launch_walk(a, st, 1));
+    CK(mark(9));
     return BH_OK;
 }
 
 // FP32 FMA throughput probe: 8 independent FMA chains per thread, no memory
 // traffic except one store per thread (kept so the chains are not removed).
+// 128 FMAs (256 flops) per thread and iteration.
 __global__ void __launch_bounds__(256) k_ffma_peak(float* out, int iters, float a, float b) {
     float v0 = threadIdx.x * 1e-3f, v1 = v0 + 1.f, v2 = v0 + 2.f, v3 = v0 + 3.f;
     float v4 = v0 + 4.f, v5 = v0 + 5.f, v6 = v0 + 6.f, v7 = v0 + 7.f;
@@ -564,6 +566,28 @@ __global__ void __launch_bounds__(256) k_ffma_peak(float* out, int iters, float 
         }
     }
     out[blockIdx.x * blockDim.x + threadIdx.x] = v0 + v1 + v2 + v3 + v4 + v5 + v6 + v7;
+}
+
+// The same with packed FP32x2 FMAs (__ffma2_rn, the force walk's instruction):
+// 8 independent chains of float2, 64 FFMA2 = 128 FMAs (256 flops) per thread
+// and iteration.
+__global__ void __launch_bounds__(256) k_ffma2_peak(float* out, int iters, float a, float b) {
+    const float s = threadIdx.x * 1e-3f;
+    float2 v[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) v[c] = make_float2(s + c, s + c + 0.5f);
+    const float2 av = make_float2(a, a), bv = make_float2(b, b);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+#pragma unroll
+            for (int c = 0; c < 8; ++c) v[c] = __ffma2_rn(v[c], av, bv);
+        }
+    }
+    float acc = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 8; ++c) acc += v[c].x + v[c].y;
+    out[blockIdx.x * blockDim.x + threadIdx.x] = acc;
 }
 
 // FP64 direct sum for a sample of targets: grid (target tiles, source chunks),
@@ -1446,8 +1470,8 @@ int bh_direct_sum_f64(bh_system* s, int ns, const int* idx, double* ax, double* 
     return BH_OK;
 }
 
-int bh_measure_fp32_peak(int device, double* tflops) {
-    if (!tflops) return BH_ERR_ARG;
+int bh_measure_fp32_peaks(int device, double* scalar, double* packed) {
+    if (!scalar || !packed) return BH_ERR_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return BH_ERR_NO_DEVICE;
     if (device >= 0) CK(cudaSetDevice(device));
@@ -1461,22 +1485,43 @@ int bh_measure_fp32_peak(int device, double* tflops) {
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    float best = 1e30f;
-    for (int rep = 0; rep < 6; ++rep) {
-        CK(cudaEventRecord(e0));
-        k_ffma_peak<<<blocks, threads>>>(out, iters, 0.999f, 1e-6f);
-        CK(cudaEventRecord(e1));
-        CK(cudaEventSynchronize(e1));
-        float ms = 0.f;
-        CK(cudaEventElapsedTime(&ms, e0, e1));
-        if (rep > 0) best = ms < best ? ms : best;
+    // both kernels: 256 flops per thread and iteration; best of 5 after one warm-up
+    const double flops = 256.0 * iters * (double)blocks * threads;
+    double* res[2] = {scalar, packed};
+    int rc = BH_OK;
+    for (int kind = 0; kind < 2 && rc == BH_OK; ++kind) {
+        float best = 1e30f;
+        for (int rep = 0; rep < 6; ++rep) {
+            cudaError_t e = cudaEventRecord(e0);
+            if (kind == 0)
+                k_ffma_peak<<<blocks, threads>>>(out, iters, 0.999f, 1e-6f);
+            else
+                k_ffma2_peak<<<blocks, threads>>>(out, iters, 0.999f, 1e-6f);
+            if (e == cudaSuccess) e = cudaGetLastError();
+            if (e == cudaSuccess) e = cudaEventRecord(e1);
+            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+            float ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+            if (e != cudaSuccess) {
+                rc = cuda_fail(e, "bh_measure_fp32_peaks");
+                break;
+            }
+            if (rep > 0) best = ms < best ? ms : best;
+        }
+        *res[kind] = flops / (best * 1e-3) / 1e12;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(out);
-    double flops = 2.0 * 8.0 * 16.0 * iters * (double)blocks * threads;
-    *tflops = flops / (best * 1e-3) / 1e12;
-    return BH_OK;
+    return rc;
+}
+
+int bh_measure_fp32_peak(int device, double* tflops) {
+    if (!tflops) return BH_ERR_ARG;
+    double a = 0.0, b = 0.0;
+    int rc = bh_measure_fp32_peaks(device, &a, &b);
+    if (rc == BH_OK) *tflops = a > b ? a : b;
+    return rc;
 }
 
 // Per-system FP64 sums: out[4k..4k+3] += kinetic, potential (0.5 m phi), px, py.

@@ -135,12 +135,14 @@ def plummer24(args) -> dict:
                 phases[name] = e
             walk_ms = float(phase_ms[bh.PHASES.index("walk")])
             tflops = roofline.walk_flops(st) / (walk_ms * 1e-3) / 1e12
+            tflops_mp = roofline.walk_flops_with_multipole(st) / (walk_ms * 1e-3) / 1e12
             rows.append({"theta": theta, "mode": mode, "walk_shape": shape,
                          "steps_per_s": round(steps / secs, 3),
                          "interactions_per_step": st["interactions"],
                          "interactions_per_s": round(st["interactions"] * steps / secs, 1),
                          "force_error_vs_fp64": err, "drift_after_steps": drift,
                          "walk_tflops": round(tflops, 3), "walk_frac_fp32": round(tflops / fp32_peak, 4),
+                         "walk_tflops_with_multipole": round(tflops_mp, 3),
                          "phases": phases})
     return {"workload": "plummer2d_2^24 theta sweep", "n_bodies": n, "eps": eps, "dt": dt,
             "steps": steps, "fp32_peak_tflops": round(fp32_peak, 2), "hbm_peak_gbs": hbm,

@@ -8,8 +8,9 @@ phase on seeded inputs, through the same launch wrappers
 (Particle_cuda.cu:14-53) with one 64-thread block.  Each fixture stores the
 inputs and every phase output in a canonical, cell-numbering-independent form.
 
-Run in a container that has the reference sources:
-    python tests/golden/make_golden.py [--ref /root/reference]
+Run where the reference sources are present:
+    STELLARSOLVER_REF=<reference checkout> python tests/golden/make_golden.py
+    (or --ref <reference checkout>)
 The fixtures are committed; tests never need the reference at run time.
 
 The reference's softening and opening angle are compile-time constants
@@ -201,8 +202,11 @@ def make_case(lib, name, gen, dt, damp, steps=3):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("STELLARSOLVER_REF"),
+                    help="reference sources (default: $STELLARSOLVER_REF)")
     args = ap.parse_args()
+    if not args.ref:
+        sys.exit("give the reference sources with --ref or STELLARSOLVER_REF")
     lib = load_ref(args.ref)
     for name, (gen, dt, damp) in CASES.items():
         make_case(lib, name, gen, dt, damp)

@@ -174,3 +174,32 @@ def test_debug_invariants(run):
     st = rec["start"]
     cells = np.arange(n, rec["index"])
     assert (st[cells] >= 0).all()
+
+
+def test_two_systems_alternating(L):
+    """Two systems of different sizes (disk 4096, clustered 512) stepped in
+    turn through the nine wrappers on one device: each build replaces the
+    device's workspace layout record, and every step must still match the
+    golden outputs of its own system."""
+    cases = [gc.load("disk4096"), gc.load("clustered512")]
+    names = ["disk4096", "clustered512"]
+    arrs = [RefArrays(g) for g in cases]
+    L.bh_compat_clear_status()
+    first = [{}, {}]
+    steps = int(cases[0]["steps"])
+    assert steps == int(cases[1]["steps"])
+    for k in range(steps):
+        for i, (g, a) in enumerate(zip(cases, arrs)):
+            update(L, a, float(g["dt"]), float(g["damp"]), first[i] if k == 0 else {})
+    assert L.bh_compat_status() == 0
+    for g, a, rec, name in zip(cases, arrs, first, names):
+        n = int(g["n"])
+        assert np.array_equal(rec["box"].view(np.uint32), g["box"].view(np.uint32)), name
+        assert np.array_equal(rec["sorted"][:n], g["sorted"]), name
+        rms = np.sqrt(np.mean(g["ax"].astype(np.float64) ** 2 + g["ay"].astype(np.float64) ** 2))
+        err = np.hypot(rec["ax"] - g["ax"], rec["ay"] - g["ay"]).max() / rms
+        assert err <= FORCE_TOL[name], (name, err)
+        tol = TRAJ_TOL[name]
+        final = tuple(t[:n].cpu().numpy() for t in (a.x, a.y, a.vx, a.vy))
+        for v, ref in zip(final, ("x3", "y3", "vx3", "vy3")):
+            assert np.max(np.abs(v - g[ref])) <= 3 * tol * np.abs(g[ref]).max(), (name, ref)

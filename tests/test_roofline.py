@@ -28,4 +28,7 @@ def test_phase_bytes():
 
 def test_walk_flops():
     stats = {"interactions": 1000, "cell_interactions": 600}
-    assert roofline.walk_flops(stats) == 14 * 400 + 33 * 600
+    # the roofline counts 14 flops per interaction of either kind
+    assert roofline.walk_flops(stats) == 14 * 1000
+    # executed arithmetic: quadrupole cells at 33
+    assert roofline.walk_flops_with_multipole(stats) == 14 * 400 + 33 * 600
