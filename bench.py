@@ -83,6 +83,15 @@ class ClockSampler:
             self.proc = None
         return self
 
+    def wait_first_sample(self, timeout=5.0):
+        """Block until nvidia-smi has written its first sample (it takes a
+        moment to start), so that the samples cover the region that follows."""
+        t0 = time.perf_counter()
+        while self.proc and time.perf_counter() - t0 < timeout:
+            if os.path.getsize(self.path) > 0:
+                return
+            time.sleep(0.02)
+
     def __exit__(self, *exc):
         if self.proc:
             self.proc.terminate()
@@ -179,17 +188,34 @@ def run_engine(args):
     for _ in range(args.warmup):
         sysm.step(1, sp)
     sysm.sync(sp)
-    st0 = sysm.get_state()
     barrier()
+
+    def hold_load(seconds):
+        """Untimed graph steps for `seconds` (clock samples under load)."""
+        t_end = time.perf_counter() + seconds
+        while time.perf_counter() < t_end:
+            for _ in range(20):
+                sysm.step(1, sp)
+            torch.cuda.synchronize()
+
     with ClockSampler(local) as clk:
+        # the timed steps last a few tens of ms, less than the 200 ms sampling
+        # period: the samples span a window of load around them
+        clk.wait_first_sample()
+        hold_load(0.5)
+        sysm.sync(sp)
+        st0 = sysm.get_state()
+        barrier()
         t_wall0 = time.perf_counter()
         secs = timed_steps(sysm, args.steps)
         t_wall = time.perf_counter() - t_wall0
-    barrier()
-    sysm.sync(sp)
-    st1 = sysm.get_state()
+        barrier()
+        sysm.sync(sp)
+        st1 = sysm.get_state()
+        hold_load(0.3)
     stats = sysm.stats()
     clocks = clk.summary()
+    clocks["window"] = "0.5 s of untimed steps, the timed steps, 0.3 s of untimed steps"
     if world > 1:
         t = torch.tensor([secs], device="cuda", dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -421,8 +447,15 @@ def run_ensemble(bh, torch, stream, sp, local, world, rank, args):
         b.autotune(sp)
         for _ in range(2):
             b.step(1, sp)
+        e0 = b.energy(sp)  # FP64 (kinetic, potential, px, py) per system
         t_batch = timed(lambda: b.step(1, sp))
         inter = b.stats(sp)["interactions"]
+        e1 = b.energy(sp)
+    # per-system diagnostics gathered once, after the timed steps, in system order
+    gather = torch.distributed.all_gather_object if world > 1 else None
+    diag = sharding.gather_by_system(len(sizes), mine, np.hstack([e0, e1]), gather)
+    E0, E1 = diag[:, 0] + diag[:, 1], diag[:, 4] + diag[:, 5]
+    drift = np.abs(E1 - E0) / np.abs(E0)
     handles = []
     try:
         for sy in systems:
@@ -449,7 +482,11 @@ def run_ensemble(bh, torch, stream, sp, local, world, rank, args):
             "batched_mixed_graph_steps_per_s": round(1.0 / t_batch, 3),
             "one_handle_per_system_plain_steps_per_s": round(1.0 / t_each, 3),
             "batched_over_per_system": round(t_each / t_batch, 2),
-            "interactions_per_s": round(inter / t_batch, 1)}
+            "interactions_per_s": round(inter / t_batch, 1),
+            "systems_diagnosed": int(np.sum(np.isfinite(drift))),
+            "energy_drift_rel_max_over_systems": float(np.max(drift)),
+            "diagnostics": "FP64 energy and momentum per system before and after the timed "
+                           "steps, gathered by system over the ranks"}
 
 
 CPU_BASELINE_STEPS = 5
