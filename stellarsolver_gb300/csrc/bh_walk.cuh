@@ -39,19 +39,24 @@ struct WalkOut {
     int* gcost;   // this step's walk-group cost (interaction entries) of each body
 };
 
-// Heaviest groups first.  A group whose first body's previous-step group cost
-// is at least 1.5x its system's mean of the previous step (mean > 0) is
-// heavy: k_frontier lists the heavy groups, and the main walk takes them
-// before the others, so that the longest groups do not start late and leave
-// the SMs idle.
+// Heaviest groups first.  A group is heavy when the largest previous-step
+// group cost carried by its bodies is at least 1.5x its system's mean of the
+// previous step (mean > 0): k_frontier lists the heavy groups, and the main
+// walk takes them before the others, so that the longest groups do not start
+// late and leave the SMs idle.  The largest over the group's bodies, not one
+// body's: group boundaries move by a position or two from one step to the
+// next, and a group's cost is set mostly by its body of smallest |a| (the
+// relative rule), which brings its old group's high cost along when it
+// crosses a boundary.  (Plummer 2^20: the first body's cost missed about a
+// quarter of the heavy groups, the middle body's an eighth, the largest 4 %.)
 struct Heavy {
     const int* list = nullptr;           // heavy group indices, in any order
     const int* count = nullptr;          // their number; null: no reordering
     const int* mean = nullptr;           // [nseg] each system's mean group cost, last step
     unsigned long long* cost = nullptr;  // [nseg] this step's cost (entries x bodies)
 };
-__device__ __forceinline__ bool heavy_group(const int* __restrict__ gcost, int gstart, int mean) {
-    return mean > 0 && 2ll * __ldg(gcost + gstart) >= 3ll * mean;
+__device__ __forceinline__ bool heavy_cost(int max_cost, int mean) {
+    return mean > 0 && 2ll * max_cost >= 3ll * mean;
 }
 
 // Next group for this warp: dynamic scheduling, groups differ ~10x in cost.
@@ -559,17 +564,32 @@ __global__ void __launch_bounds__(WARPS * 32) k_frontier(Segs segs, int nsupers,
     const int s0 = lo + ((S - (segs.nseg > 1 ? __ldg(sup_off + sg) : 0)) << kSuperLog2);
     const int s1 = min(hi, s0 + (1 << kSuperLog2));
     {
-        // this super-group's heavy walk groups (at most 32: gw >= 32 bodies)
+        // this super-group's heavy walk groups (at most 32: gw >= 32 bodies).
+        // Load k of a lane reads position s0 + 32 k + lane: the 32-body slice
+        // k of the super-group, which belongs to group (32 k) / gw.
+        constexpr int kSlices = (1 << kSuperLog2) / 32;
+        int v[kSlices];
+#pragma unroll
+        for (int k = 0; k < kSlices; ++k) {
+            const int i = s0 + 32 * k + lane;
+            v[k] = i < s1 ? __ldg(gcost + i) : 0;
+        }
         const int mean = mean_cost[sg];
-        const int gs = s0 + lane * gw;
-        const bool h = gs < s1 && heavy_group(gcost, gs, mean);
-        const unsigned hm = __ballot_sync(kFull, h);
+        const int per = gw >> 5;  // slices per group
+        unsigned hm = 0;          // bit q: group q of the super-group is heavy
+#pragma unroll
+        for (int k = 0; k < kSlices; ++k) {
+            int mx = v[k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(kFull, mx, o));
+            if (s0 + 32 * k < s1 && heavy_cost(mx, mean)) hm |= 1u << (k / per);
+        }
         int base = 0;
         if (lane == 0 && hm) base = atomicAdd(nheavy, __popc(hm));
         base = __shfl_sync(kFull, base, 0);
-        if (h)
+        if ((hm >> lane) & 1u)
             heavy[base + __popc(hm & lt)] =
-                (segs.nseg > 1 ? __ldg(gseg_off + sg) : 0) + (gs - lo) / gw;
+                (segs.nseg > 1 ? __ldg(gseg_off + sg) : 0) + (s0 + lane * gw - lo) / gw;
     }
     float bx0 = __int_as_float(0x7f800000), bx1 = -bx0, by0 = bx0, by1 = -bx0;
     for (int i = s0 + lane; i < s1; i += 32) {
@@ -747,7 +767,16 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
         const int g = c < nh ? hv.list[c] : c - nh;
         int lo, hi, gstart, sg;
         group_range(segs, gr, g, &lo, &hi, &gstart, GW, &sg);
-        if (c >= nh && nh > 0 && heavy_group(in.gcost, gstart, hv.mean[sg])) continue;  // done first
+        if (c >= nh && nh > 0) {
+            // a heavy group was taken first: the same test as k_frontier's
+            int mx = 0;
+#pragma unroll
+            for (int b = 0; b < BPL; ++b)
+                if (gstart + 32 * b + lane < hi) mx = max(mx, __ldg(in.gcost + gstart + 32 * b + lane));
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(kFull, mx, o));
+            if (heavy_cost(mx, hv.mean[sg])) continue;  // done first
+        }
         const int cnt = min(GW, hi - gstart);
         // body b of this lane is position gstart + 32 b + lane; invalid ones
         // mirror the group's first body
