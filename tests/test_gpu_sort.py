@@ -134,3 +134,31 @@ def test_four_pass_sort_above_2e21_bodies(bh, oracle, graph):
         assert s.stats()["status"] == 0
         assert np.array_equal(s.debug("perm"), operm.astype(np.int32))
         assert np.array_equal(s.debug("keys"), k[operm])
+
+
+@pytest.mark.parametrize("graph", [False, True])
+@pytest.mark.parametrize("mode", ["reference", "mixed"])
+def test_sort_over_consecutive_steps(bh, oracle, graph, mode):
+    """A stepped system enters each sort in the previous step's key order (the
+    first step after bh_set_state in the caller's order).  Over eight steps,
+    every step's permutation (caller index of each sorted position) and sorted
+    keys equal the oracle's stable sort of that step's positions, bit for
+    bit."""
+    from stellarsolver_gb300 import models
+
+    n = 1 << 17
+    x, y, vx, vy, m = models.plummer(n, 0x5EED8000)
+    kw = dict(mode=mode, theta=0.5, eps2=1e-4, timestep=1e-4, use_graph=graph)
+    if mode == "reference":
+        kw["eps2"] = 0.025
+    with bh.BarnesHutSystem(n, **kw) as s:
+        s.set_state(x, y, vx, vy, m)
+        for step in range(8):
+            st = s.get_state() if step else dict(x=x, y=y)
+            s.step(1)
+            s.sync()
+            assert s.stats()["status"] == 0
+            k = oracle.keys(st["x"], st["y"], oracle.bbox(st["x"], st["y"]))
+            ok, _ = oracle.sort_keys(k)
+            assert np.array_equal(s.debug("perm"), ok.astype(np.int32)), step
+            assert np.array_equal(s.debug("keys"), k[ok]), step
