@@ -196,7 +196,8 @@ int bh_check(bh_system* s, void* stream, unsigned* failed);
 
 /* Copy a named internal array of the last step to host memory (test and
  * debugging aid).  Names and element types:
- *   "box" f32[4], "keys" u64[n] (sorted), "perm" i32[n] (caller index of each
+ *   "box" f32[4] (left, right, bottom, top of system 0), "boxes" f32[4 nseg]
+ *   (every system's), "keys" u64[n] (sorted), "perm" i32[n] (caller index of each
  *   sorted position), "node_left" "node_right" "node_split" "node_first"
  *   "node_last" "node_parent" i32[n], "node_m" "node_mx" "node_my" "node_cx"
  *   "node_cy" f32[n] (node arrays have n entries; entry n-1 is unused),

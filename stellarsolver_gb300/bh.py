@@ -355,7 +355,8 @@ class BarnesHutSystem:
 
     def debug(self, name: str):
         n = self.n
-        spec = {"box": (np.float32, 4), "keys": (np.uint64, n), "perm": (np.int32, n),
+        spec = {"box": (np.float32, 4), "boxes": (np.float32, 4 * self.num_systems),
+                "keys": (np.uint64, n), "perm": (np.int32, n),
                 "accel_sorted": (np.float32, 2 * n)}
         dt, cnt = spec.get(name, (np.float32 if name in ("node_m", "node_mx", "node_my",
                                                           "node_cx", "node_cy") else np.int32, n))

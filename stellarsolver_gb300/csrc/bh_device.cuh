@@ -255,18 +255,21 @@ static __global__ void k_keys(const float* __restrict__ x, const float* __restri
 // step's first `nzero` scheduling and statistics words.  With nzero > 0 (a
 // step, not the energy pass) each system's walk cost of the last step
 // (seg_cost, entries x bodies) becomes its mean walk-group cost (mean_cost)
-// and is cleared.
+// and is cleared.  box_copy (non-null when the box was carried from the last
+// walk): block 0 copies the box read (box_ord) there, for the later phases.
 static __global__ void k_keys_step(const float* __restrict__ x, const float* __restrict__ y, int n,
                                    Segs segs, const int* __restrict__ box_ord,
                                    uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
                                    int* __restrict__ counter, int* __restrict__ zero, int nzero,
                                    int* __restrict__ flags,
                                    unsigned long long* __restrict__ seg_cost,
-                                   int* __restrict__ mean_cost) {
+                                   int* __restrict__ mean_cost, int* __restrict__ box_copy) {
     pdl_wait();
     if (blockIdx.x == 0) {
         if (threadIdx.x < nzero) zero[threadIdx.x] = 0;
         if (threadIdx.x < 2) flags[threadIdx.x] = 0;
+        if (box_copy)
+            for (int w = threadIdx.x; w < 4 * segs.nseg; w += blockDim.x) box_copy[w] = box_ord[w];
     }
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (nzero > 0 && t < segs.nseg) {
@@ -466,11 +469,17 @@ static __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(
 constexpr int kShortSortMax = 1 << 21;
 constexpr int kFixupRun = 256;
 
+//
+// Block 0 also resets box_reset (box_words ints, when non-null) to the origin
+// box: the key kernel, which may have read it, has completed.
 static __global__ void k_sort_fixup(int n, int shift, const uint64_t* __restrict__ kin,
                                     const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
                                     uint32_t* __restrict__ vout, int* __restrict__ overflow,
-                                    cudaGraphConditionalHandle cond, int set_cond) {
+                                    cudaGraphConditionalHandle cond, int set_cond,
+                                    int* __restrict__ box_reset, int box_words) {
     pdl_wait();
+    if (box_reset && blockIdx.x == 0)
+        for (int w = threadIdx.x; w < box_words; w += blockDim.x) box_reset[w] = 0;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint64_t k = kin[i];

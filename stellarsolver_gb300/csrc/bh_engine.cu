@@ -71,7 +71,8 @@ constexpr int kStepZero = 4 + 6;
 // Parts of a step: all of it, or split after the sort (bh_step joins the input
 // copies of bh_set_state in between).
 enum StepPart { kStepAll = 0, kStepPre = 1, kStepPost = 2 };
-constexpr int kGraphs = 5;
+constexpr int kGraphs = 6;
+constexpr int kGraphCarried = 5;  // a whole step on the box carried from the last walk
 
 template <typename T>
 T* carve(char*& cur, size_t count) {
@@ -221,6 +222,8 @@ struct bh_system {
     uint32_t* vfinal = nullptr;  // permutation after the last pass
     uint32_t *hist = nullptr, *totals = nullptr;
     int tiles = 0;
+    int* box_next = nullptr;  // [4 nseg] the next step's box, folded by the integrating walk
+    bool box_valid = false;   // box_next is the box of the current positions (host's record)
     int* box_ord = nullptr;
     int *seg_off = nullptr, *seg_of_pos = nullptr, *gseg_off = nullptr, *gseg_off2 = nullptr;
     int *chunk_seg = nullptr, *chunk_begin = nullptr, *chunk_end = nullptr;
@@ -319,7 +322,7 @@ ssg::StepArgs step_args(bh_system* s) {
     a.in = WalkIn{g.x, g.y, g.vx, g.vy, g.m, mixed ? g.xlo : nullptr, mixed ? g.ylo : nullptr, g.id,
                   g.amag, g.gcost};
     a.out = WalkOut{c.x, c.y, c.vx, c.vy, c.m, mixed ? c.xlo : nullptr, mixed ? c.ylo : nullptr, c.id,
-                    s->ax, s->ay, c.amag, c.gcost};
+                    s->ax, s->ay, c.amag, c.gcost, s->box_next};
     a.recA = s->rec.A;
     a.recB = s->rec.B;
     a.recC = s->rec.C;
@@ -348,8 +351,11 @@ ssg::StepArgs step_args(bh_system* s) {
 
 // Phases 0-3 of a step: box, keys, sort.  The sorted keys and permutation end
 // in keys_alt / vals_alt, or in keys3 / vals3 after an odd number of
-// system-index passes.
-int enqueue_sort(bh_system* s, cudaStream_t st, cudaEvent_t* ev, bool keep_stats) {
+// system-index passes.  carry: the box is the one the last walk folded
+// (box_next), no box kernel.  fold: this step's walk folds the next box, so
+// box_next is reset once the keys are made.
+int enqueue_sort(bh_system* s, cudaStream_t st, cudaEvent_t* ev, bool keep_stats, bool carry,
+                 bool fold) {
     const int n = s->n;
     auto mark = [&](int k) -> cudaError_t { return ev ? cudaEventRecord(ev[k], st) : cudaSuccess; };
     Segs segs{s->nseg, s->seg_off, s->nseg > 1 ? s->seg_of_pos : nullptr};
@@ -357,15 +363,18 @@ int enqueue_sort(bh_system* s, cudaStream_t st, cudaEvent_t* ev, bool keep_stats
     const int tb = 256, nb = (n + tb - 1) / tb;
     uint64_t *k0 = s->keys, *kA = s->keys_alt, *kB = s->keys3;
     uint32_t *v0 = s->vals, *vA = s->vals_alt, *vB = s->vals3;
-    CK(cudaMemsetAsync(s->box_ord, 0, sizeof(int) * 4 * s->nseg, st));  // origin box
+    if (!carry) CK(cudaMemsetAsync(s->box_ord, 0, sizeof(int) * 4 * s->nseg, st));  // origin box
     CK(mark(0));
-    CK(launch_pdl(k_bbox<kBboxThreads>, s->nchunks, kBboxThreads, 0, st, cur.x, cur.y,
-                  s->chunk_seg, s->chunk_begin, s->chunk_end, s->box_ord, s->status));
+    if (!carry)
+        CK(launch_pdl(k_bbox<kBboxThreads>, s->nchunks, kBboxThreads, 0, st, cur.x, cur.y,
+                      s->chunk_seg, s->chunk_begin, s->chunk_end, s->box_ord, s->status));
     CK(mark(1));
     // keys and positions; the moments counters and the step's words cleared
-    CK(launch_pdl(k_keys_step, nb, tb, 0, st, cur.x, cur.y, n, segs, s->box_ord, s->keys, s->vals,
+    CK(launch_pdl(k_keys_step, nb, tb, 0, st, cur.x, cur.y, n, segs,
+                  carry ? (const int*)s->box_next : (const int*)s->box_ord, s->keys, s->vals,
                   s->counter, reinterpret_cast<int*>(s->inter), keep_stats ? 0 : kStepZero,
-                  s->work + kWorkSortOverflow, s->seg_cost, s->mean_cost));
+                  s->work + kWorkSortOverflow, s->seg_cost, s->mean_cost,
+                  carry ? s->box_ord : (int*)nullptr));
     CK(mark(2));
 
     // Sort (stable, by key, then by system): LSD passes over the key's top
@@ -425,8 +434,9 @@ int enqueue_sort(bh_system* s, cudaStream_t st, cudaEvent_t* ev, bool keep_stats
             vi = vo;
         }
     }
+    // the fixup also resets box_next for this step's walk (fold)
     CK(launch_pdl(k_sort_fixup, nb, tb, 0, st, n, 64 - 8 * s->high_passes, kB, vB, kA, vA, overflow,
-                  cond, capturing ? 1 : 0));
+                  cond, capturing ? 1 : 0, fold ? s->box_next : (int*)nullptr, 4 * s->nseg));
     if (capturing) {
         const cudaGraphNode_t* deps = nullptr;
         size_t ndeps = 0;
@@ -466,8 +476,10 @@ int enqueue_sort(bh_system* s, cudaStream_t st, cudaEvent_t* ev, bool keep_stats
 // ev (optional): events recorded at the phase boundaries.  keep_stats: leave
 // the last step's interaction counts and walk statistics (the energy pass).
 // part: kStepPre stops after the sort, kStepPost starts at the reorder.
+// carry, fold: see enqueue_sort.
 int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev,
-                  bool keep_stats = false, int part = kStepAll) {
+                  bool keep_stats = false, int part = kStepAll, bool carry = false,
+                  bool fold = false) {
     const int n = s->n;
     auto mark = [&](int k) -> cudaError_t { return ev ? cudaEventRecord(ev[k], st) : cudaSuccess; };
     const bool mixed = s->p.mode == BH_MODE_MIXED;
@@ -475,7 +487,7 @@ int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev,
     const BodyPtrs& cur = s->st[0];
     const int tb = 256, nb = (n + tb - 1) / tb;
     if (part != kStepPost) {
-        int rc = enqueue_sort(s, st, ev, keep_stats);
+        int rc = enqueue_sort(s, st, ev, keep_stats, carry, fold);
         if (rc != BH_OK) return rc;
     }
     // the sorted keys and permutation: in kA after the fixup, moved by each
@@ -527,11 +539,22 @@ int enqueue_front(bh_system* s, cudaStream_t st, bool accuracy, cudaEvent_t* ev,
 // state only) and the walk fused with the integration (phases 6-7).
 // boot < 0: the bootstrap pass is launched iff bh_set_state came since the last
 // step (the host's record, cleared here); 0 / 1: left out / launched (graph capture).
+// carry < 0: a whole step takes the box folded by the last walk iff the host's
+// record says it is the box of the current positions; 0 / 1: box kernel /
+// carried (graph capture).  The walk folds the next step's box.  The host's
+// record is updated here for steps enqueued outside a capture, and by bh_step
+// for graph launches.
 int enqueue_step(bh_system* s, cudaStream_t st, cudaEvent_t* ev = nullptr, int boot = -1,
-                 int part = kStepAll) {
+                 int part = kStepAll, int carry = -1) {
     auto mark = [&](int k) -> cudaError_t { return ev ? cudaEventRecord(ev[k], st) : cudaSuccess; };
-    int rc = enqueue_front(s, st, s->p.mode != BH_MODE_REFERENCE, ev, false, part);
-    if (rc != BH_OK || part == kStepPre) return rc;
+    const bool carried = carry < 0 ? (part == kStepAll && s->box_valid) : carry > 0;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(st, &cap));
+    const bool capturing = cap == cudaStreamCaptureStatusActive;
+    int rc = enqueue_front(s, st, s->p.mode != BH_MODE_REFERENCE, ev, false, part, carried, true);
+    if (rc != BH_OK) return rc;
+    if (!capturing) s->box_valid = false;  // box_next is reset by this step's sort
+    if (part == kStepPre) return rc;
     const bool with_boot = boot < 0 ? s->fresh_host : boot > 0;
     if (boot < 0) s->fresh_host = false;
     StepArgs a = step_args(s);
@@ -549,6 +572,7 @@ int enqueue_step(bh_system* s, cudaStream_t st, cudaEvent_t* ev = nullptr, int b
     CK(mark(8));
     CK(launch_walk(a, st, 1));
     CK(mark(9));
+    if (!capturing) s->box_valid = true;
     return BH_OK;
 }
 
@@ -690,10 +714,10 @@ int build_graph(bh_system* s, int slot) {
     if (!s->cap_stream) CK(cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking));
     if (!s->cond_stream) CK(cudaStreamCreateWithFlags(&s->cond_stream, cudaStreamNonBlocking));
     RC(make_fork_stream(s));
-    const int part = slot < 2 ? kStepAll : slot == 2 ? kStepPre : kStepPost;
+    const int part = (slot < 2 || slot == kGraphCarried) ? kStepAll : slot == 2 ? kStepPre : kStepPost;
     const int boot = (slot == 1 || slot == 4) ? 1 : 0;
     CK(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal));
-    int st = enqueue_step(s, s->cap_stream, nullptr, boot, part);
+    int st = enqueue_step(s, s->cap_stream, nullptr, boot, part, slot == kGraphCarried ? 1 : 0);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(s->cap_stream, &g);
     if (st != BH_OK) {
@@ -817,6 +841,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     bytes += 2 * (8 * span<float>(N) + 2 * span<int>(N));
     bytes += 3 * span<uint64_t>(N) + 3 * span<uint32_t>(N);
     bytes += span<uint32_t>((size_t)256 * s->tiles) + span<uint32_t>(256);
+    bytes += span<int>(4 * (size_t)nseg);
     bytes += span<int>(4 * (size_t)nseg) + 3 * span<int>(nseg + 1) + span<int>(N);
     bytes += 3 * span<int>(s->nchunks);
     bytes += 8 * span<int>(N) + span<int4>(N);                  // tree arrays, counter, climb
@@ -856,6 +881,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     s->vals3 = carve<uint32_t>(c, N);
     s->hist = carve<uint32_t>(c, (size_t)256 * s->tiles);
     s->totals = carve<uint32_t>(c, 256);
+    s->box_next = carve<int>(c, 4 * (size_t)nseg);
     s->box_ord = carve<int>(c, 4 * (size_t)nseg);
     s->seg_off = carve<int>(c, nseg + 1);
     s->gseg_off = carve<int>(c, nseg + 1);
@@ -1040,6 +1066,7 @@ int bh_num_bodies(const bh_system* s) { return s ? s->n : -1; }
 int bh_set_state(bh_system* s, const float* x, const float* y, const float* vx, const float* vy,
                  const float* mass, void* stream) {
     if (!s || !x || !y || !vx || !vy || !mass) return BH_ERR_ARG;
+    s->box_valid = false;  // new positions: the next step takes the box kernel
     CK(cudaSetDevice(s->device));
     cudaStream_t st = (cudaStream_t)stream;
     const size_t b = sizeof(float) * s->n;
@@ -1192,10 +1219,12 @@ int bh_step(bh_system* s, int steps, void* stream) {
                 RC(join_inputs(s, st));
                 CK(cudaGraphLaunch(s->graph_exec[3 + gi], st));
             } else {
-                int rc = ensure(gi);
+                const int slot = (gi == 0 && s->box_valid) ? kGraphCarried : gi;
+                int rc = ensure(slot);
                 if (rc != BH_OK) return rc;
-                CK(cudaGraphLaunch(s->graph_exec[gi], st));
+                CK(cudaGraphLaunch(s->graph_exec[slot], st));
             }
+            s->box_valid = true;  // every step graph ends with the folding walk
             s->fresh_host = false;
             s->caller_order = false;
             if (s->energy_every > 0 && ++s->energy_steps % s->energy_every == 0) {
@@ -1360,12 +1389,14 @@ int bh_get_debug(bh_system* s, const char* name, void* host_out, size_t bytes, v
     const void* src = nullptr;
     size_t need = 0;
     std::string nm(name);
-    if (nm == "box") {
-        if (bytes < 16) return BH_ERR_ARG;
-        int box[4];
-        CK(cudaMemcpy(box, s->box_ord, sizeof(box), cudaMemcpyDeviceToHost));
+    if (nm == "box" || nm == "boxes") {
+        // the last step's box of system 0 (box) or of every system (boxes: 4 nseg floats)
+        const size_t words = nm == "box" ? 4 : 4 * (size_t)s->nseg;
+        if (bytes < 4 * words) return BH_ERR_ARG;
+        std::vector<int> box(words);
+        CK(cudaMemcpy(box.data(), s->box_ord, 4 * words, cudaMemcpyDeviceToHost));
         float* f = (float*)host_out;
-        for (int k = 0; k < 4; ++k) {
+        for (size_t k = 0; k < words; ++k) {
             int i = box[k];
             int b = i >= 0 ? i : (i ^ 0x7fffffff);
             std::memcpy(&f[k], &b, 4);
@@ -1731,6 +1762,7 @@ int bh_autotune(bh_system* s, void* stream, bh_params* chosen) {
         CK(cudaMemcpyAsync(s->fresh, bk + 9 * N, sizeof(int), cudaMemcpyDeviceToDevice, st));
         CK(cudaMemsetAsync(s->status, 0, sizeof(int), st));
         s->fresh_host = orig_fresh;
+        s->box_valid = false;  // positions put back: box_next is a trial step's
         return BH_OK;
     };
     const bh_params orig = s->p;

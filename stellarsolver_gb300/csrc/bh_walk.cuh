@@ -37,6 +37,60 @@ struct WalkOut {
     float *ax, *ay;
     float* amag;  // |a| of this step, for the next step's relative rule
     int* gcost;   // this step's walk-group cost (interaction entries) of each body
+    int* box_next;  // [4 nseg] the next step's box (order-preserving ints), folded by the
+                    // integrating passes; null: not folded
+};
+
+// The next step's bounding box, folded into the integration (the positions a
+// walk writes are the next step's): each lane keeps the min / max of the
+// positions it writes, starting from the origin as the box kernel does
+// (kernels.cu:54-57); a warp adds its box to box_next[4 seg] when its system
+// changes and at its end, with one atomicMin / atomicMax per value that would
+// move the box.  Min and max are exact, so the box is the box kernel's over
+// the same positions.  A non-finite position raises ST_NONFINITE, as the box
+// kernel would in the next step.
+struct BoxFold {
+    float l = 0.0f, r = 0.0f, b = 0.0f, t = 0.0f;
+    int seg = -1;  // warp-uniform: the system of the positions held
+    bool bad = false;
+
+    __device__ __forceinline__ void add(float x, float y) {
+        bad |= !isfinite(x) || !isfinite(y);
+        l = fminf(l, x);
+        r = fmaxf(r, x);
+        b = fminf(b, y);
+        t = fmaxf(t, y);
+    }
+    // whole warp
+    __device__ __forceinline__ void flush(int* box_next, int* status) {
+        if (seg < 0 || !box_next) return;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            l = fminf(l, __shfl_xor_sync(kFull, l, o));
+            r = fmaxf(r, __shfl_xor_sync(kFull, r, o));
+            b = fminf(b, __shfl_xor_sync(kFull, b, o));
+            t = fmaxf(t, __shfl_xor_sync(kFull, t, o));
+        }
+        const bool any_bad = __any_sync(kFull, bad);
+        if ((threadIdx.x & 31) == 0) {
+            int* bo = box_next + 4 * seg;
+            const int4 cur = __ldcg(reinterpret_cast<const int4*>(bo));  // may be stale: only skips
+            if (f2ord(l) < cur.x) atomicMin(bo + 0, f2ord(l));
+            if (f2ord(r) > cur.y) atomicMax(bo + 1, f2ord(r));
+            if (f2ord(b) < cur.z) atomicMin(bo + 2, f2ord(b));
+            if (f2ord(t) > cur.w) atomicMax(bo + 3, f2ord(t));
+            if (any_bad) atomicOr(status, ST_NONFINITE);
+        }
+        l = r = b = t = 0.0f;
+        bad = false;
+    }
+    // whole warp, before the positions of a group of system sg are added
+    __device__ __forceinline__ void enter(int sg, int* box_next, int* status) {
+        if (sg != seg) {
+            flush(box_next, status);
+            seg = sg;
+        }
+    }
 };
 
 // Heaviest groups first.  A group is heavy when the largest previous-step
@@ -313,9 +367,10 @@ static __global__ void __launch_bounds__(kVoteWarps * 32) k_walk_vote(Segs segs,
     int* clist = s_clist[warp];
     int* blist = s_blist[warp];
     unsigned long long my_inter = 0;
+    BoxFold fold;
     for (int g = next_group(work); g < gr.ngroups; g = next_group(work)) {
-        int lo, hi, gstart;
-        group_range(segs, gr, g, &lo, &hi, &gstart);
+        int lo, hi, gstart, sg;
+        group_range(segs, gr, g, &lo, &hi, &gstart, 32, &sg);
         const int j = gstart + lane;
         const bool valid = j < hi;
         const int cnt = min(32, hi - gstart);
@@ -465,12 +520,16 @@ static __global__ void __launch_bounds__(kVoteWarps * 32) k_walk_vote(Segs segs,
         if (bcnt > 0) flush_bodies(bcnt);
         if (overflow && lane == 0) atomicOr(status, ST_STACK);
         my_inter += (unsigned long long)(entries * cnt);
+        fold.enter(sg, out.box_next, status);
         if (valid) {
             // kernels.cu:529-533: v += dt*a; x += d*dt*v
             float vx = __fadd_rn(in.vx[j], __fmul_rn(dt, ax));
             float vy = __fadd_rn(in.vy[j], __fmul_rn(dt, ay));
-            out.x[j] = __fadd_rn(px, __fmul_rn(ddt, vx));
-            out.y[j] = __fadd_rn(py, __fmul_rn(ddt, vy));
+            const float nx = __fadd_rn(px, __fmul_rn(ddt, vx));
+            const float ny = __fadd_rn(py, __fmul_rn(ddt, vy));
+            fold.add(nx, ny);
+            out.x[j] = nx;
+            out.y[j] = ny;
             out.vx[j] = vx;
             out.vy[j] = vy;
             out.m[j] = in.m[j];
@@ -479,6 +538,7 @@ static __global__ void __launch_bounds__(kVoteWarps * 32) k_walk_vote(Segs segs,
             out.ay[j] = ay;
         }
     }
+    fold.flush(out.box_next, status);
     if (lane == 0 && my_inter) atomicAdd(inter_total, my_inter);
 }
 
@@ -760,6 +820,7 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
     int* stack = clist + 64;
     int* blist = stack + ((STACK + 3) & ~3);
     unsigned long long my_inter = 0, my_cinter = 0;
+    BoxFold fold;  // main pass only (the bootstrap and diagnostics passes write no positions)
 
     // heavy groups first (hv.count set: the main pass), then the others in order
     const int nh = hv.count ? *hv.count : 0;
@@ -1219,6 +1280,7 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
             my_inter += (unsigned long long)(entries * cnt);
             my_cinter += (unsigned long long)(centries * cnt);
             if (hv.cost && lane == 0) atomicAdd(hv.cost + sg, (unsigned long long)(entries * cnt));
+            fold.enter(sg, out.box_next, status);
         }
 #pragma unroll
         for (int b = 0; b < BPL; ++b) {
@@ -1241,6 +1303,7 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
                 float inc = ddt * vx, hx = px[b], s = hx + inc, bb = s - hx;
                 float e = (hx - (s - bb)) + (inc - bb);
                 float lo2 = in.xlo[jb] + e, h2 = s + lo2;
+                const float nx = h2;
                 out.x[jb] = h2;
                 out.xlo[jb] = lo2 - (h2 - s);
                 inc = ddt * vy;
@@ -1252,9 +1315,12 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
                 h2 = s + lo2;
                 out.y[jb] = h2;
                 out.ylo[jb] = lo2 - (h2 - s);
+                fold.add(nx, h2);
             } else {
-                out.x[jb] = fmaf(ddt, vx, px[b]);
-                out.y[jb] = fmaf(ddt, vy, py[b]);
+                const float nx = fmaf(ddt, vx, px[b]), ny = fmaf(ddt, vy, py[b]);
+                out.x[jb] = nx;
+                out.y[jb] = ny;
+                fold.add(nx, ny);
             }
             out.vx[jb] = vx;
             out.vy[jb] = vy;
@@ -1266,6 +1332,7 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
             out.gcost[jb] = (int)min(entries, 1ll << 30);  // next step's heavy-group estimate
         }
     }
+    if (!ESTIMATE && !DIAG) fold.flush(out.box_next, status);
     if (!ESTIMATE && !DIAG && lane == 0 && my_inter) {
         atomicAdd(inter_total, my_inter);
         atomicAdd(inter_total + 1, my_cinter);  // of which body-cell

@@ -158,7 +158,9 @@ def test_sort_over_consecutive_steps(bh, oracle, graph, mode):
             s.step(1)
             s.sync()
             assert s.stats()["status"] == 0
-            k = oracle.keys(st["x"], st["y"], oracle.bbox(st["x"], st["y"]))
+            box = oracle.bbox(st["x"], st["y"])  # from step 1 on: the box the last walk folded
+            assert np.array_equal(s.debug("box").view(np.uint32), box.view(np.uint32)), step
+            k = oracle.keys(st["x"], st["y"], box)
             ok, _ = oracle.sort_keys(k)
             assert np.array_equal(s.debug("perm"), ok.astype(np.int32)), step
             assert np.array_equal(s.debug("keys"), k[ok]), step
