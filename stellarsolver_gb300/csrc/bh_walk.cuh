@@ -42,28 +42,39 @@ struct WalkOut {
 };
 
 // The next step's bounding box, folded into the integration (the positions a
-// walk writes are the next step's): each lane keeps the min / max of the
-// positions it writes, starting from the origin as the box kernel does
-// (kernels.cu:54-57); a warp adds its box to box_next[4 seg] when its system
-// changes and at its end, with one atomicMin / atomicMax per value that would
-// move the box.  Min and max are exact, so the box is the box kernel's over
-// the same positions.  A non-finite position raises ST_NONFINITE, as the box
-// kernel would in the next step.
+// walk writes are the next step's).  After each group a warp reduces its new
+// positions' box (from the origin, as the box kernel starts: kernels.cu:54-57)
+// with shuffles into a per-warp box in shared memory (a float4 and the
+// system it belongs to, no registers held across the walk); when the system
+// changes and at the warp's end, the box goes to box_next[4 seg] with one
+// atomicMin / atomicMax per value that would move it.  Min and max are exact,
+// so the box is the box kernel's over the same positions.  A non-finite
+// position raises ST_NONFINITE, as the box kernel would in the next step.
 struct BoxFold {
-    float l = 0.0f, r = 0.0f, b = 0.0f, t = 0.0f;
-    int seg = -1;  // warp-uniform: the system of the positions held
-    bool bad = false;
+    float4* box;  // shared: this warp's box (l, r, b, t)
+    int* seg;     // shared: its system, -1: none
+    int* box_next;
+    int* status;
 
-    __device__ __forceinline__ void add(float x, float y) {
-        bad |= !isfinite(x) || !isfinite(y);
-        l = fminf(l, x);
-        r = fmaxf(r, x);
-        b = fminf(b, y);
-        t = fmaxf(t, y);
+    __device__ __forceinline__ void init() const {
+        if ((threadIdx.x & 31) == 0) {
+            *box = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            *seg = -1;
+        }
+        __syncwarp();
     }
-    // whole warp
-    __device__ __forceinline__ void flush(int* box_next, int* status) {
-        if (seg < 0 || !box_next) return;
+    // lane 0
+    __device__ __forceinline__ void publish(int sg, float4 v) const {
+        int* bo = box_next + 4 * sg;
+        const int4 cur = __ldcg(reinterpret_cast<const int4*>(bo));  // may be stale: only skips
+        if (f2ord(v.x) < cur.x) atomicMin(bo + 0, f2ord(v.x));
+        if (f2ord(v.y) > cur.y) atomicMax(bo + 1, f2ord(v.y));
+        if (f2ord(v.z) < cur.z) atomicMin(bo + 2, f2ord(v.z));
+        if (f2ord(v.w) > cur.w) atomicMax(bo + 3, f2ord(v.w));
+    }
+    // whole warp, after a group of system sg: (l, r, b, t) is this lane's new
+    // positions' box from the origin
+    __device__ __forceinline__ void group(int sg, float l, float r, float b, float t) const {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             l = fminf(l, __shfl_xor_sync(kFull, l, o));
@@ -71,25 +82,24 @@ struct BoxFold {
             b = fminf(b, __shfl_xor_sync(kFull, b, o));
             t = fmaxf(t, __shfl_xor_sync(kFull, t, o));
         }
-        const bool any_bad = __any_sync(kFull, bad);
         if ((threadIdx.x & 31) == 0) {
-            int* bo = box_next + 4 * seg;
-            const int4 cur = __ldcg(reinterpret_cast<const int4*>(bo));  // may be stale: only skips
-            if (f2ord(l) < cur.x) atomicMin(bo + 0, f2ord(l));
-            if (f2ord(r) > cur.y) atomicMax(bo + 1, f2ord(r));
-            if (f2ord(b) < cur.z) atomicMin(bo + 2, f2ord(b));
-            if (f2ord(t) > cur.w) atomicMax(bo + 3, f2ord(t));
-            if (any_bad) atomicOr(status, ST_NONFINITE);
+            float4 v = *box;
+            if (*seg != sg) {
+                if (*seg >= 0) publish(*seg, v);
+                v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                *seg = sg;
+            }
+            *box = make_float4(fminf(v.x, l), fmaxf(v.y, r), fminf(v.z, b), fmaxf(v.w, t));
         }
-        l = r = b = t = 0.0f;
-        bad = false;
+        __syncwarp();
     }
-    // whole warp, before the positions of a group of system sg are added
-    __device__ __forceinline__ void enter(int sg, int* box_next, int* status) {
-        if (sg != seg) {
-            flush(box_next, status);
-            seg = sg;
-        }
+    // one position written by this lane
+    __device__ __forceinline__ void check(float x, float y) const {
+        if (!isfinite(x) || !isfinite(y)) atomicOr(status, ST_NONFINITE);
+    }
+    // whole warp, at its end
+    __device__ __forceinline__ void finish() const {
+        if ((threadIdx.x & 31) == 0 && *seg >= 0) publish(*seg, *box);
     }
 };
 
@@ -367,7 +377,10 @@ static __global__ void __launch_bounds__(kVoteWarps * 32) k_walk_vote(Segs segs,
     int* clist = s_clist[warp];
     int* blist = s_blist[warp];
     unsigned long long my_inter = 0;
-    BoxFold fold;
+    __shared__ float4 s_fold[kVoteWarps];
+    __shared__ int s_fold_seg[kVoteWarps];
+    const BoxFold fold{s_fold + warp, s_fold_seg + warp, out.box_next, status};
+    if (out.box_next) fold.init();
     for (int g = next_group(work); g < gr.ngroups; g = next_group(work)) {
         int lo, hi, gstart, sg;
         group_range(segs, gr, g, &lo, &hi, &gstart, 32, &sg);
@@ -520,14 +533,18 @@ static __global__ void __launch_bounds__(kVoteWarps * 32) k_walk_vote(Segs segs,
         if (bcnt > 0) flush_bodies(bcnt);
         if (overflow && lane == 0) atomicOr(status, ST_STACK);
         my_inter += (unsigned long long)(entries * cnt);
-        fold.enter(sg, out.box_next, status);
+        float wl = 0.0f, wr = 0.0f, wb = 0.0f, wt = 0.0f;  // new positions' box, from the origin
         if (valid) {
             // kernels.cu:529-533: v += dt*a; x += d*dt*v
             float vx = __fadd_rn(in.vx[j], __fmul_rn(dt, ax));
             float vy = __fadd_rn(in.vy[j], __fmul_rn(dt, ay));
             const float nx = __fadd_rn(px, __fmul_rn(ddt, vx));
             const float ny = __fadd_rn(py, __fmul_rn(ddt, vy));
-            fold.add(nx, ny);
+            fold.check(nx, ny);
+            wl = fminf(wl, nx);
+            wr = fmaxf(wr, nx);
+            wb = fminf(wb, ny);
+            wt = fmaxf(wt, ny);
             out.x[j] = nx;
             out.y[j] = ny;
             out.vx[j] = vx;
@@ -537,8 +554,9 @@ static __global__ void __launch_bounds__(kVoteWarps * 32) k_walk_vote(Segs segs,
             out.ax[j] = ax;
             out.ay[j] = ay;
         }
+        if (out.box_next) fold.group(sg, wl, wr, wb, wt);
     }
-    fold.flush(out.box_next, status);
+    if (out.box_next) fold.finish();
     if (lane == 0 && my_inter) atomicAdd(inter_total, my_inter);
 }
 
@@ -814,13 +832,19 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
     float4* bxy = reinterpret_cast<float4*>(cpair.t11 + 16);
     float2* bm = reinterpret_cast<float2*>(bxy + 16);
     int2* bid = reinterpret_cast<int2*>(bm + 16);
-    float2* gp = reinterpret_cast<float2*>(wbase + 3 * 32 * 16);  // the group's GW positions
-    float4* gext = reinterpret_cast<float4*>(gp + GW);  // y at min/max x, x at min/max y
+    // the group's GW positions in pairs: (x_2i, x_2i+1, y_2i, y_2i+1)
+    float4* gp = reinterpret_cast<float4*>(wbase + 3 * 32 * 16);
+    float4* gext = gp + GW / 2;  // y at min/max x, x at min/max y
     int* clist = reinterpret_cast<int*>(gext + 1);
     int* stack = clist + 64;
     int* blist = stack + ((STACK + 3) & ~3);
     unsigned long long my_inter = 0, my_cinter = 0;
-    BoxFold fold;  // main pass only (the bootstrap and diagnostics passes write no positions)
+    // main pass only (the bootstrap and diagnostics passes write no positions);
+    // its shared box sits in the spare bytes after the staged body pairs
+    const bool folding = !ESTIMATE && !DIAG && out.box_next != nullptr;
+    const BoxFold fold{reinterpret_cast<float4*>(wbase + 1408), reinterpret_cast<int*>(wbase + 1424),
+                       out.box_next, status};
+    if (folding) fold.init();
 
     // heavy groups first (hv.count set: the main pass), then the others in order
     const int nh = hv.count ? *hv.count : 0;
@@ -856,7 +880,9 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
         float gx0 = px[0], gx1 = px[0], gy0 = py[0], gy1 = py[0];
 #pragma unroll
         for (int b = 0; b < BPL; ++b) {
-            gp[32 * b + lane] = make_float2(px[b], py[b]);
+            float* gq = reinterpret_cast<float*>(gp + ((32 * b + lane) >> 1));
+            gq[lane & 1] = px[b];
+            gq[2 + (lane & 1)] = py[b];
             gx0 = fminf(gx0, px[b]);
             gx1 = fmaxf(gx1, px[b]);
             gy0 = fminf(gy0, py[b]);
@@ -1160,6 +1186,9 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
             // group's bodies is needed only when the box test is inconclusive,
             // i.e. d_box <= ropen < d_box + box diagonal, for some lane.
             float4 A = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            // the children are loaded with the node's records (not after the
+            // decision): an opened node then costs no second round trip
+            int4 C = make_int4(kNoChild, kNoChild, kNoChild, kNoChild);
             float d2 = 0.0f;
             bool need = false;
             if (node >= 0) {
@@ -1196,14 +1225,20 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
                 }
                 unsigned nm = __ballot_sync(kFull, need);
                 if (__popc(nm) > kSerialExactLanes) {
-                    float e2 = __int_as_float(0x7f800000);
+                    // every lane: its node against the group's bodies, two at a
+                    // time in FP32x2 (per component the scalar operations)
+                    float2 e2 = make_float2(__int_as_float(0x7f800000), __int_as_float(0x7f800000));
+                    const float2 nax = make_float2(-A.x, -A.x), nay = make_float2(-A.y, -A.y);
 #pragma unroll 8
-                    for (int e = 0; e < GW; ++e) {
-                        float2 q = gp[e];
-                        float dx = q.x - A.x, dy = q.y - A.y;
-                        e2 = fminf(e2, fmaf(dx, dx, dy * dy));
+                    for (int e = 0; e < GW / 2; ++e) {
+                        const float4 q = gp[e];
+                        const float2 dx = __fadd2_rn(make_float2(q.x, q.y), nax);
+                        const float2 dy = __fadd2_rn(make_float2(q.z, q.w), nay);
+                        const float2 r = __ffma2_rn(dx, dx, __fmul2_rn(dy, dy));
+                        e2.x = fminf(e2.x, r.x);
+                        e2.y = fminf(e2.y, r.y);
                     }
-                    if (need) d2 = e2;
+                    if (need) d2 = fminf(e2.x, e2.y);
                 } else {
                     while (nm) {
                         const int src = __ffs(nm) - 1;
@@ -1231,7 +1266,6 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
             unsigned mc = __ballot_sync(kFull, cat == 0);
             if (cat == 0) clist[ccnt + __popc(mc & lt)] = node;
             ccnt += __popc(mc);
-            int4 C = make_int4(kNoChild, kNoChild, kNoChild, kNoChild);
             if (cat == 2) C = recC[node];
             const int cs[4] = {C.x, C.y, C.z, C.w};
             int nb = cat == 1 ? D.y : 0, nn = 0;
@@ -1280,8 +1314,8 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
             my_inter += (unsigned long long)(entries * cnt);
             my_cinter += (unsigned long long)(centries * cnt);
             if (hv.cost && lane == 0) atomicAdd(hv.cost + sg, (unsigned long long)(entries * cnt));
-            fold.enter(sg, out.box_next, status);
         }
+        float wl = 0.0f, wr = 0.0f, wb = 0.0f, wt = 0.0f;  // new positions' box, from the origin
 #pragma unroll
         for (int b = 0; b < BPL; ++b) {
             if (!valid[b]) continue;
@@ -1315,12 +1349,20 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
                 h2 = s + lo2;
                 out.y[jb] = h2;
                 out.ylo[jb] = lo2 - (h2 - s);
-                fold.add(nx, h2);
+                fold.check(nx, h2);
+                wl = fminf(wl, nx);
+                wr = fmaxf(wr, nx);
+                wb = fminf(wb, h2);
+                wt = fmaxf(wt, h2);
             } else {
                 const float nx = fmaf(ddt, vx, px[b]), ny = fmaf(ddt, vy, py[b]);
                 out.x[jb] = nx;
                 out.y[jb] = ny;
-                fold.add(nx, ny);
+                fold.check(nx, ny);
+                wl = fminf(wl, nx);
+                wr = fmaxf(wr, nx);
+                wb = fminf(wb, ny);
+                wt = fmaxf(wt, ny);
             }
             out.vx[jb] = vx;
             out.vy[jb] = vy;
@@ -1331,8 +1373,9 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
             out.amag[jb] = sqrtf(gax * gax + gay * gay);
             out.gcost[jb] = (int)min(entries, 1ll << 30);  // next step's heavy-group estimate
         }
+        if (folding) fold.group(sg, wl, wr, wb, wt);
     }
-    if (!ESTIMATE && !DIAG) fold.flush(out.box_next, status);
+    if (folding) fold.finish();
     if (!ESTIMATE && !DIAG && lane == 0 && my_inter) {
         atomicAdd(inter_total, my_inter);
         atomicAdd(inter_total + 1, my_cinter);  // of which body-cell
