@@ -18,6 +18,8 @@ force walk fused with the integration.
           quadrupole cells at 33 flops beside it, and per-phase HBM fractions.
   reference_mode  the reference's own walk rule (monopole warp vote) on the
           GPU, same workload: the like-for-like figure for the reference arm.
+  dropin  the reference's own update() order through the nine drop-in
+          wrappers (Particle_cuda.cuh) on arrays of its layout, same workload.
   ensemble  256 systems, N log-uniform in [2^10, 2^17]: the batched MIXED
           engine against one PLAIN handle per system.
 
@@ -285,6 +287,9 @@ def run_engine(args):
                       "interactions_per_step": ref_inter,
                       "rule": "reference warp vote (monopole, kernels.cu:395-411), CUDA graph, "
                               "L2 flushed before every timed step"}
+    # the drop-in path: the reference's own update() order through the nine
+    # C-linkage wrappers on arrays of its layout (m = 2n + 12000), same workload
+    dropin = run_dropin(torch, stream, sp, flush, n, x, y, vx, vy, m, args)
     ens = None
     if not args.no_ensemble:
         ens = run_ensemble(bh, torch, stream, sp, local, world, rank, args)
@@ -319,6 +324,7 @@ def run_engine(args):
                        "interactions_per_step": inter["plain"]},
         "mixed_over_plain_single_system": round(value / world / sides["plain_single_system_nograph"], 3),
         "reference_mode": reference_mode,
+        "dropin": dropin,
         "momentum_drift_rel": float(np.abs(p1 - p0).max() / pscale),
         "tree": {"cells": stats["cells"], "nodes": stats["nodes"], "max_depth": stats["max_depth"]},
         "roofline": {"bound": "fp32", "kernel": "k_walk_acc", "achieved": round(achieved, 3),
@@ -414,6 +420,40 @@ def run_e2e(bh, torch, stream, sp, n, x, y, vx, vy, m, params, local, args):
             "h2d_bytes_per_step": 28 * n, "d2h_bytes_per_step": 8 * n,
             "path": "bh_set_state + bh_set_accel (pinned host: the arrays of the reference's "
                     "reset()) + bh_step + bh_get_state(x, y -> pinned host)"}
+
+
+def run_dropin(torch, stream, sp, flush, n, x, y, vx, vy, m, args):
+    """steps/s of BarnesHutParticleSystem::update() (BarnesHutParticleSystem.cpp:308-315)
+    through the drop-in wrappers: ResetArrays ... FillOutputArray on the compat stream,
+    CUDA events per step, L2 flushed before each."""
+    from stellarsolver_gb300 import dropin
+
+    L = dropin.load()
+    L.bh_compat_set_stream(sp)
+    L.bh_compat_set_constants(THETA, EPS * EPS)
+    L.bh_compat_clear_status()
+    a = dropin.RefArrays(torch, x, y, vx, vy, m)
+    for _ in range(args.warmup):
+        dropin.update(L, a, DT, 1.0)
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    for e0, e1 in evs:
+        flush.zero_()
+        e0.record(stream)
+        dropin.update(L, a, DT, 1.0)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    secs = sum(e0.elapsed_time(e1) for e0, e1 in evs) / 1e3
+    status = L.bh_compat_status()
+    L.bh_compat_set_stream(None)
+    L.bh_compat_release()
+    return {"steps_per_s": round(args.steps / secs, 3), "ms_per_step": round(1e3 * secs / args.steps, 4),
+            "status": status,
+            "path": "ResetArrays, ComputeBoundingBox, BuildQuadTree, ComputeCentreOfMass, "
+                    "SortParticles, CalculateForces, IntegrateParticles, FillOutputArray "
+                    "(BarnesHutParticleSystem.cpp:308-315), C linkage, arrays of 2n + 12000, "
+                    "L2 flushed before every timed step"}
 
 
 def run_ensemble(bh, torch, stream, sp, local, world, rank, args):

@@ -90,7 +90,7 @@ void bh_compat_release(void);
  * allocation stall, and code whose allocator the library cannot call.
  * BuildQuadTree grows a cached workspace with cudaMalloc; this variant calls
  * no cudaMalloc/cudaFree and no allocating library routine.  Its scratch is
- * one static device array sized for at most 65536 bodies (about 8 MiB), which
+ * one static device array sized for at most 65536 bodies (about 8.5 MiB), which
  * every GPU that loads the library holds until the process exits.
  *   - Same arguments and outputs as BuildQuadTree.  Returns a BH_* status:
  *     BH_ERR_CAPACITY for n > 65536 (see bh_last_error), else the build's

@@ -53,8 +53,9 @@ struct Workspace {
     size_t cap = 0;  // bodies
     size_t mcap = 0;  // nodes (m) for the frontier queues
     void* base = nullptr;
-    uint64_t *keys, *keys_alt;
-    uint32_t *vals, *vals_alt;
+    uint64_t *keys, *keys_alt, *keys3;  // keys3: the third buffer of the high-word sort
+    uint32_t *vals, *vals_alt, *vals3;
+    int* overflow;                       // a run of equal high words longer than kFixupRun
     uint32_t *hist, *totals;
     int tiles;
     int* box_ord;
@@ -143,9 +144,10 @@ Workspace* workspace(size_t n, size_t m) {
     size_t N = std::max(n, w->cap), M = std::max(m, w->mcap);
     int tiles = (int)((N + kSortTile - 1) / kSortTile);
     int nb = (int)((N + 1023) / 1024);
-    size_t bytes = 2 * al(8 * N) + 2 * al(4 * N) + al(4 * 256 * (size_t)tiles) + al(4 * 256) +
-                   al(16) + al(8) + 8 * al(4 * N) + al(16 * N) + 2 * al(16 * N) + 3 * al(4 * N) +
-                   2 * al(4 * N) + al(4 * (size_t)nb) + al(4) + 2 * al(4 * M) + al(4);
+    size_t bytes = 3 * al(8 * N) + 3 * al(4 * N) + al(4) + al(4 * 256 * (size_t)tiles) +
+                   al(4 * 256) + al(16) + al(8) + 8 * al(4 * N) + al(16 * N) + 2 * al(16 * N) +
+                   3 * al(4 * N) + 2 * al(4 * N) + al(4 * (size_t)nb) + al(4) + 2 * al(4 * M) +
+                   al(4);
     if (cudaMalloc(&w->base, bytes) != cudaSuccess) {
         w->base = nullptr;
         w->cap = w->mcap = 0;
@@ -159,8 +161,11 @@ Workspace* workspace(size_t n, size_t m) {
     };
     w->keys = (uint64_t*)take(8 * N);
     w->keys_alt = (uint64_t*)take(8 * N);
+    w->keys3 = (uint64_t*)take(8 * N);
     w->vals = (uint32_t*)take(4 * N);
     w->vals_alt = (uint32_t*)take(4 * N);
+    w->vals3 = (uint32_t*)take(4 * N);
+    w->overflow = (int*)take(4);
     w->hist = (uint32_t*)take(4 * 256 * (size_t)tiles);
     w->totals = (uint32_t*)take(4 * 256);
     w->box_ord = (int*)take(16);
@@ -611,9 +616,12 @@ int fetch_status(Workspace* w) {
 
 // BuildQuadTree's launch sequence on the scratch of w, which must hold n
 // bodies (shared by BuildQuadTree and BuildQuadTreeNoAlloc).  Keys of the
-// bodies in the caller's box, the 8-pass radix sort of the whole key, the
-// radix tree and its node sums, then the tree written out in the reference
-// layout (child, count, start, cell x/y/mass, *index).
+// bodies in the caller's box; the engine's sort: stable passes over the high
+// word (3, or 4 above 2^21 bodies), then each run of equal high words put in
+// whole-key order, and, only when a run is longer than kFixupRun, the 8-pass
+// sort of the whole key (its kernels return at once unless the fixup raised
+// the flag); the radix tree and its node sums, then the tree written out in
+// the reference layout (child, count, start, cell x/y/mass, *index).
 cudaError_t enqueue_build(Workspace& w, float* x, float* y, float* mass, int* count, int* start,
                           int* child, int* index, float* left, float* right, float* bottom,
                           float* top, int n, int m, cudaStream_t st) {
@@ -623,18 +631,47 @@ cudaError_t enqueue_build(Workspace& w, float* x, float* y, float* mass, int* co
     k_c_box_to_ord<<<1, 1, 0, st>>>(left, right, bottom, top, w.box_ord, w.seg_off, n);
     Segs segs{1, w.seg_off, nullptr};
     k_keys<<<nb, 256, 0, st>>>(x, y, n, segs, w.box_ord, w.keys, w.vals);
-    uint64_t *ka = w.keys, *kb = w.keys_alt;
-    uint32_t *va = w.vals, *vb = w.vals_alt;
+    e = cudaMemsetAsync(w.overflow, 0, sizeof(int), st);
+    if (e != cudaSuccess) return e;
     const int tiles = (n + kSortTile - 1) / kSortTile;
-    for (int ps = 0; ps < 8; ++ps) {
-        k_radix_hist<<<tiles, kSortThreads, 0, st>>>(ka, va, n, 8 * ps, 0, nullptr, w.hist, tiles,
-                                                     nullptr);
-        k_radix_scan<<<256, kSortThreads, 0, st>>>(w.hist, tiles, w.totals, nullptr);
-        k_radix_scatter<<<tiles, kSortThreads, 0, st>>>(ka, va, kb, vb, n, 8 * ps, 0, nullptr,
-                                                        w.hist, w.totals, tiles, nullptr);
-        std::swap(ka, kb);
-        std::swap(va, vb);
+    auto pass = [&](const uint64_t* ki, const uint32_t* vi, uint64_t* ko, uint32_t* vo, int shift,
+                    const int* only_if) {
+        k_radix_hist<<<tiles, kSortThreads, 0, st>>>(ki, vi, n, shift, 0, nullptr, w.hist, tiles,
+                                                     only_if);
+        k_radix_scan<<<256, kSortThreads, 0, st>>>(w.hist, tiles, w.totals, only_if);
+        k_radix_scatter<<<tiles, kSortThreads, 0, st>>>(ki, vi, ko, vo, n, shift, 0, nullptr,
+                                                        w.hist, w.totals, tiles, only_if);
+    };
+    // high word: keys -> ... -> keys3, the fixup into keys_alt; the full sort
+    // (if flagged) keys -> keys3 / keys_alt alternately -> keys_alt
+    const int hp = n <= kShortSortMax ? 3 : 4;
+    {
+        const uint64_t* ki = w.keys;
+        const uint32_t* vi = w.vals;
+        for (int ps = 0; ps < hp; ++ps) {
+            const bool to_alt = ((hp - 1 - ps) & 1) != 0;
+            uint64_t* ko = to_alt ? w.keys_alt : w.keys3;
+            uint32_t* vo = to_alt ? w.vals_alt : w.vals3;
+            pass(ki, vi, ko, vo, 64 - 8 * (hp - ps), nullptr);
+            ki = ko;
+            vi = vo;
+        }
     }
+    k_sort_fixup<<<nb, 256, 0, st>>>(n, 64 - 8 * hp, w.keys3, w.vals3, w.keys_alt, w.vals_alt,
+                                     w.overflow, (cudaGraphConditionalHandle)0, 0, nullptr, 0);
+    {
+        const uint64_t* ki = w.keys;
+        const uint32_t* vi = w.vals;
+        for (int ps = 0; ps < 8; ++ps) {
+            uint64_t* ko = (ps & 1) ? w.keys_alt : w.keys3;
+            uint32_t* vo = (ps & 1) ? w.vals_alt : w.vals3;
+            pass(ki, vi, ko, vo, 8 * ps, w.overflow);
+            ki = ko;
+            vi = vo;
+        }
+    }
+    uint64_t* ka = w.keys_alt;
+    uint32_t* va = w.vals_alt;
     k_c_gather3<<<nb, 256, 0, st>>>(n, va, x, y, mass, w.sx, w.sy, w.sm);
     k_build<<<nb, 256, 0, st>>>(ka, n, segs, w.tree, w.status);
     k_moments<<<(n + kMomentsThreads - 1) / kMomentsThreads, kMomentsThreads, 0, st>>>(
@@ -826,7 +863,7 @@ void FillOutputArray(float* x, float* y, float* out, int n) { ssg::compat_FillOu
 // The existing wrapper grows a cached workspace with cudaMalloc.  This variant
 // takes its scratch from one file-scope __device__ array instead, sized for at
 // most kNoAllocMaxBodies bodies.  Every GPU that loads the library holds that
-// array (about 8 MiB) until the process exits.
+// array (about 8.5 MiB) until the process exits.
 // ---------------------------------------------------------------------------
 namespace {
 
@@ -836,7 +873,7 @@ constexpr size_t na_al(size_t b) { return (b + 255) & ~size_t(255); }
 
 // scratch bytes for n bodies, in the carve order of noalloc_layout()
 constexpr size_t noalloc_bytes(size_t n) {
-    return 2 * na_al(8 * n) + 2 * na_al(4 * n)                    // keys, values (ping-pong)
+    return 3 * na_al(8 * n) + 3 * na_al(4 * n) + na_al(4)        // keys, values (3 each), overflow
            + na_al(4 * 256 * ((n + kSortTile - 1) / kSortTile))  // digit histograms
            + na_al(4 * 256) + na_al(16) + na_al(8)                // totals, box, system offsets
            + 8 * na_al(4 * n) + na_al(16 * n)                     // tree arrays, counter, climb
@@ -890,8 +927,11 @@ void noalloc_layout(unsigned char* base, size_t n, Workspace* w) {
     const int nb = (int)((n + 1023) / 1024);
     w->keys = (uint64_t*)take(8 * n);
     w->keys_alt = (uint64_t*)take(8 * n);
+    w->keys3 = (uint64_t*)take(8 * n);
     w->vals = (uint32_t*)take(4 * n);
     w->vals_alt = (uint32_t*)take(4 * n);
+    w->vals3 = (uint32_t*)take(4 * n);
+    w->overflow = (int*)take(4);
     w->hist = (uint32_t*)take(4 * 256 * (size_t)tiles);
     w->totals = (uint32_t*)take(4 * 256);
     w->box_ord = (int*)take(16);
