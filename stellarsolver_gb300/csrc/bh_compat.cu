@@ -6,15 +6,18 @@
 // from n in node order, a chain of single-child cells above every branching
 // cell (the reference's tree is uncompressed, kernels.cu:197-252), child slots
 // by quadrant digit, cell x/y/mass = sum(m*x), sum(m*y), sum(m) and count.
-// SortParticles fills sorted[]/start[] by a level-by-level pass in one block;
+// SortParticles fills sorted[]/start[] by a level-by-level pass over the
+// whole device (a cooperative grid, one grid barrier per tree level);
 // CalculateForces is the warp-vote walk over child[] (kernels.cu:340-435).
 // Scratch buffers (keys, sort, tree, frontier queues) are kept per device and
 // grown on demand.  Each device also keeps the last tree layout a builder
 // produced (its child[] pointer and m), which SortParticles and
 // CalculateForces use to bound their reads of child[].
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -66,6 +69,7 @@ struct Workspace {
     float *sx, *sy, *sm;
     int *ncell, *cbase, *bsum, *total;
     int *qa, *qb;
+    int* qcount;  // three level counters of the SortParticles queues
     int* status;
 };
 
@@ -147,7 +151,7 @@ Workspace* workspace(size_t n, size_t m) {
     size_t bytes = 3 * al(8 * N) + 3 * al(4 * N) + al(4) + al(4 * 256 * (size_t)tiles) +
                    al(4 * 256) + al(16) + al(8) + 8 * al(4 * N) + al(16 * N) + 2 * al(16 * N) +
                    3 * al(4 * N) + 2 * al(4 * N) + al(4 * (size_t)nb) + al(4) + 2 * al(4 * M) +
-                   al(4);
+                   al(12) + al(4);
     if (cudaMalloc(&w->base, bytes) != cudaSuccess) {
         w->base = nullptr;
         w->cap = w->mcap = 0;
@@ -190,6 +194,7 @@ Workspace* workspace(size_t n, size_t m) {
     w->total = (int*)take(4);
     w->qa = (int*)take(4 * M);
     w->qb = (int*)take(4 * M);
+    w->qcount = (int*)take(12);
     w->status = (int*)take(4);
     w->tiles = tiles;
     w->cap = N;
@@ -511,6 +516,107 @@ __global__ void __launch_bounds__(1024) k_c_sort(const int* count, int* start, i
     if (threadIdx.x == 0 && (s_bad || level == 128)) atomicOr(status, ST_CAPACITY);
 }
 
+// The same assignment over the whole device: a cooperative grid of one block
+// per SM (fewer blocks make each grid barrier cheaper, and a level rarely holds
+// more cells than the grid has threads) takes each level's cells in a grid-stride loop and appends the next
+// level's cells with a global counter; one grid barrier per level.  A cell's
+// start and its bodies' places depend only on its parent's start and the
+// counts of its earlier siblings, so the result is the single block's (and the
+// reference's, kernels.cu:292-336) whatever the order of a level's cells.
+// Level counters rotate over three words: level L reads qcount[L % 3], fills
+// qcount[(L + 1) % 3] and clears qcount[(L + 2) % 3], which nobody reads or
+// writes during level L.
+constexpr int kSortGridThreads = 512;
+__global__ void __launch_bounds__(kSortGridThreads) k_c_sort_grid(const int* count, int* start, int* sorted,
+                                                     const int* child, int n, int mlimit, int* qa,
+                                                     int* qb, int cap, int* qcount, int* status,
+                                                     int child16) {
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    const long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long gsize = (long long)gridDim.x * blockDim.x;
+    bool bad = false;
+    if (gid == 0) {
+        int s = 0, k = 0;
+        for (int i = 0; i < 4; ++i) {
+            const int node = child[i];
+            if (node >= n) {
+                if (node >= mlimit || k >= cap) {
+                    bad = true;
+                    continue;
+                }
+                start[node] = s;
+                s += count[node];
+                qa[k++] = node;
+            } else if (node >= 0) {
+                if (s < n) sorted[s] = node;
+                ++s;
+            }
+        }
+        qcount[0] = k;
+        qcount[1] = 0;
+        qcount[2] = 0;
+    }
+    grid.sync();
+    int* in = qa;
+    int* out = qb;
+    int level = 0;
+    for (; level < 128; ++level) {
+        const int cin = min(*(volatile int*)(qcount + level % 3), cap);
+        if (cin == 0) break;  // the same value in every thread: read after the barrier
+        int* next = qcount + (level + 1) % 3;
+        if (gid == 0) qcount[(level + 2) % 3] = 0;
+        for (long long tt = gid; tt < cin; tt += gsize) {
+            const int cell = __ldcg(in + tt);
+            int s = __ldcg(start + cell);
+            int ch[4];
+            if (child16) {  // child[] 16-byte aligned: the four slots in one load
+                const int4 c4 = *reinterpret_cast<const int4*>(child + 4 * (size_t)cell);
+                ch[0] = c4.x, ch[1] = c4.y, ch[2] = c4.z, ch[3] = c4.w;
+            } else {
+#pragma unroll
+                for (int i = 0; i < 4; ++i) ch[i] = child[4 * (size_t)cell + i];
+            }
+            int cnt[4], ncell = 0;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const bool is_cell = ch[i] >= n && ch[i] < mlimit;
+                cnt[i] = is_cell ? count[ch[i]] : 0;
+                ncell += is_cell;
+            }
+            int pos = ncell ? atomicAdd(next, ncell) : 0;  // this cell's slots in the next level
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int node = ch[i];
+                if (node >= n) {
+                    if (node >= mlimit) {
+                        bad = true;
+                        continue;
+                    }
+                    start[node] = s;
+                    s += cnt[i];
+                    if (pos < cap)
+                        out[pos] = node;
+                    else
+                        bad = true;
+                    ++pos;
+                } else if (node >= 0) {
+                    if (s >= 0 && s < n)
+                        sorted[s] = node;
+                    else
+                        bad = true;
+                    ++s;
+                }
+            }
+        }
+        grid.sync();
+        int* tmp = in;
+        in = out;
+        out = tmp;
+    }
+    if (bad || (gid == 0 && level == 128)) atomicOr(status, ST_CAPACITY);
+}
+
 // warp-vote walk on the reference layout (kernels.cu:340-435)
 template <int WARPS, int STACK>
 __global__ void __launch_bounds__(WARPS * 32) k_c_forces(
@@ -797,9 +903,32 @@ void compat_SortParticles(int* count, int* start, int* sorted, int* child, int* 
         record(BH_ERR_NOMEM);
         return;
     }
-    k_c_sort<<<1, 1024, 0, g_set.stream>>>(count, start, sorted, child, n, mlimit, w->qa, w->qb,
-                                           (int)w->mcap, w->status);
-    record_cuda(cudaGetLastError(), "SortParticles");
+    // one grid over the device (cooperative: every block resident at once)
+    static int s_blocks_per_sm[kMaxDevices] = {};
+    const int dev = current_device();
+    int bps = dev >= 0 && dev < kMaxDevices ? s_blocks_per_sm[dev] : 0;
+    if (bps <= 0) {
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_c_sort_grid,
+                                                                      kSortGridThreads, 0);
+        if (e != cudaSuccess || bps < 1) bps = 0;
+        if (dev >= 0 && dev < kMaxDevices) s_blocks_per_sm[dev] = bps;
+    }
+    if (bps < 1) {  // no cooperative grid: the single block
+        k_c_sort<<<1, 1024, 0, g_set.stream>>>(count, start, sorted, child, n, mlimit, w->qa,
+                                               w->qb, (int)w->mcap, w->status);
+        record_cuda(cudaGetLastError(), "SortParticles");
+        return;
+    }
+    const int* c_count = count;
+    const int* c_child = child;
+    int cap = (int)w->mcap;
+    int child16 = (reinterpret_cast<uintptr_t>(child) & 15) == 0 ? 1 : 0;
+    void* args[] = {(void*)&c_count, (void*)&start, (void*)&sorted, (void*)&c_child, (void*)&n,
+                    (void*)&mlimit, (void*)&w->qa, (void*)&w->qb, (void*)&cap, (void*)&w->qcount,
+                    (void*)&w->status, (void*)&child16};
+    record_cuda(cudaLaunchCooperativeKernel((const void*)k_c_sort_grid, device_sms(),
+                                            kSortGridThreads, args, 0, g_set.stream),
+                "SortParticles");
 }
 
 void compat_CalculateForces(float* x, float* y, float* vx, float* vy, float* ax, float* ay, float* mass,

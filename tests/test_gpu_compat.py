@@ -203,3 +203,25 @@ def test_two_systems_alternating(L):
         final = tuple(t[:n].cpu().numpy() for t in (a.x, a.y, a.vx, a.vy))
         for v, ref in zip(final, ("x3", "y3", "vx3", "vy3")):
             assert np.max(np.abs(v - g[ref])) <= 3 * tol * np.abs(g[ref]).max(), (name, ref)
+
+
+def test_unaligned_child_array(L):
+    """child[] 4 bytes off a 16-byte boundary (a caller's sub-array): SortParticles
+    reads its slots one by one there, and the whole update() gives exactly the
+    results of an aligned child[]."""
+    g = gc.load("plummer2048")
+    n = int(g["n"])
+    outs = []
+    for offset in (0, 1):
+        a = RefArrays(g)
+        big = torch.zeros(4 * a.m + 4, dtype=torch.int32, device="cuda")
+        a.child = big[offset:offset + 4 * a.m]
+        L.bh_compat_clear_status()
+        rec = {}
+        update(L, a, float(g["dt"]), float(g["damp"]), rec)
+        assert L.bh_compat_status() == 0
+        outs.append(rec)
+    for k in ("sorted", "start", "count"):
+        assert np.array_equal(outs[0][k], outs[1][k]), k
+    assert np.array_equal(outs[0]["ax"].view(np.uint32), outs[1]["ax"].view(np.uint32))
+    assert np.array_equal(outs[0]["sorted"][:n], g["sorted"])
