@@ -617,75 +617,213 @@ __global__ void __launch_bounds__(kSortGridThreads) k_c_sort_grid(const int* cou
     if (bad || (gid == 0 && level == 128)) atomicOr(status, ST_CAPACITY);
 }
 
-// warp-vote walk on the reference layout (kernels.cu:340-435)
+// The warp-vote walk on the reference layout (kernels.cu:340-435), with the
+// engine's REFERENCE-mode machinery (k_walk_vote): lanes test up to 32 stack cells at once, each against the
+// whole group (dp <= min over the group's bodies of r_b: the group box's
+// nearest point bounds that minimum from below, the four extreme bodies from
+// above, and the exact minimum is taken only in between), accepted cells and
+// the bodies of opened cells are staged and evaluated 32 at a time with the
+// reference's arithmetic (kernels.cu:403-411).  The stack holds cells to test
+// with the dp of their level (kernels.cu:376, 395); the root's children are
+// opened without a test (kernels.cu:370-388).  Only the summation order
+// differs from the reference's.
 template <int WARPS, int STACK>
-__global__ void __launch_bounds__(WARPS * 32) k_c_forces(
+__global__ void __launch_bounds__(WARPS * 32) k_c_forces_vote(
     const float* __restrict__ x, const float* __restrict__ y, const float* __restrict__ mass,
     const int* __restrict__ sorted, const int* __restrict__ child, const float* left,
     const float* right, int n, int mlimit, float theta, float eps2, float* ax, float* ay,
     int* status) {
     __shared__ int s_node[WARPS][STACK];
     __shared__ float s_dp[WARPS][STACK];
+    __shared__ float4 s_stage[WARPS][32];
+    __shared__ int s_clist[WARPS][64];
+    __shared__ int s_blist[WARPS][32 + 4 * 32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned lt = lanemask_lt();
+    int* stack = s_node[w];
+    float* sdp = s_dp[w];
+    float4* stage = s_stage[w];
+    int* clist = s_clist[w];
+    int* blist = s_blist[w];
     const float radius = __fmul_rn(__fsub_rn(*right, *left), 0.5f);  // kernels.cu:349
     const float dp1 = __fdiv_rn(__fmul_rn(radius, radius), theta);    // :376
     const int groups = (n + 31) / 32;
     for (int g = blockIdx.x * WARPS + w; g < groups; g += gridDim.x * WARPS) {
         const int j = 32 * g + lane;
         const bool valid = j < n;
-        const int b = valid ? sorted[j] : 0;
-        const float px = valid ? x[b] : 0.0f, py = valid ? y[b] : 0.0f;
+        const int b = sorted[valid ? j : 32 * g];  // invalid lanes mirror the group's first body
+        const float px = x[b], py = y[b];
+        float gx0 = px, gx1 = px, gy0 = py, gy1 = py;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            gx0 = fminf(gx0, __shfl_xor_sync(kFull, gx0, o));
+            gx1 = fmaxf(gx1, __shfl_xor_sync(kFull, gx1, o));
+            gy0 = fminf(gy0, __shfl_xor_sync(kFull, gy0, o));
+            gy1 = fmaxf(gy1, __shfl_xor_sync(kFull, gy1, o));
+        }
+        float ext[4];  // y at min/max x, x at min/max y
+        {
+            const float key[4] = {gx0, gx1, gy0, gy1};
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const unsigned hit = __ballot_sync(kFull, (q < 2 ? px : py) == key[q]);
+                ext[q] = __shfl_sync(kFull, q < 2 ? py : px, __ffs(hit) - 1);
+            }
+        }
         float acx = 0.0f, acy = 0.0f;
-        int top = 0;
         bool bad = false;
-        auto interact = [&](int c, float dx, float dy, float r) {
-            float ri = rsqrtf(r);
-            float f = mass[c] * ri * ri * ri;
-            acx = fmaf(f, dx, acx);
-            acy = fmaf(f, dy, acy);
+        int top = 0, ccnt = 0, bcnt = 0;
+        auto interact = [&](int k) {
+            for (int e = 0; e < k; ++e) {
+                const float4 c = stage[e];
+                float dx, dy;
+                const float r = ref_r(c.x, c.y, px, py, eps2, &dx, &dy);
+                const float ri = rsqrtf(r);
+                const float f = c.z * ri * ri * ri;
+                acx = fmaf(f, dx, acx);
+                acy = fmaf(f, dy, acy);
+            }
         };
-        for (int i = 0; i < 4; ++i) {  // root children: cells always opened (:370-388)
-            int c = child[i];
-            if (c >= n && c < mlimit) {
-                if (lane == 0) {
-                    s_node[w][top] = c;
-                    s_dp[w][top] = dp1;
-                }
-                ++top;
-            } else if (c >= 0 && c < n) {
-                float dx, dy;
-                float r = ref_r(x[c], y[c], px, py, eps2, &dx, &dy);
-                interact(c, dx, dy, r);
-            }
-        }
-        while (top > 0 && !bad) {
+        auto flush_cells = [&](int k) {  // the last k entries of clist
             __syncwarp();
-            --top;
-            const int node = s_node[w][top];
-            const float dp = 0.25f * s_dp[w][top];  // :395
+            if (lane < k) {
+                const int c = clist[ccnt - k + lane];
+                stage[lane] = make_float4(x[c], y[c], mass[c], 0.0f);
+            }
+            __syncwarp();
+            interact(k);
+            ccnt -= k;
+        };
+        auto flush_bodies = [&](int k) {
+            __syncwarp();
+            if (lane < k) {
+                const int c = blist[bcnt - k + lane];
+                stage[lane] = make_float4(x[c], y[c], mass[c], 0.0f);
+            }
+            __syncwarp();
+            interact(k);
+            bcnt -= k;
+        };
+        // the root's children, opened without a test: their bodies interact,
+        // their cells' children go to the body list or the stack (dp1 / 4)
+        __syncwarp();
+        if (lane == 0) {
             for (int i = 0; i < 4; ++i) {
-                int c = child[4 * node + i];
-                if (c < 0) continue;
-                if (c >= mlimit) {
-                    bad = true;
-                    continue;
-                }
-                float dx, dy;
-                float r = ref_r(x[c], y[c], px, py, eps2, &dx, &dy);
-                if (c < n || __all_sync(kFull, !valid || dp <= r)) {
-                    interact(c, dx, dy, r);
-                } else if (top < STACK) {
-                    __syncwarp();
-                    if (lane == 0) {
-                        s_node[w][top] = c;
-                        s_dp[w][top] = dp;
+                const int c = child[i];
+                if (c >= 0 && c < n) {
+                    blist[bcnt++] = c;
+                } else if (c >= n && c < mlimit) {
+                    for (int q = 0; q < 4; ++q) {
+                        const int cc = child[4 * c + q];
+                        if (cc < 0) continue;
+                        if (cc >= mlimit) {
+                            bad = true;
+                        } else if (cc < n) {
+                            blist[bcnt++] = cc;
+                        } else {
+                            stack[top] = cc;
+                            sdp[top] = 0.25f * dp1;  // :395
+                            ++top;
+                        }
                     }
-                    ++top;
-                } else {
-                    bad = true;
                 }
             }
         }
+        top = __shfl_sync(kFull, top, 0);
+        bcnt = __shfl_sync(kFull, bcnt, 0);
+        bad = __shfl_sync(kFull, bad ? 1 : 0, 0) != 0;
+        __syncwarp();
+        int rounds = 0;
+        while (top > 0 && !bad) {
+            if (++rounds > kMaxWalkRounds) {  // far beyond any valid tree (a cycle in child[])
+                bad = true;
+                break;
+            }
+            int k = min(32, top);
+            if (top + 3 * k > STACK) {  // pop k, push <= 4k
+                k = max((STACK - top) / 3, 0);
+                if (k == 0) {
+                    bad = true;
+                    break;
+                }
+            }
+            __syncwarp();
+            const int node = lane < k ? stack[top - 1 - lane] : -1;
+            const float dp = lane < k ? sdp[top - 1 - lane] : 0.0f;
+            top -= k;
+            float cx = 0.0f, cy = 0.0f;
+            bool acc = false, need = false;
+            if (node >= 0) {
+                cx = x[node];
+                cy = y[node];
+                // lower bound of min_b r_b: the box's nearest point
+                const float nx = fminf(fmaxf(cx, gx0), gx1), ny = fminf(fmaxf(cy, gy0), gy1);
+                if (dp <= ref_r_only(cx, cy, nx, ny, eps2)) {
+                    acc = true;
+                } else {
+                    float rhi = ref_r_only(cx, cy, gx0, ext[0], eps2);
+                    rhi = fminf(rhi, ref_r_only(cx, cy, gx1, ext[1], eps2));
+                    rhi = fminf(rhi, ref_r_only(cx, cy, ext[2], gy0, eps2));
+                    rhi = fminf(rhi, ref_r_only(cx, cy, ext[3], gy1, eps2));
+                    need = dp <= rhi;
+                }
+            }
+            unsigned nm = __ballot_sync(kFull, need);
+            while (nm) {  // the exact minimum over the group's bodies, one cell at a time
+                const int src = __ffs(nm) - 1;
+                nm &= nm - 1;
+                const float sx = __shfl_sync(kFull, cx, src), sy = __shfl_sync(kFull, cy, src);
+                float r = ref_r_only(sx, sy, px, py, eps2);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) r = fminf(r, __shfl_xor_sync(kFull, r, o));
+                if (lane == src) acc = dp <= r;
+            }
+            const unsigned mc = __ballot_sync(kFull, acc);
+            if (acc) clist[ccnt + __popc(mc & lt)] = node;
+            ccnt += __popc(mc);
+            const bool open = node >= 0 && !acc;
+            int cs[4] = {-1, -1, -1, -1};
+            if (open)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) cs[q] = child[4 * node + q];
+            int nb = 0, nn = 0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (cs[q] >= mlimit) {
+                    bad = true;
+                    cs[q] = -1;
+                }
+                nb += (cs[q] >= 0 && cs[q] < n);
+                nn += (cs[q] >= n);
+            }
+            int tot;
+            const int off = warp_excl_scan(nb | (nn << 16), &tot);
+            __syncwarp();  // every lane has read its stack slot before children overwrite it
+            if (open) {
+                int* bw = blist + bcnt + (off & 0xffff);
+                int* nw = stack + top + (off >> 16);
+                float* dw = sdp + top + (off >> 16);
+                const float cdp = 0.25f * dp;  // :395
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (cs[q] < 0) continue;
+                    if (cs[q] < n) {
+                        *bw++ = cs[q];  // bodies always interact (:395-399)
+                    } else {
+                        *nw++ = cs[q];
+                        *dw++ = cdp;
+                    }
+                }
+            }
+            bcnt += tot & 0xffff;
+            top += tot >> 16;
+            bad = __any_sync(kFull, bad);
+            __syncwarp();
+            while (ccnt >= 32) flush_cells(32);
+            while (bcnt >= 32) flush_bodies(32);
+        }
+        if (ccnt > 0) flush_cells(ccnt);
+        if (bcnt > 0) flush_bodies(bcnt);
         if (bad && lane == 0) atomicOr(status, ST_STACK);
         if (valid) {
             ax[b] = acx;  // :428-429
@@ -946,12 +1084,12 @@ void compat_CalculateForces(float* x, float* y, float* vx, float* vy, float* ax,
         record(BH_ERR_NOMEM);
         return;
     }
-    constexpr int W = 8, S = 256;
+    constexpr int W = 4, S = 1024;
     // a grid-stride loop over the warp groups: at most 16 blocks per SM
     int blocks = std::min(blocks_for((n + 31) / 32, W), 16 * device_sms());
-    k_c_forces<W, S><<<blocks, W * 32, 0, g_set.stream>>>(x, y, mass, sorted, child, left, right, n,
-                                                        mlimit, g_set.theta, g_set.eps2, ax, ay,
-                                                        w->status);
+    k_c_forces_vote<W, S><<<blocks, W * 32, 0, g_set.stream>>>(x, y, mass, sorted, child, left,
+                                                             right, n, mlimit, g_set.theta,
+                                                             g_set.eps2, ax, ay, w->status);
     record_cuda(cudaGetLastError(), "CalculateForces");
 }
 
