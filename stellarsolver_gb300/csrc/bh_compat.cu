@@ -567,15 +567,31 @@ __global__ void __launch_bounds__(kSortGridThreads) k_c_sort_grid(const int* cou
         int* next = qcount + (level + 1) % 3;
         if (gid == 0) qcount[(level + 2) % 3] = 0;
         for (long long tt = gid; tt < cin; tt += gsize) {
-            const int cell = __ldcg(in + tt);
+            int cell = __ldcg(in + tt);
             int s = __ldcg(start + cell);
             int ch[4];
-            if (child16) {  // child[] 16-byte aligned: the four slots in one load
-                const int4 c4 = *reinterpret_cast<const int4*>(child + 4 * (size_t)cell);
-                ch[0] = c4.x, ch[1] = c4.y, ch[2] = c4.z, ch[3] = c4.w;
-            } else {
+            // a cell whose only child is a cell (the chains of the uncompressed
+            // tree) gives that child its own start: followed down in this
+            // thread, not level by level
+            for (int chain = 0;; ++chain) {
+                if (child16) {  // child[] 16-byte aligned: the four slots in one load
+                    const int4 c4 = *reinterpret_cast<const int4*>(child + 4 * (size_t)cell);
+                    ch[0] = c4.x, ch[1] = c4.y, ch[2] = c4.z, ch[3] = c4.w;
+                } else {
 #pragma unroll
-                for (int i = 0; i < 4; ++i) ch[i] = child[4 * (size_t)cell + i];
+                    for (int i = 0; i < 4; ++i) ch[i] = child[4 * (size_t)cell + i];
+                }
+                int only = -1, used = 0;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    if (ch[i] >= 0) {
+                        only = ch[i];
+                        ++used;
+                    }
+                }
+                if (used != 1 || only < n || only >= mlimit || chain == 128) break;
+                start[only] = s;
+                cell = only;
             }
             int cnt[4], ncell = 0;
 #pragma unroll
@@ -874,17 +890,25 @@ cudaError_t enqueue_build(Workspace& w, float* x, float* y, float* mass, int* co
     const int nb = blocks_for(n, 256);
     k_c_box_to_ord<<<1, 1, 0, st>>>(left, right, bottom, top, w.box_ord, w.seg_off, n);
     Segs segs{1, w.seg_off, nullptr};
-    k_keys<<<nb, 256, 0, st>>>(x, y, n, segs, w.box_ord, w.keys, w.vals);
     e = cudaMemsetAsync(w.overflow, 0, sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    // the kernels that wait for their predecessor (pdl_wait) are launched with
+    // programmatic serialisation: each one's launch overlaps the previous one's
+    // tail, which matters for the flag-gated full sort that returns at once
+    e = launch_pdl(k_keys, nb, 256, 0, st, x, y, n, segs, (const int*)w.box_ord, w.keys, w.vals);
     if (e != cudaSuccess) return e;
     const int tiles = (n + kSortTile - 1) / kSortTile;
     auto pass = [&](const uint64_t* ki, const uint32_t* vi, uint64_t* ko, uint32_t* vo, int shift,
                     const int* only_if) {
-        k_radix_hist<<<tiles, kSortThreads, 0, st>>>(ki, vi, n, shift, 0, nullptr, w.hist, tiles,
-                                                     only_if);
-        k_radix_scan<<<256, kSortThreads, 0, st>>>(w.hist, tiles, w.totals, only_if);
-        k_radix_scatter<<<tiles, kSortThreads, 0, st>>>(ki, vi, ko, vo, n, shift, 0, nullptr,
-                                                        w.hist, w.totals, tiles, only_if);
+        cudaError_t r = launch_pdl(k_radix_hist, tiles, kSortThreads, 0, st, ki, vi, n, shift, 0,
+                                   (const int*)nullptr, w.hist, tiles, only_if);
+        if (r == cudaSuccess)
+            r = launch_pdl(k_radix_scan, 256, kSortThreads, 0, st, w.hist, tiles, w.totals, only_if);
+        if (r == cudaSuccess)
+            r = launch_pdl(k_radix_scatter, tiles, kSortThreads, 0, st, ki, vi, ko, vo, n, shift, 0,
+                           (const int*)nullptr, (const uint32_t*)w.hist, (const uint32_t*)w.totals,
+                           tiles, only_if);
+        return r;
     };
     // high word: keys -> ... -> keys3, the fixup into keys_alt; the full sort
     // (if flagged) keys -> keys3 / keys_alt alternately -> keys_alt
@@ -896,20 +920,24 @@ cudaError_t enqueue_build(Workspace& w, float* x, float* y, float* mass, int* co
             const bool to_alt = ((hp - 1 - ps) & 1) != 0;
             uint64_t* ko = to_alt ? w.keys_alt : w.keys3;
             uint32_t* vo = to_alt ? w.vals_alt : w.vals3;
-            pass(ki, vi, ko, vo, 64 - 8 * (hp - ps), nullptr);
+            e = pass(ki, vi, ko, vo, 64 - 8 * (hp - ps), nullptr);
+            if (e != cudaSuccess) return e;
             ki = ko;
             vi = vo;
         }
     }
-    k_sort_fixup<<<nb, 256, 0, st>>>(n, 64 - 8 * hp, w.keys3, w.vals3, w.keys_alt, w.vals_alt,
-                                     w.overflow, (cudaGraphConditionalHandle)0, 0, nullptr, 0);
+    e = launch_pdl(k_sort_fixup, nb, 256, 0, st, n, 64 - 8 * hp, (const uint64_t*)w.keys3,
+                   (const uint32_t*)w.vals3, w.keys_alt, w.vals_alt, w.overflow,
+                   (cudaGraphConditionalHandle)0, 0, (int*)nullptr, 0);
+    if (e != cudaSuccess) return e;
     {
         const uint64_t* ki = w.keys;
         const uint32_t* vi = w.vals;
         for (int ps = 0; ps < 8; ++ps) {
             uint64_t* ko = (ps & 1) ? w.keys_alt : w.keys3;
             uint32_t* vo = (ps & 1) ? w.vals_alt : w.vals3;
-            pass(ki, vi, ko, vo, 8 * ps, w.overflow);
+            e = pass(ki, vi, ko, vo, 8 * ps, w.overflow);
+            if (e != cudaSuccess) return e;
             ki = ko;
             vi = vo;
         }
@@ -917,9 +945,13 @@ cudaError_t enqueue_build(Workspace& w, float* x, float* y, float* mass, int* co
     uint64_t* ka = w.keys_alt;
     uint32_t* va = w.vals_alt;
     k_c_gather3<<<nb, 256, 0, st>>>(n, va, x, y, mass, w.sx, w.sy, w.sm);
-    k_build<<<nb, 256, 0, st>>>(ka, n, segs, w.tree, w.status);
-    k_moments<<<(n + kMomentsThreads - 1) / kMomentsThreads, kMomentsThreads, 0, st>>>(
-        n, 0, w.sx, w.sy, w.sm, w.tree.climb, w.tree.leaf_parent, w.counter, w.sums, w.status);
+    e = launch_pdl(k_build, nb, 256, 0, st, (const uint64_t*)ka, n, segs, w.tree, w.status);
+    if (e == cudaSuccess)
+        e = launch_pdl(k_moments, (n + kMomentsThreads - 1) / kMomentsThreads, kMomentsThreads, 0,
+                       st, n, 0, (const float*)w.sx, (const float*)w.sy, (const float*)w.sm,
+                       (const int4*)w.tree.climb, (const int*)w.tree.leaf_parent, w.counter, w.sums,
+                       w.status);
+    if (e != cudaSuccess) return e;
     k_c_ncells<<<nb, 256, 0, st>>>(n, w.tree.split, w.tree.parent, w.ncell);
     const int sb = blocks_for(n, 1024);
     k_c_scan_block<<<sb, 1024, 0, st>>>(w.ncell, w.cbase, w.bsum, n);

@@ -82,36 +82,6 @@ T* carve(char*& cur, size_t count) {
     return p;
 }
 
-// Launch with programmatic stream serialisation: the kernel may begin while the
-// previous kernel on the stream drains (it calls pdl_wait before reading).
-template <typename... KArgs, typename... Args>
-cudaError_t launch_pdl(void (*kernel)(KArgs...), int grid, int block, size_t smem,
-                       cudaStream_t st, Args... args) {
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(block);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
-}
-
-// The same launch without the attribute (the body of a conditional graph node).
-template <typename... KArgs, typename... Args>
-cudaError_t launch_plain(void (*kernel)(KArgs...), int grid, int block, size_t smem,
-                         cudaStream_t st, Args... args) {
-    cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(block);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
-}
-
 template <typename T>
 size_t span(size_t count) {
     return (sizeof(T) * count + 255) & ~size_t(255);
