@@ -225,3 +225,40 @@ def test_unaligned_child_array(L):
         assert np.array_equal(outs[0][k], outs[1][k]), k
     assert np.array_equal(outs[0]["ax"].view(np.uint32), outs[1]["ax"].view(np.uint32))
     assert np.array_equal(outs[0]["sorted"][:n], g["sorted"])
+
+
+@pytest.mark.parametrize("n", [1 << 17, (1 << 18) + 333])
+def test_dropin_update_matches_reference_mode(L, n):
+    """The drop-in update() (reference layout, cooperative-grid SortParticles,
+    batched warp-vote CalculateForces) against the engine's REFERENCE mode on
+    the same Plummer state, two independent paths to the reference's step:
+    sorted[] equals the engine's permutation (both are the bodies in key
+    order), the forces agree to 1e-5 of their RMS (the same interaction set,
+    summed in another order), and the integrated positions to 1e-5 of their
+    extent."""
+    from stellarsolver_gb300 import bh, dropin, models
+
+    x, y, vx, vy, m = models.plummer(n, 0x5EEDC0DE)
+    eps2, dt = 1e-4, 1e-4
+    L.bh_compat_set_constants(0.5, eps2)
+    L.bh_compat_clear_status()
+    a = dropin.RefArrays(torch, x, y, vx, vy, m)
+    dropin.update(L, a, dt, 1.0)
+    torch.cuda.synchronize()
+    assert L.bh_compat_status() == 0
+    L.bh_compat_set_constants(0.5, 0.025)  # the fixtures' constants, for the other tests
+    sorted_ = a.sorted[:n].cpu().numpy()
+    dax, day = a.ax[:n].cpu().numpy(), a.ay[:n].cpu().numpy()
+    dx1, dy1 = a.x[:n].cpu().numpy(), a.y[:n].cpu().numpy()
+    with bh.BarnesHutSystem(n, mode="reference", theta=0.5, eps2=eps2, timestep=dt) as s:
+        s.set_state(x, y, vx, vy, m)
+        s.step(1)
+        s.sync()
+        perm = s.debug("perm")
+        eax, eay = s.get_accel()
+        st = s.get_state()
+    assert np.array_equal(sorted_, perm)
+    r = np.sqrt(np.mean(eax.astype(np.float64) ** 2 + eay.astype(np.float64) ** 2))
+    assert np.hypot(dax - eax, day - eay).max() <= 1e-5 * r
+    ext = max(np.ptp(x), np.ptp(y))
+    assert max(np.abs(dx1 - st["x"]).max(), np.abs(dy1 - st["y"]).max()) <= 1e-5 * ext
