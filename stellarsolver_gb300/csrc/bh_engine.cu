@@ -1712,9 +1712,30 @@ int bh_autotune(bh_system* s, void* stream, bh_params* chosen) {
     RC(join_inputs(s, (cudaStream_t)stream));
     cudaStream_t st = (cudaStream_t)stream;
     const size_t N = (size_t)s->n;
+    // scratch of this call, released on every way out; an early return (a
+    // CUDA error) also puts back the parameters and the sort's pass count
+    struct Scratch {
+        bh_system* s;
+        bh_params p;
+        int passes;
+        float* bk = nullptr;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        bool done = false;
+        ~Scratch() {
+            if (bk) cudaFree(bk);
+            if (e0) cudaEventDestroy(e0);
+            if (e1) cudaEventDestroy(e1);
+            if (!done) {
+                s->p = p;
+                s->high_passes = passes;
+                s->box_valid = false;
+                drop_graph(s);
+            }
+        }
+    } sc{s, s->p, s->high_passes};
     // back up the state the candidates will all start from
-    float* bk = nullptr;
-    CK(cudaMalloc(&bk, N * 9 * sizeof(float) + sizeof(int)));
+    CK(cudaMalloc(&sc.bk, N * 9 * sizeof(float) + sizeof(int)));
+    float* bk = sc.bk;
     BodyPtrs& c = s->st[0];
     float* arrs[8] = {c.x, c.y, c.vx, c.vy, c.m, c.xlo, c.ylo, c.amag};
     const bool orig_fresh = s->fresh_host;
@@ -1754,11 +1775,11 @@ int bh_autotune(bh_system* s, void* stream, bh_params* chosen) {
         const int blocks[2] = {128, 256};
         const int buckets[3] = {4, 8, 16};
         const int bpls[2] = {1, 2};
-        cudaEvent_t e0 = nullptr, e1 = nullptr;
         if (rc == BH_OK) {
-            CK(cudaEventCreate(&e0));
-            CK(cudaEventCreate(&e1));
+            CK(cudaEventCreate(&sc.e0));
+            CK(cudaEventCreate(&sc.e1));
         }
+        cudaEvent_t e0 = sc.e0, e1 = sc.e1;
         // one candidate from the saved state: a warm-up step (with the box
         // kernel and, if fresh, the bootstrap), then `steps` timed steps; ms per
         // step, +inf if a step reported an error
@@ -1831,12 +1852,10 @@ int bh_autotune(bh_system* s, void* stream, bh_params* chosen) {
             const float keep = pass_ms[size_rule - 3], other = pass_ms[4 - size_rule];
             if (other < 0.99f * keep) s->high_passes = 7 - size_rule;
         }
-        if (e0) cudaEventDestroy(e0);
-        if (e1) cudaEventDestroy(e1);
     }
     if (rc == BH_OK) rc = restore();
     if (rc == BH_OK) CK(cudaStreamSynchronize(st));
-    cudaFree(bk);
+    sc.done = true;
     best.use_graph = orig.use_graph;
     s->p = rc == BH_OK ? best : orig;
     s->caller_order = orig_caller;
