@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 #include <memory>
@@ -1074,9 +1075,9 @@ void compat_SortParticles(int* count, int* start, int* sorted, int* child, int* 
         return;
     }
     // one grid over the device (cooperative: every block resident at once)
-    static int s_blocks_per_sm[kMaxDevices] = {};
+    static std::atomic<int> s_blocks_per_sm[kMaxDevices] = {};  // per device, read once
     const int dev = current_device();
-    int bps = dev >= 0 && dev < kMaxDevices ? s_blocks_per_sm[dev] : 0;
+    int bps = dev >= 0 && dev < kMaxDevices ? s_blocks_per_sm[dev].load() : 0;
     if (bps <= 0) {
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_c_sort_grid,
                                                                       kSortGridThreads, 0);
