@@ -73,6 +73,8 @@ constexpr int kStepZero = 4 + 6;
 enum StepPart { kStepAll = 0, kStepPre = 1, kStepPost = 2 };
 constexpr int kGraphs = 6;
 constexpr int kGraphCarried = 5;  // a whole step on the box carried from the last walk
+constexpr int kTrialSteps = 8;                     // bh_autotune: timed steps per run at most
+constexpr size_t kTrialFlushBytes = 256ull << 20;  // bh_autotune: written before each timed step
 
 template <typename T>
 T* carve(char*& cur, size_t count) {
@@ -1719,12 +1721,14 @@ int bh_autotune(bh_system* s, void* stream, bh_params* chosen) {
         bh_params p;
         int passes;
         float* bk = nullptr;
-        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        void* flush = nullptr;  // written before every timed step: larger than L2
+        cudaEvent_t ev[2 * kTrialSteps] = {};
         bool done = false;
         ~Scratch() {
             if (bk) cudaFree(bk);
-            if (e0) cudaEventDestroy(e0);
-            if (e1) cudaEventDestroy(e1);
+            if (flush) cudaFree(flush);
+            for (cudaEvent_t e : ev)
+                if (e) cudaEventDestroy(e);
             if (!done) {
                 s->p = p;
                 s->high_passes = passes;
@@ -1735,6 +1739,10 @@ int bh_autotune(bh_system* s, void* stream, bh_params* chosen) {
     } sc{s, s->p, s->high_passes};
     // back up the state the candidates will all start from
     CK(cudaMalloc(&sc.bk, N * 9 * sizeof(float) + sizeof(int)));
+    if (cudaMalloc(&sc.flush, kTrialFlushBytes) != cudaSuccess) {  // optional: no flush then
+        sc.flush = nullptr;
+        cudaGetLastError();
+    }
     float* bk = sc.bk;
     BodyPtrs& c = s->st[0];
     float* arrs[8] = {c.x, c.y, c.vx, c.vy, c.m, c.xlo, c.ylo, c.amag};
@@ -1775,14 +1783,13 @@ int bh_autotune(bh_system* s, void* stream, bh_params* chosen) {
         const int blocks[2] = {128, 256};
         const int buckets[3] = {4, 8, 16};
         const int bpls[2] = {1, 2};
-        if (rc == BH_OK) {
-            CK(cudaEventCreate(&sc.e0));
-            CK(cudaEventCreate(&sc.e1));
-        }
-        cudaEvent_t e0 = sc.e0, e1 = sc.e1;
+        if (rc == BH_OK)
+            for (cudaEvent_t& e : sc.ev) CK(cudaEventCreate(&e));
         // one candidate from the saved state: a warm-up step (with the box
-        // kernel and, if fresh, the bootstrap), then `steps` timed steps; ms per
-        // step, +inf if a step reported an error
+        // kernel and, if fresh, the bootstrap), then `steps` timed steps, each
+        // after a write larger than L2 (a step's working set does not stay in
+        // L2 from one step to the next at the sizes where the shapes differ);
+        // ms per step, +inf if a step reported an error
         auto trial = [&](const bh_params& cand, int passes, int steps, float* ms) -> int {
             s->p = cand;
             s->p.use_graph = 0;
@@ -1791,21 +1798,29 @@ int bh_autotune(bh_system* s, void* stream, bh_params* chosen) {
             int r = restore();
             if (r == BH_OK) r = enqueue_step(s, st);
             if (r != BH_OK) return r;
-            CK(cudaEventRecord(e0, st));
-            for (int k = 0; k < steps && r == BH_OK; ++k) r = enqueue_step(s, st);
+            steps = std::min(steps, kTrialSteps);
+            for (int k = 0; k < steps && r == BH_OK; ++k) {
+                if (sc.flush) CK(cudaMemsetAsync(sc.flush, k, kTrialFlushBytes, st));
+                CK(cudaEventRecord(sc.ev[2 * k], st));
+                r = enqueue_step(s, st);
+                CK(cudaEventRecord(sc.ev[2 * k + 1], st));
+            }
             if (r != BH_OK) return r;
-            CK(cudaEventRecord(e1, st));
-            CK(cudaEventSynchronize(e1));
+            CK(cudaEventSynchronize(sc.ev[2 * steps - 1]));
             float t = 0.f;
-            CK(cudaEventElapsedTime(&t, e0, e1));
+            for (int k = 0; k < steps; ++k) {
+                float tk = 0.f;
+                CK(cudaEventElapsedTime(&tk, sc.ev[2 * k], sc.ev[2 * k + 1]));
+                t += tk;
+            }
             int bits = 0;
             CK(cudaMemcpy(&bits, s->status, sizeof(int), cudaMemcpyDeviceToHost));
             *ms = status_code(bits, cand.mode) == BH_OK ? t / (float)steps : 1e30f;
             return BH_OK;
         };
-        // every shape for 3 steps, then the best three again, twice for 6 steps
-        // each in turn, by their faster run: candidates within a few per cent
-        // of one another are told apart by more than two steps
+        // every shape for 3 steps, then the best three again, three times for 8
+        // steps each in turn, by their fastest run: candidates within a few per
+        // cent of one another are told apart by more than two steps
         const int size_rule = s->high_passes;
         std::vector<std::pair<float, bh_params>> cands;
         for (int li = 0; li < 2 && rc == BH_OK; ++li)
@@ -1825,10 +1840,10 @@ int bh_autotune(bh_system* s, void* stream, bh_params* chosen) {
                              [](const auto& a, const auto& b) { return a.first < b.first; });
             const int top = std::min<int>(3, (int)cands.size());
             std::vector<float> again(top, 1e30f);
-            for (int round = 0; round < 2 && rc == BH_OK; ++round)
+            for (int round = 0; round < 3 && rc == BH_OK; ++round)
                 for (int q = 0; q < top && rc == BH_OK; ++q) {
                     float ms = 1e30f;
-                    rc = trial(cands[q].second, size_rule, 6, &ms);
+                    rc = trial(cands[q].second, size_rule, kTrialSteps, &ms);
                     again[q] = std::min(again[q], ms);
                 }
             int bq = 0;
@@ -1844,7 +1859,7 @@ int bh_autotune(bh_system* s, void* stream, bh_params* chosen) {
         for (int round = 0; round < 2 && rc == BH_OK; ++round)
             for (int hp = 3; hp <= 4 && rc == BH_OK; ++hp) {
                 float ms = 1e30f;
-                rc = trial(best, hp, 6, &ms);
+                rc = trial(best, hp, kTrialSteps, &ms);
                 pass_ms[hp - 3] = std::min(pass_ms[hp - 3], ms);
             }
         s->high_passes = size_rule;
