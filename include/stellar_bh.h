@@ -37,7 +37,8 @@ extern "C" {
 #define BH_ERR_NO_DEVICE 9      /* no CUDA device, or not an sm_103 device */
 #define BH_ERR_TREE 10          /* a traversal exceeded its bound: the tree is not a valid
                                    tree of the keys (never for a valid build; reported
-                                   instead of looping) */
+                                   instead of looping), or a bounded wait of the walk's
+                                   shared groups ran out */
 
 /* ---------------------------------------------------------------- modes */
 /* REFERENCE: the reference's force law and opening rule, bit-for-bit tree:
@@ -75,6 +76,12 @@ typedef struct bh_params {
                           (Springel 2005-style); 0 = geometric rule only; default 0.01 */
     int bodies_per_lane; /* PLAIN/MIXED walk: a warp walks the tree once for 32 (1) or 64 (2)
                             consecutive bodies; 0 = tuned default */
+    int share_tail;      /* PLAIN/MIXED walk, shared groups: the owner of a shared walk group
+                            walks the tree, warps between groups evaluate its interactions.
+                            Results are bit-identical with or without sharing.  k > 0: the
+                            heavy groups and the last k groups handed out; 0 = default: the
+                            heavy groups when the walk has no more groups than the GPU has
+                            resident walk warps (about 2^17 bodies on GB300); -1 = none */
 } bh_params;
 
 typedef struct bh_system bh_system;
@@ -201,7 +208,9 @@ int bh_check(bh_system* s, void* stream, unsigned* failed);
  *   sorted position), "node_left" "node_right" "node_split" "node_first"
  *   "node_last" "node_parent" i32[n], "node_m" "node_mx" "node_my" "node_cx"
  *   "node_cy" f32[n] (node arrays have n entries; entry n-1 is unused),
- *   "accel_sorted" f32[2n] (ax then ay).
+ *   "accel_sorted" f32[2n] (ax then ay), "share" i32[4] (the last walk's shared
+ *   groups: slices handed out from the queue, slices reserved, pool batches
+ *   reserved, slices taken back by their owners).
  * Returns BH_ERR_ARG for an unknown name or a too small buffer. */
 int bh_get_debug(bh_system* s, const char* name, void* host_out, size_t bytes, void* stream);
 

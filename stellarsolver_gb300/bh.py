@@ -43,7 +43,7 @@ class Params(ctypes.Structure):
                 ("dampening", ctypes.c_float), ("leaf_bucket", ctypes.c_int),
                 ("block_size", ctypes.c_int), ("stack_depth", ctypes.c_int),
                 ("use_graph", ctypes.c_int), ("alpha", ctypes.c_float),
-                ("bodies_per_lane", ctypes.c_int)]
+                ("bodies_per_lane", ctypes.c_int), ("share_tail", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -166,7 +166,7 @@ def measure_fp32_peaks(device: int = -1) -> dict:
 
 def make_params(mode="reference", theta=0.5, eps2=0.025, gravity=1.0, timestep=1e-3,
                 dampening=1.0, leaf_bucket=0, use_graph=False, stack_depth=0,
-                block_size=0, alpha=0.01, bodies_per_lane=0) -> Params:
+                block_size=0, alpha=0.01, bodies_per_lane=0, share_tail=0) -> Params:
     p = Params()
     lib().bh_default_params(ctypes.byref(p))
     p.mode = MODES[mode] if isinstance(mode, str) else int(mode)
@@ -176,6 +176,7 @@ def make_params(mode="reference", theta=0.5, eps2=0.025, gravity=1.0, timestep=1
     p.stack_depth, p.block_size = int(stack_depth), int(block_size)
     p.alpha = alpha
     p.bodies_per_lane = int(bodies_per_lane)
+    p.share_tail = int(share_tail)
     return p
 
 
@@ -357,7 +358,7 @@ class BarnesHutSystem:
         n = self.n
         spec = {"box": (np.float32, 4), "boxes": (np.float32, 4 * self.num_systems),
                 "keys": (np.uint64, n), "perm": (np.int32, n),
-                "accel_sorted": (np.float32, 2 * n)}
+                "accel_sorted": (np.float32, 2 * n), "share": (np.int32, 4)}
         dt, cnt = spec.get(name, (np.float32 if name in ("node_m", "node_mx", "node_my",
                                                           "node_cx", "node_cy") else np.int32, n))
         out = np.empty(cnt, dt)

@@ -281,8 +281,10 @@ static __global__ void k_keys(const float* __restrict__ x, const float* __restri
 }
 
 // k_keys for the engine's step: also clears the moments arrival counters of
-// these positions, the two per-step flags (flags[0..1]) and (block 0) the
-// step's first `nzero` scheduling and statistics words.  With nzero > 0 (a
+// these positions, the per-step flags (flags[0..nflags)), the first `nstates`
+// words of the walk's shared-group counters and slice states (nstates <= the
+// grid's threads) and (block 0) the step's first `nzero` scheduling and
+// statistics words.  With nzero > 0 (a
 // step, not the energy pass) each system's walk cost of the last step
 // (seg_cost, entries x bodies) becomes its mean walk-group cost (mean_cost)
 // and is cleared.  box_copy (non-null when the box was carried from the last
@@ -291,13 +293,18 @@ static __global__ void k_keys_step(const float* __restrict__ x, const float* __r
                                    Segs segs, const int* __restrict__ box_ord,
                                    uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
                                    int* __restrict__ counter, int* __restrict__ zero, int nzero,
-                                   int* __restrict__ flags,
+                                   int* __restrict__ flags, int nflags,
+                                   int* __restrict__ states, int nstates,
                                    unsigned long long* __restrict__ seg_cost,
                                    int* __restrict__ mean_cost, int* __restrict__ box_copy) {
     pdl_wait();
+    {
+        const int t = blockIdx.x * blockDim.x + threadIdx.x;
+        if (t < nstates) states[t] = 0;
+    }
     if (blockIdx.x == 0) {
         if (threadIdx.x < nzero) zero[threadIdx.x] = 0;
-        if (threadIdx.x < 2) flags[threadIdx.x] = 0;
+        if (threadIdx.x < nflags) flags[threadIdx.x] = 0;
         if (box_copy)
             for (int w = threadIdx.x; w < 4 * segs.nseg; w += blockDim.x) box_copy[w] = box_ord[w];
     }

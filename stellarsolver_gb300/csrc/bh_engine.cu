@@ -50,9 +50,8 @@ constexpr int kMaxStack = 2048;
 constexpr int kDefaultBucket = 8;
 constexpr int kDefaultBpl = 1;  // bodies per lane of the accuracy walk
 constexpr int kMaxBucket = 32;
-// worst case: 8 warps x (staging + 2048-entry stack + 32-body buckets)
-constexpr int kMaxWalkSmem = 8 * (3 * 32 * 16 + 32 * 8 * 2 + 16 + 64 * 4 + kMaxStack * 4 +
-                                  (32 + 32 * kMaxBucket) * 4);
+// worst case: 8 warps x (staging + 2048-entry stack + 32-body buckets + slice list)
+constexpr int kMaxWalkSmem = 8 * acc_warp_bytes(AccShape{kMaxStack, kMaxBucket, 2}, true);
 constexpr int kBboxThreads = 256;
 constexpr int kBboxChunk = 2048;
 
@@ -61,12 +60,17 @@ int walk_grid_cap(int device_sms, int blocks_per_sm) { return device_sms * std::
 // Per-step words: 2 x u64 interaction counts, then bh_system::work (11 ints):
 //   work[0..2] walk scheduling, [3..5] walk statistics, [6..8] the energy pass,
 //   [9] the sort's run overflow flag, [10] heavy walk groups listed.
-// A step's key kernel clears the counts and work[0..5] (kStepZero words) and
-// the two flags; the energy pass's tree build clears only the flags.
+// A step's key kernel clears the counts and work[0..5] (kStepZero words), the
+// two flags, and the shared walk groups' counters and slice states; the
+// energy pass's tree build clears all but the counts and work[0..5].
 constexpr int kStepWords = 16;
 constexpr int kWorkSortOverflow = 9;
 constexpr int kWorkHeavy = 10;
+constexpr int kStepFlags = 2;
 constexpr int kStepZero = 4 + 6;
+// Shared walk groups: pool batches per body (a quarter of the worst case of
+// one batch per 32 interactions of every body), slices at most one per two batches.
+constexpr int kShareBatchDiv = 4;
 
 // Parts of a step: all of it, or split after the sort (bh_step joins the input
 // copies of bh_set_state in between).
@@ -110,6 +114,12 @@ static cudaError_t walk_attributes(int bytes) {
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_walk_acc<false, true, false, BPL>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_walk_acc<false, false, false, BPL, true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_walk_acc<true, false, false, BPL, true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
     return e;
 }
 
@@ -137,12 +147,23 @@ static cudaError_t launch_acc(const StepArgs& a, cudaStream_t st, int part) {
         return launch_pdl(k_walk_acc<false, true, false, 2>, gb, warps * 32, smb, st, sb, a.segs,
                           a.groups2, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt,
                           a.ddt, a.alpha, a.out, a.status, a.inter, a.work + 1, a.fresh,
-                          a.max_stack, (double*)nullptr, Frontier{}, Heavy{});
+                          a.max_stack, (double*)nullptr, Frontier{}, Heavy{}, Share{});
+    } else if (a.share.ctr) {
+        // shared groups; the pool holds sums for one or two bodies per lane: half
+        // the batches with two
+        Share shr = a.share;
+        shr.cap_batches /= BPL;
+        shr.cap_slices = std::min(shr.cap_slices, shr.cap_batches);
+        return launch_pdl(k_walk_acc<MIXED, false, false, BPL, true>, grid, warps * 32,
+                          (size_t)warps * acc_warp_bytes(sh, true), st, sh, a.segs, gr, a.in,
+                          a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt, a.alpha,
+                          a.out, a.status, a.inter, a.work + 2, a.fresh, a.max_stack,
+                          (double*)nullptr, a.frontier, a.heavy, shr);
     } else {
         return launch_pdl(k_walk_acc<MIXED, false, false, BPL>, grid, warps * 32, smem, st, sh,
                           a.segs, gr, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt,
                           a.ddt, a.alpha, a.out, a.status, a.inter, a.work + 2, a.fresh,
-                          a.max_stack, (double*)nullptr, a.frontier, a.heavy);
+                          a.max_stack, (double*)nullptr, a.frontier, a.heavy, Share{});
     }
 }
 
@@ -216,6 +237,14 @@ struct bh_system {
     int* fresh = nullptr;  // 1 after bh_set_state: bootstrap |a_old| in the next step
     int* flist = nullptr;   // walk frontiers, kFrontierCap per super-group
     int* heavy = nullptr;   // heavy walk groups of the step (k_frontier)
+    // shared walk groups: the batch pool (entries, and sums for one body per
+    // lane: half as many batches with two) and the slice table
+    int* share_idx = nullptr;
+    float2* share_sum = nullptr;
+    int* share_ctr = nullptr;    // [kCtrWords] counters, then the slice states
+    int* share_state = nullptr;
+    int4* share_desc = nullptr;
+    int share_batches = 0, share_slices = 0;
     unsigned long long* seg_cost = nullptr;  // [nseg] walk cost of each system, this step
     int* mean_cost = nullptr;                // [nseg] mean walk-group cost, last step
     int2* fcount = nullptr;  // per super-group: (nodes to test, accepted cells); -1: the root
@@ -225,6 +254,7 @@ struct bh_system {
     int high_passes = 4;  // radix passes of the sort's fast path (k_sort_fixup)
 
     int walk_grid_ref = 0, walk_grid_acc = 0;
+    int walk_warps_resident = 0;  // accuracy walk warps resident at once (default shape)
     bool have_state = false;
     bool caller_order = false;  // true from bh_set_state until the next step
 
@@ -318,6 +348,14 @@ ssg::StepArgs step_args(bh_system* s) {
     // shared walk starts: super-groups of 512 bodies counted from each system's start
     a.frontier = Frontier{s->flist, s->fcount, s->nseg > 1 ? s->sup_off : nullptr};
     a.heavy = Heavy{s->heavy, s->work + kWorkHeavy, s->mean_cost, s->seg_cost};
+    // Shared walk groups.  share_tail > 0: the heavy groups and the last
+    // share_tail groups handed out; 0 (default): the heavy groups, when the walk
+    // has no more groups than the GPU has resident walk warps (measured faster
+    // there, slower above); -1: none.
+    const int ng = a.bpl == 2 ? s->ngroups2 : s->ngroups;
+    if (s->p.share_tail > 0 || (s->p.share_tail == 0 && ng <= s->walk_warps_resident))
+        a.share = Share{s->share_ctr, s->share_state, s->share_desc, s->share_idx, s->share_sum,
+                        s->share_batches, s->share_slices, std::min(std::max(s->p.share_tail, 0), ng)};
     return a;
 }
 
@@ -345,8 +383,8 @@ int enqueue_sort(bh_system* s, cudaStream_t st, cudaEvent_t* ev, bool keep_stats
     CK(launch_pdl(k_keys_step, nb, tb, 0, st, cur.x, cur.y, n, segs,
                   carry ? (const int*)s->box_next : (const int*)s->box_ord, s->keys, s->vals,
                   s->counter, reinterpret_cast<int*>(s->inter), keep_stats ? 0 : kStepZero,
-                  s->work + kWorkSortOverflow, s->seg_cost, s->mean_cost,
-                  carry ? s->box_ord : (int*)nullptr));
+                  s->work + kWorkSortOverflow, kStepFlags, s->share_ctr, kCtrWords + s->share_slices,
+                  s->seg_cost, s->mean_cost, carry ? s->box_ord : (int*)nullptr));
     CK(mark(2));
 
     // Sort (stable, by key, then by system): LSD passes over the key's top
@@ -824,6 +862,12 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     bytes += span<int>((size_t)s->nsupers * kFrontierCap) + span<int2>((size_t)s->nsupers) +
              span<int>(nseg + 1) + span<int>((size_t)s->ngroups) +
              span<unsigned long long>(nseg) + span<int>(nseg);
+    // (below 2^27: the walk's slice list packs a first batch times 16 in an int)
+    s->share_batches = (int)std::max<size_t>(64, std::min<size_t>(N / kShareBatchDiv, 1u << 26));
+    // the key kernel's threads (n rounded up to 256) clear the counters and slice states
+    s->share_slices = std::min((int)((N + 255) / 256 * 256) - kCtrWords, s->share_batches / 2);
+    bytes += span<int>((size_t)s->share_batches * 32) + span<float2>((size_t)s->share_batches * 32) +
+             span<int>(kCtrWords + (size_t)s->share_slices) + span<int4>((size_t)s->share_slices);
     cudaError_t e = cudaMalloc(&s->arena, bytes);
     if (e != cudaSuccess) {
         cuda_fail(e, "cudaMalloc(arena)");
@@ -895,6 +939,11 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     s->heavy = carve<int>(c, (size_t)s->ngroups);
     s->seg_cost = carve<unsigned long long>(c, nseg);
     s->mean_cost = carve<int>(c, nseg);
+    s->share_idx = carve<int>(c, (size_t)s->share_batches * 32);
+    s->share_sum = carve<float2>(c, (size_t)s->share_batches * 32);
+    s->share_ctr = carve<int>(c, kCtrWords + (size_t)s->share_slices);
+    s->share_state = s->share_ctr + kCtrWords;
+    s->share_desc = carve<int4>(c, (size_t)s->share_slices);
 
     std::vector<int> sop;
     if (nseg > 1) {
@@ -936,6 +985,7 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
                                                       (size_t)kWalkWarps * acc_warp_bytes(sh));
         s->walk_grid_ref = walk_grid_cap(s->sms, bref) * 4;
         s->walk_grid_acc = walk_grid_cap(s->sms, bacc) * 4;
+        s->walk_warps_resident = walk_grid_cap(s->sms, bacc) * kWalkWarps;
         cudaGetLastError();
     }
     if (rc != BH_OK) {
@@ -1381,6 +1431,14 @@ int bh_get_debug(bh_system* s, const char* name, void* host_out, size_t bytes, v
         CK(cudaMemcpy((char*)host_out + 4 * N, s->ay, 4 * N, cudaMemcpyDeviceToHost));
         return BH_OK;
     }
+    if (nm == "share") {  // the last walk's Share counters
+        if (bytes < 4 * 4) return BH_ERR_ARG;
+        std::vector<int> ctr(kCtrWords);
+        CK(cudaMemcpy(ctr.data(), s->share_ctr, 4 * kCtrWords, cudaMemcpyDeviceToHost));
+        const int at[4] = {kCtrHead, kCtrTail, kCtrBatches, kCtrBack};
+        for (int k = 0; k < 4; ++k) static_cast<int*>(host_out)[k] = ctr[at[k]];
+        return BH_OK;
+    }
     if (nm == "keys") { src = s->kfinal; need = 8 * N; }
     else if (nm == "perm") { src = s->st[0].id; need = 4 * N; }
     else if (nm == "node_left") { src = s->tree.left; need = 4 * N; }
@@ -1596,11 +1654,13 @@ int enqueue_energy(bh_system* s, cudaStream_t st) {
     if (a.bpl == 2)
         k_walk_acc<false, false, true, 2><<<grid, a.warps * 32, smem, st>>>(
             sh, a.segs, gr, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt, 0.0f,
-            a.out, a.status, a.inter, counter, a.fresh, s->work + 7, pot, Frontier{}, Heavy{});
+            a.out, a.status, a.inter, counter, a.fresh, s->work + 7, pot, Frontier{}, Heavy{},
+            Share{});
     else
         k_walk_acc<false, false, true, 1><<<grid, a.warps * 32, smem, st>>>(
             sh, a.segs, gr, a.in, a.recA, a.recB, a.recC, a.recD, a.eps2, a.G, a.dt, a.ddt, 0.0f,
-            a.out, a.status, a.inter, counter, a.fresh, s->work + 7, pot, Frontier{}, Heavy{});
+            a.out, a.status, a.inter, counter, a.fresh, s->work + 7, pot, Frontier{}, Heavy{},
+            Share{});
     CK(cudaGetLastError());
     CK(cudaMemsetAsync(s->diag, 0, sizeof(double) * 4 * s->nseg, st));
     Segs segs{s->nseg, s->seg_off, s->nseg > 1 ? s->seg_of_pos : nullptr};

@@ -36,6 +36,7 @@ struct StepArgs {
     int walk_grid_ref, walk_grid_acc;
     Frontier frontier;  // shared walk starts (main accuracy pass)
     Heavy heavy;        // heavy walk groups first (main accuracy pass)
+    Share share;        // shared walk groups (main accuracy pass)
 };
 
 cudaError_t launch_walk(const StepArgs& a, cudaStream_t st, int part);

@@ -323,15 +323,21 @@ struct AccShape {
     int bpl;     // bodies per lane: a warp walks for a group of 32 * bpl bodies (1 or 2)
 };
 
+// Slices a shared walk group lists before its owner adds them up (see the
+// shared groups below).
+constexpr int kOwnSlices = 64;
+
 // Per-warp shared memory of the accuracy walk (bytes, 16-byte aligned pieces):
-// staged cell records, staged bodies, the group's positions, the cell list,
+// staged cell records and bodies (with 128 spare bytes), a shared group's
+// slice list (walks that share groups), the group's positions, the cell list,
 // the node stack and the body list.
-__host__ __device__ __forceinline__ int acc_body_cap(int bucket) {
+__host__ __device__ constexpr int acc_body_cap(int bucket) {
     return 32 + 32 * (bucket > 4 ? bucket : 4);
 }
-__host__ __device__ __forceinline__ int acc_warp_bytes(AccShape sh) {
-    return 3 * 32 * 16 + 32 * 8 * sh.bpl + 16 + 64 * 4 + ((sh.stack * 4 + 15) & ~15) +
-           ((acc_body_cap(sh.bucket) * 4 + 15) & ~15);
+__host__ __device__ constexpr int acc_own_bytes(bool share) { return share ? kOwnSlices * 8 : 0; }
+__host__ __device__ constexpr int acc_warp_bytes(AccShape sh, bool share = false) {
+    return 3 * 32 * 16 + acc_own_bytes(share) + 32 * 8 * sh.bpl + 16 + 64 * 4 +
+           ((sh.stack * 4 + 15) & ~15) + ((acc_body_cap(sh.bucket) * 4 + 15) & ~15);
 }
 
 // ------------------------------------------------------------------ REFERENCE walk, batched
@@ -787,6 +793,275 @@ __global__ void __launch_bounds__(WARPS * 32) k_frontier(Segs segs, int nsupers,
 // loop over the 32 bodies in every lane.
 constexpr int kSerialExactLanes = 8;
 
+// The sum of one staged batch for each of a lane's bodies: the value the walk
+// adds to its running sums.  k cells as quadrupoles (cells_sum) or k bodies
+// (bodies_sum), pairs in FP32x2 and an odd last entry in scalar arithmetic.
+// The walk's own batches and the batches of a shared group evaluated by
+// another warp both go through these, so a batch sums to the same floats
+// whichever warp evaluates it.
+template <int BPL>
+__device__ __forceinline__ void cells_sum(const CellPairs& cp, int k, const float (&px)[BPL],
+                                          const float (&py)[BPL], const float2 (&npx)[BPL],
+                                          const float2 (&npy)[BPL], float eps2, float (&ox)[BPL],
+                                          float (&oy)[BPL]) {
+    const float2 e2v = make_float2(eps2, eps2);
+    float bx[BPL], by[BPL];
+    float2 sx[BPL], sy[BPL];
+#pragma unroll
+    for (int b = 0; b < BPL; ++b) {
+        bx[b] = by[b] = 0.0f;
+        sx[b] = sy[b] = make_float2(0.0f, 0.0f);
+    }
+    if (k == 32) {
+#pragma unroll 8
+        for (int e = 0; e < 16; ++e) {
+            const float4 xy = cp.xy[e], mh = cp.mh[e], t01 = cp.t01[e];
+            const float2 t11 = cp.t11[e];
+#pragma unroll
+            for (int b = 0; b < BPL; ++b) p2m_pair(xy, mh, t01, t11, npx[b], npy[b], e2v, sx[b], sy[b]);
+        }
+    } else {
+        for (int e = 0; e < (k >> 1); ++e) {
+            const float4 xy = cp.xy[e], mh = cp.mh[e], t01 = cp.t01[e];
+            const float2 t11 = cp.t11[e];
+#pragma unroll
+            for (int b = 0; b < BPL; ++b) p2m_pair(xy, mh, t01, t11, npx[b], npy[b], e2v, sx[b], sy[b]);
+        }
+        if (k & 1) {
+            float4 A, B;
+            unpair_cell(cp, k - 1, A, B);
+#pragma unroll
+            for (int b = 0; b < BPL; ++b) p2m(A, B, px[b], py[b], eps2, bx[b], by[b]);
+        }
+    }
+#pragma unroll
+    for (int b = 0; b < BPL; ++b) {
+        ox[b] = bx[b] + (sx[b].x + sx[b].y);
+        oy[b] = by[b] + (sy[b].x + sy[b].y);
+    }
+}
+
+template <int BPL>
+__device__ __forceinline__ void bodies_sum(const float4* bxy, const float2* bm, int k,
+                                           const float (&px)[BPL], const float (&py)[BPL],
+                                           const float2 (&npx)[BPL], const float2 (&npy)[BPL],
+                                           float eps2, float (&ox)[BPL], float (&oy)[BPL]) {
+    const float2 e2v = make_float2(eps2, eps2);
+    // entry e of the staged bodies, unpaired
+    auto body = [&](int e, float& x, float& y, float& m) {
+        const float4 q = bxy[e >> 1];
+        const float2 w = bm[e >> 1];
+        x = (e & 1) ? q.y : q.x;
+        y = (e & 1) ? q.w : q.z;
+        m = (e & 1) ? w.y : w.x;
+    };
+    float bx[BPL], by[BPL];
+    float2 sx[BPL], sy[BPL];
+#pragma unroll
+    for (int b = 0; b < BPL; ++b) {
+        bx[b] = by[b] = 0.0f;
+        sx[b] = sy[b] = make_float2(0.0f, 0.0f);
+    }
+    if (eps2 > 0.0f) {
+        if (k == 32) {
+#pragma unroll 8
+            for (int e = 0; e < 16; ++e) {
+                const float4 xy = bxy[e];
+                const float2 w = bm[e];
+#pragma unroll
+                for (int b = 0; b < BPL; ++b) p2p_pair(xy, w, npx[b], npy[b], e2v, sx[b], sy[b]);
+            }
+        } else {
+            for (int e = 0; e < (k >> 1); ++e) {
+                const float4 xy = bxy[e];
+                const float2 w = bm[e];
+#pragma unroll
+                for (int b = 0; b < BPL; ++b) p2p_pair(xy, w, npx[b], npy[b], e2v, sx[b], sy[b]);
+            }
+            if (k & 1) {
+                float x, y, m;
+                body(k - 1, x, y, m);
+#pragma unroll
+                for (int b = 0; b < BPL; ++b) p2p<false>(x, y, m, px[b], py[b], eps2, bx[b], by[b]);
+            }
+        }
+    } else {
+        for (int e = 0; e < k; ++e) {
+            float x, y, m;
+            body(e, x, y, m);
+#pragma unroll
+            for (int b = 0; b < BPL; ++b) p2p<true>(x, y, m, px[b], py[b], eps2, bx[b], by[b]);
+        }
+    }
+#pragma unroll
+    for (int b = 0; b < BPL; ++b) {
+        ox[b] = bx[b] + (sx[b].x + sx[b].y);
+        oy[b] = by[b] + (sy[b].x + sy[b].y);
+    }
+}
+
+// ------------------------------------------------------------------ shared groups
+//
+// The heaviest groups of the main accuracy walk (taken first, they still last
+// about as long as the whole walk) keep one warp busy each.  The warp that
+// takes a shared group walks the tree for it as usual, but records each batch
+// of up to 32 entries it would evaluate (the nodes or the bodies) in a pool
+// instead of evaluating it, and publishes the batches kSliceBatches at a time
+// as a slice.  A warp between two groups takes a published slice first: it
+// evaluates the slice's batches for the group's bodies and stores every
+// lane's batch sums.  At the end of its walk the owner evaluates every slice
+// that no other warp has taken (the latest first), then adds all batch sums
+// in the order it recorded them.  The batch sums are the ones the owner would
+// have formed (the same entries, staged the same way, cells_sum / bodies_sum),
+// added in the same order: a shared group's results are bit for bit those of
+// an unshared one, whichever warps evaluated its batches.  A group that runs
+// out of pool or slice list is walked again, unshared.  Every wait is
+// bounded: a slice reserved but not yet published is left to its owner, and a
+// taken slice that is never finished (a running warp always finishes it) is
+// reported as ST_TREE.
+// Measured on GB300 (Plummer, MIXED, graph step): sharing the heavy groups
+// gains 6 % at 2^16 bodies and 4 % at 2^17, where a system has fewer walk
+// groups than the GPU has resident warps, and loses 3-12 % from 2^18 on, where
+// every warp has several groups and the pool's extra loads and stores cost
+// more than the heavy groups' tail; the host shares by default only below
+// that size.
+constexpr int kSliceBatches = 8;      // batches per slice (at most 15: 4 bits in the slice list)
+constexpr int kReadyPolls = 64;       // polls for a reserved slice to be published
+constexpr int kDonePolls = 1 << 18;   // polls for a taken slice to be evaluated (~0.2 s)
+// Counters of the shared groups (Share::ctr), each on its own 128-byte line:
+// every warp reads the queue's head and tail between groups.
+enum : int { kCtrHead = 0, kCtrTail = 1, kCtrBatches = 32, kCtrBack = 64, kCtrWords = 96 };
+static_assert(kSliceBatches < 16, "slice list packs the batch count in 4 bits");
+enum : int { SL_EMPTY = 0, SL_READY = 1, SL_TAKEN = 2, SL_DONE = 3 };
+
+struct Share {
+    int* ctr = nullptr;     // [kCtrWords]: slices handed out (kCtrHead), slices reserved
+                            // (kCtrTail), pool batches reserved, slices taken back by their
+                            // owners; cleared every step.  null: no sharing
+    int* state = nullptr;   // [cap_slices] SL_*, cleared every step
+    int4* desc = nullptr;   // [cap_slices] (first batch, batches, group's first body, system end)
+    int* idx = nullptr;     // [cap_batches][32] an entry's node, or ~body; INT_MIN past the end
+    float2* sum = nullptr;  // [cap_batches][bodies per lane][32] each lane's batch sum (x, y)
+    int cap_batches = 0, cap_slices = 0;
+    int tail = 0;           // the last `tail` groups handed out are shared as well
+};
+
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ int ld_relaxed_gpu(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(int* p, int v) {
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+// The first value >= least that *p holds, or the last one read after `polls` more reads.
+__device__ __forceinline__ int wait_state(const int* p, int least, int polls) {
+    int v = ld_acquire_gpu(p);
+    for (int i = 0; v < least && i < polls; ++i) {
+        __nanosleep(64);
+        v = ld_acquire_gpu(p);
+    }
+    return v;
+}
+// lane 0: the oldest published slice not yet handed out, now taken by this
+// warp (SL_READY -> SL_TAKEN), or -1.  The queue's head moves by atomicAdd (a
+// compare-and-swap loop serialises thousands of warps); a warp that moves it
+// past the tail in a race, or finds its slice unpublished after kReadyPolls
+// reads or taken back by its owner, goes on to the next one.  A slice skipped
+// that way is evaluated by its owner.
+__device__ __forceinline__ int take_slice(const Share& sh) {
+    for (;;) {
+        if (ld_relaxed_gpu(sh.ctr + kCtrHead) >= ld_relaxed_gpu(sh.ctr + kCtrTail)) return -1;
+        const int s = atomicAdd(sh.ctr + kCtrHead, 1);
+        if (s >= sh.cap_slices) return -1;
+        if (wait_state(sh.state + s, SL_READY, kReadyPolls) == SL_READY &&
+            atomicCAS(sh.state + s, SL_READY, SL_TAKEN) == SL_READY)
+            return s;
+    }
+}
+
+// A warp's staging area at the start of its shared memory: 16 cell pairs
+// (896 bytes), 16 body pairs (256 + 128), their indices (128), 128 spare.
+__device__ __forceinline__ void acc_staging(unsigned char* wbase, CellPairs& cp, float4*& bxy,
+                                            float2*& bm, int2*& bid) {
+    cp.xy = reinterpret_cast<float4*>(wbase);
+    cp.mh = cp.xy + 16;
+    cp.t01 = cp.mh + 16;
+    cp.t11 = reinterpret_cast<float2*>(cp.t01 + 16);
+    bxy = reinterpret_cast<float4*>(cp.t11 + 16);
+    bm = reinterpret_cast<float2*>(bxy + 16);
+    bid = reinterpret_cast<int2*>(bm + 16);
+}
+
+// Batches first .. first + nb - 1 of the pool (idx) for a group whose lane
+// bodies are at (px, py), staged in the warp's staging area (wbase): every
+// lane's batch sums to sum[].
+template <int BPL>
+__device__ __forceinline__ void eval_batches(unsigned char* wbase, const float4* __restrict__ recA,
+                                             const float4* __restrict__ recB,
+                                             const float* __restrict__ x,
+                                             const float* __restrict__ y,
+                                             const float* __restrict__ m, const int* idx,
+                                             float2* sum, float eps2, int first, int nb,
+                                             const float (&px)[BPL], const float (&py)[BPL]) {
+    const int lane = threadIdx.x & 31;
+    CellPairs cp;
+    float4* bxy;
+    float2* bm;
+    int2* bid;
+    acc_staging(wbase, cp, bxy, bm, bid);
+    float2 npx[BPL], npy[BPL];
+#pragma unroll
+    for (int b = 0; b < BPL; ++b) {
+        npx[b] = make_float2(-px[b], -px[b]);
+        npy[b] = make_float2(-py[b], -py[b]);
+    }
+    // each batch's entries are loaded one batch ahead
+    int vnext = __ldcg(idx + (size_t)first * 32 + lane);
+    for (int t = 0; t < nb; ++t) {
+        const size_t bt = (size_t)first + t;
+        const int v = vnext;
+        if (t + 1 < nb) vnext = __ldcg(idx + (bt + 1) * 32 + lane);
+        const int k = __popc(__ballot_sync(kFull, v != INT_MIN));  // the entries are a prefix
+        const bool body = __shfl_sync(kFull, v, 0) < 0;
+        float ox[BPL], oy[BPL];
+        __syncwarp();  // the staging area of the last batch is read
+        const int q = lane >> 1, h = lane & 1;
+        if (body) {
+            if (lane < k) {
+                const int bi = ~v;
+                reinterpret_cast<float*>(&bxy[q])[h] = x[bi];
+                reinterpret_cast<float*>(&bxy[q])[2 + h] = y[bi];
+                reinterpret_cast<float*>(&bm[q])[h] = m[bi];
+            }
+            __syncwarp();
+            bodies_sum<BPL>(bxy, bm, k, px, py, npx, npy, eps2, ox, oy);
+        } else {
+            if (lane < k) {
+                const float4 A = recA[v], B = recB[v];
+                reinterpret_cast<float*>(cp.xy + q)[h] = A.x;
+                reinterpret_cast<float*>(cp.xy + q)[2 + h] = A.y;
+                reinterpret_cast<float*>(cp.mh + q)[h] = A.z;
+                reinterpret_cast<float*>(cp.mh + q)[2 + h] = -B.w;
+                reinterpret_cast<float*>(cp.t01 + q)[h] = -B.x;
+                reinterpret_cast<float*>(cp.t01 + q)[2 + h] = -B.y;
+                reinterpret_cast<float*>(cp.t11 + q)[h] = -B.z;
+            }
+            __syncwarp();
+            cells_sum<BPL>(cp, k, px, py, npx, npy, eps2, ox, oy);
+        }
+#pragma unroll
+        for (int b = 0; b < BPL; ++b)
+            __stcg(sum + (bt * BPL + b) * 32 + lane, make_float2(ox[b], oy[b]));
+    }
+    __syncwarp();
+}
+
 // PLAIN / MIXED walk.  ESTIMATE = the bootstrap pass after bh_set_state: the
 // geometric rule only, at opening angle max(theta, kBootstrapTheta) (radius
 // in recD.w), cells as monopoles, launched with 64-body groups; writes |G a|
@@ -795,8 +1070,9 @@ constexpr int kSerialExactLanes = 8;
 // d = min over the group's bodies of |COM - p|; the geometric rule is d > l/theta + delta.
 // DIAG = diagnostics pass: the main rule, but each body's potential (FP64
 // accumulation of float batches, own body excluded) goes to pot[] and nothing
-// is integrated.
-template <bool MIXED, bool ESTIMATE, bool DIAG = false, int BPL = 1>
+// is integrated.  SHARE = the main pass with shared groups (sh); without it
+// none of their code or shared memory is compiled in.
+template <bool MIXED, bool ESTIMATE, bool DIAG = false, int BPL = 1, bool SHARE = false>
 __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape shape, Segs segs, Groups gr, WalkIn in,
                                                          const float4* __restrict__ recA,
                                                          const float4* __restrict__ recB,
@@ -809,7 +1085,7 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
                                                          int* __restrict__ fresh,
                                                          int* __restrict__ max_stack,
                                                          double* __restrict__ pot,
-                                                         Frontier fr, Heavy hv) {
+                                                         Frontier fr, Heavy hv, Share sh) {
     pdl_wait();
     static_assert(BPL == 1 || BPL == 2, "one or two bodies per lane");
     if (ESTIMATE) {
@@ -822,18 +1098,15 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
     const unsigned lt = lanemask_lt();
     const int STACK = shape.stack, BUCKET = shape.bucket;
     constexpr int GW = 32 * BPL;  // bodies per group
-    unsigned char* wbase = smem_raw + (size_t)warp * acc_warp_bytes(shape);
+    unsigned char* wbase = smem_raw + (size_t)warp * acc_warp_bytes(shape, SHARE);
     // 1536 bytes: 16 cell pairs (896), 16 body pairs (512), 128 spare
     CellPairs cpair;
-    cpair.xy = reinterpret_cast<float4*>(wbase);
-    cpair.mh = cpair.xy + 16;
-    cpair.t01 = cpair.mh + 16;
-    cpair.t11 = reinterpret_cast<float2*>(cpair.t01 + 16);
-    float4* bxy = reinterpret_cast<float4*>(cpair.t11 + 16);
-    float2* bm = reinterpret_cast<float2*>(bxy + 16);
-    int2* bid = reinterpret_cast<int2*>(bm + 16);
+    float4* bxy;
+    float2* bm;
+    int2* bid;
+    acc_staging(wbase, cpair, bxy, bm, bid);
     // the group's GW positions in pairs: (x_2i, x_2i+1, y_2i, y_2i+1)
-    float4* gp = reinterpret_cast<float4*>(wbase + 3 * 32 * 16);
+    float4* gp = reinterpret_cast<float4*>(wbase + 3 * 32 * 16 + acc_own_bytes(SHARE));
     float4* gext = gp + GW / 2;  // y at min/max x, x at min/max y
     int* clist = reinterpret_cast<int*>(gext + 1);
     int* stack = clist + 64;
@@ -845,10 +1118,52 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
     const BoxFold fold{reinterpret_cast<float4*>(wbase + 1408), reinterpret_cast<int*>(wbase + 1424),
                        out.box_next, status};
     if (folding) fold.init();
+    // shared groups (main pass only): this warp's slice list; its open slice
+    // as (first batch, batches recorded, slices listed, 1: out of room); its
+    // group as (first body, system end, hand-out index, 1: shared)
+    const bool sharing = SHARE && !ESTIMATE && !DIAG && sh.ctr != nullptr;
+    // (all at fixed offsets: the slice list after the staging area, the rest
+    // in its spare bytes after the folded box)
+    int2* own = reinterpret_cast<int2*>(wbase + 3 * 32 * 16);
+    int4* ows = reinterpret_cast<int4*>(wbase + 1440);
+    int4* ogr = reinterpret_cast<int4*>(wbase + 1456);
 
     // heavy groups first (hv.count set: the main pass), then the others in order
     const int nh = hv.count ? *hv.count : 0;
-    for (int c = next_group(work); c < nh + gr.ngroups; c = next_group(work)) {
+    const int total = nh + gr.ngroups;
+    int retry = -1;  // a shared group that ran out of room, to be walked again unshared
+    for (;;) {
+        const bool again = retry >= 0;
+        int c = retry;
+        retry = -1;
+        if (!again) {
+        if (sharing) {
+            // a published slice of a shared group comes before a new group
+            int sl = lane == 0 ? take_slice(sh) : -1;
+            sl = __shfl_sync(kFull, sl, 0);
+            if (sl >= 0) {
+                // the slice's group: its first body and its system's end; lanes
+                // past the end mirror the first body, as in the walk
+                const int4 d = __ldcg(sh.desc + sl);
+                float qx[BPL], qy[BPL];
+#pragma unroll
+                for (int b = 0; b < BPL; ++b) {
+                    const int jb = d.z + 32 * b + lane;
+                    qx[b] = in.x[jb < d.w ? jb : d.z];
+                    qy[b] = in.y[jb < d.w ? jb : d.z];
+                }
+                eval_batches<BPL>(wbase, recA, recB, in.x, in.y, in.m, sh.idx, sh.sum, eps2, d.x, d.y,
+                                  qx, qy);
+                __threadfence();  // this lane's sums before the slice is marked done
+                __syncwarp();
+                if (lane == 0) st_release_gpu(sh.state + sl, SL_DONE);
+                continue;
+            }
+        }
+        // (a warp without groups leaves: the owners take back what is left)
+        c = next_group(work);
+        if (c >= total) break;
+        }
         const int g = c < nh ? hv.list[c] : c - nh;
         int lo, hi, gstart, sg;
         group_range(segs, gr, g, &lo, &hi, &gstart, GW, &sg);
@@ -937,6 +1252,16 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
             }
             aa = alpha * fmaxf(amin, 0.1f * asum / (float)cnt);
         }
+        if (sharing) {
+            // a heavy group, or one of the last `tail` handed out: shared
+            // (unless it ran out of room in the pool before)
+            const bool shared = !again && (c < nh || c >= total - sh.tail);
+            if (lane == 0) {
+                *ows = make_int4(0, 0, 0, 0);
+                *ogr = make_int4(gstart, hi, c, shared ? 1 : 0);
+            }
+            __syncwarp();
+        }
         float ax[BPL], ay[BPL];    // running sums
         float cax[BPL], cay[BPL];  // Kahan compensation (MIXED)
         double phi[BPL];           // DIAG: potential
@@ -982,7 +1307,97 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
             npy[b] = make_float2(-py[b], -py[b]);
         }
         const float2 e2v = make_float2(eps2, eps2);
+        // Shared group: add up the recorded batches, in order.  First every
+        // slice that no other warp has taken (the open one, never published,
+        // among them) is evaluated here, the latest first, while the others
+        // finish theirs; then all batch sums are added in the recorded order,
+        // waiting for the slices still being evaluated elsewhere.
+        auto combine = [&]() {
+            int4 w = *ows;
+            __syncwarp();
+            if (w.y > 0) {
+                if (lane == 0) own[w.z] = make_int2(w.x * 16 + w.y, -1);
+                ++w.z;
+                __syncwarp();
+            }
+            for (int i = w.z - 1; i >= 0; --i) {
+                const int2 o = own[i];
+                int mine = o.y < 0;
+                if (!mine && lane == 0 && atomicCAS(sh.state + o.y, SL_READY, SL_TAKEN) == SL_READY) {
+                    mine = 1;
+                    atomicAdd(sh.ctr + kCtrBack, 1);
+                }
+                mine = __shfl_sync(kFull, mine, 0);
+                if (mine) {
+                    eval_batches<BPL>(wbase, recA, recB, in.x, in.y, in.m, sh.idx, sh.sum, eps2,
+                                      o.x >> 4, o.x & 15, px, py);
+                    if (lane == 0) own[i].y = -1;  // evaluated here: nothing to wait for
+                }
+            }
+            __syncwarp();
+            for (int i = 0; i < w.z; ++i) {
+                const int2 o = own[i];
+                const int first = o.x >> 4, nb = o.x & 15;
+                if (o.y >= 0 && lane == 0 && wait_state(sh.state + o.y, SL_DONE, kDonePolls) != SL_DONE)
+                    atomicOr(status, ST_TREE);  // never finished: not a running warp's
+                __syncwarp();
+                for (int t = 0; t < nb; ++t) {
+#pragma unroll
+                    for (int b = 0; b < BPL; ++b) {
+                        const float2 v = __ldcg(sh.sum + ((size_t)(first + t) * BPL + b) * 32 + lane);
+                        add_batch(b, v.x, v.y);
+                    }
+                }
+            }
+            if (lane == 0) *ows = make_int4(0, 0, 0, 0);
+            __syncwarp();
+        };
+        // Shared group: src[0..k) (nodes, or bodies when `body`) becomes the
+        // next recorded batch.  No room in the pool or the slice list: redo.
+        auto record = [&](const int* src, int k, bool body) {
+            int4 w = *ows;
+            __syncwarp();
+            if (w.y == 0) {
+                int base = INT_MAX;
+                if (lane == 0 && w.z < kOwnSlices) base = atomicAdd(sh.ctr + kCtrBatches, kSliceBatches);
+                base = __shfl_sync(kFull, base, 0);
+                if (base > sh.cap_batches - kSliceBatches) {
+                    if (lane == 0) ows->w = 1;  // redo
+                    __syncwarp();
+                    return;
+                }
+                w.x = base;
+            }
+            const int v = lane < k ? (body ? ~src[lane] : src[lane]) : INT_MIN;
+            __stcg(sh.idx + (size_t)(w.x + w.y) * 32 + lane, v);
+            if (++w.y == kSliceBatches) {
+                // publish the slice (or keep it, when the state array is full)
+                __threadfence();  // this lane's entries before the slice is published
+                __syncwarp();
+                if (lane == 0) {
+                    int sl = atomicAdd(sh.ctr + kCtrTail, 1);
+                    if (sl < sh.cap_slices) {
+                        sh.desc[sl] = make_int4(w.x, w.y, ogr->x, ogr->y);
+                        st_release_gpu(sh.state + sl, SL_READY);
+                    } else {
+                        sl = -1;
+                    }
+                    own[w.z] = make_int2(w.x * 16 + w.y, sl);
+                }
+                ++w.z;
+                w.y = 0;
+            }
+            if (lane == 0) *ows = w;
+            __syncwarp();
+        };
         auto flush_cells = [&](int k) {  // the last k entries of clist
+            if (sharing && ogr->w) {
+                if (!ows->w) record(clist + ccnt - k, k, false);
+                ccnt -= k;
+                entries += k;
+                centries += k;
+                return;
+            }
             __syncwarp();
             if (lane < k) {
                 const int node = clist[ccnt - k + lane];
@@ -1009,7 +1424,8 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
                 }
 #pragma unroll
                 for (int b = 0; b < BPL; ++b) phi[b] += (double)f[b];
-            } else {
+            } else if (ESTIMATE) {
+                // the bootstrap needs |a| to a few per cent: monopoles suffice
                 float bx[BPL], by[BPL];
                 float2 sx[BPL], sy[BPL];
 #pragma unroll
@@ -1017,55 +1433,40 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
                     bx[b] = by[b] = 0.0f;
                     sx[b] = sy[b] = make_float2(0.0f, 0.0f);
                 }
-                if (ESTIMATE) {
-                    // the bootstrap needs |a| to a few per cent: monopoles suffice
-                    for (int e = 0; e < (k >> 1); ++e) {
-                        const float4 mh = cpair.mh[e];
-                        const float4 xy = cpair.xy[e];
+                for (int e = 0; e < (k >> 1); ++e) {
+                    const float4 mh = cpair.mh[e];
+                    const float4 xy = cpair.xy[e];
 #pragma unroll
-                        for (int b = 0; b < BPL; ++b)
-                            p2p_pair(xy, make_float2(mh.x, mh.y), npx[b], npy[b], e2v, sx[b], sy[b]);
-                    }
-                    if (k & 1) {
-                        float4 A, B;
-                        unpair_cell(cpair, k - 1, A, B);
+                    for (int b = 0; b < BPL; ++b)
+                        p2p_pair(xy, make_float2(mh.x, mh.y), npx[b], npy[b], e2v, sx[b], sy[b]);
+                }
+                if (k & 1) {
+                    float4 A, B;
+                    unpair_cell(cpair, k - 1, A, B);
 #pragma unroll
-                        for (int b = 0; b < BPL; ++b)
-                            p2p<false>(A.x, A.y, A.z, px[b], py[b], eps2, bx[b], by[b]);
-                    }
-                } else if (k == 32) {
-#pragma unroll 8
-                    for (int e = 0; e < 16; ++e) {
-                        const float4 xy = cpair.xy[e], mh = cpair.mh[e], t01 = cpair.t01[e];
-                        const float2 t11 = cpair.t11[e];
-#pragma unroll
-                        for (int b = 0; b < BPL; ++b)
-                            p2m_pair(xy, mh, t01, t11, npx[b], npy[b], e2v, sx[b], sy[b]);
-                    }
-                } else {
-                    for (int e = 0; e < (k >> 1); ++e) {
-                        const float4 xy = cpair.xy[e], mh = cpair.mh[e], t01 = cpair.t01[e];
-                        const float2 t11 = cpair.t11[e];
-#pragma unroll
-                        for (int b = 0; b < BPL; ++b)
-                            p2m_pair(xy, mh, t01, t11, npx[b], npy[b], e2v, sx[b], sy[b]);
-                    }
-                    if (k & 1) {
-                        float4 A, B;
-                        unpair_cell(cpair, k - 1, A, B);
-#pragma unroll
-                        for (int b = 0; b < BPL; ++b) p2m(A, B, px[b], py[b], eps2, bx[b], by[b]);
-                    }
+                    for (int b = 0; b < BPL; ++b)
+                        p2p<false>(A.x, A.y, A.z, px[b], py[b], eps2, bx[b], by[b]);
                 }
 #pragma unroll
                 for (int b = 0; b < BPL; ++b)
                     add_batch(b, bx[b] + (sx[b].x + sx[b].y), by[b] + (sy[b].x + sy[b].y));
+            } else {
+                float ox[BPL], oy[BPL];
+                cells_sum<BPL>(cpair, k, px, py, npx, npy, eps2, ox, oy);
+#pragma unroll
+                for (int b = 0; b < BPL; ++b) add_batch(b, ox[b], oy[b]);
             }
             ccnt -= k;
             entries += k;
             centries += k;
         };
         auto flush_bodies = [&](int k) {
+            if (sharing && ogr->w) {
+                if (!ows->w) record(blist + bcnt - k, k, true);
+                bcnt -= k;
+                entries += k;
+                return;
+            }
             __syncwarp();
             if (lane < k) {
                 const int bi = blist[bcnt - k + lane];
@@ -1076,14 +1477,6 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
                 reinterpret_cast<int*>(&bid[pi])[h] = bi;
             }
             __syncwarp();
-            // entry e of the staged bodies, unpaired
-            auto body = [&](int e, float& x, float& y, float& m) {
-                const float4 q = bxy[e >> 1];
-                const float2 w = bm[e >> 1];
-                x = (e & 1) ? q.y : q.x;
-                y = (e & 1) ? q.w : q.z;
-                m = (e & 1) ? w.y : w.x;
-            };
             if (DIAG) {
                 float f[BPL];
 #pragma unroll
@@ -1091,8 +1484,11 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
                 for (int e = 0; e < k; ++e) {
                     const int2 ids = bid[e >> 1];
                     const int who = (e & 1) ? ids.y : ids.x;
-                    float x, y, m;
-                    body(e, x, y, m);
+                    const float4 q = bxy[e >> 1];
+                    const float2 w = bm[e >> 1];
+                    const float x = (e & 1) ? q.y : q.x;
+                    const float y = (e & 1) ? q.w : q.z;
+                    const float m = (e & 1) ? w.y : w.x;
 #pragma unroll
                     for (int b = 0; b < BPL; ++b) {
                         if (who == j[b]) continue;  // own body
@@ -1103,51 +1499,10 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
 #pragma unroll
                 for (int b = 0; b < BPL; ++b) phi[b] += (double)f[b];
             } else {
-                float bx[BPL], by[BPL];
-                float2 sx[BPL], sy[BPL];
+                float ox[BPL], oy[BPL];
+                bodies_sum<BPL>(bxy, bm, k, px, py, npx, npy, eps2, ox, oy);
 #pragma unroll
-                for (int b = 0; b < BPL; ++b) {
-                    bx[b] = by[b] = 0.0f;
-                    sx[b] = sy[b] = make_float2(0.0f, 0.0f);
-                }
-                if (eps2 > 0.0f) {
-                    if (k == 32) {
-#pragma unroll 8
-                        for (int e = 0; e < 16; ++e) {
-                            const float4 xy = bxy[e];
-                            const float2 w = bm[e];
-#pragma unroll
-                            for (int b = 0; b < BPL; ++b)
-                                p2p_pair(xy, w, npx[b], npy[b], e2v, sx[b], sy[b]);
-                        }
-                    } else {
-                        for (int e = 0; e < (k >> 1); ++e) {
-                            const float4 xy = bxy[e];
-                            const float2 w = bm[e];
-#pragma unroll
-                            for (int b = 0; b < BPL; ++b)
-                                p2p_pair(xy, w, npx[b], npy[b], e2v, sx[b], sy[b]);
-                        }
-                        if (k & 1) {
-                            float x, y, m;
-                            body(k - 1, x, y, m);
-#pragma unroll
-                            for (int b = 0; b < BPL; ++b)
-                                p2p<false>(x, y, m, px[b], py[b], eps2, bx[b], by[b]);
-                        }
-                    }
-                } else {
-                    for (int e = 0; e < k; ++e) {
-                        float x, y, m;
-                        body(e, x, y, m);
-#pragma unroll
-                        for (int b = 0; b < BPL; ++b)
-                            p2p<true>(x, y, m, px[b], py[b], eps2, bx[b], by[b]);
-                    }
-                }
-#pragma unroll
-                for (int b = 0; b < BPL; ++b)
-                    add_batch(b, bx[b] + (sx[b].x + sx[b].y), by[b] + (sy[b].x + sy[b].y));
+                for (int b = 0; b < BPL; ++b) add_batch(b, ox[b], oy[b]);
             }
             bcnt -= k;
             entries += k;
@@ -1302,6 +1657,15 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
         }
         if (ccnt > 0) flush_cells(ccnt);
         if (bcnt > 0) flush_bodies(bcnt);
+        if (sharing && ogr->w) {
+            const bool redo = ows->w != 0;
+            if (!redo) combine();
+            if (redo) {  // out of room: the group again, unshared, before any other
+                retry = ogr->z;
+                __syncwarp();
+                continue;
+            }
+        }
         if (lane == 0) {
             if (overflow) atomicOr(status, ST_STACK);
             atomicMax(max_stack, peak);
