@@ -57,6 +57,7 @@ struct Workspace {
     size_t cap = 0;  // bodies
     size_t mcap = 0;  // nodes (m) for the frontier queues
     void* base = nullptr;
+    unsigned gen = 0;  // allocations so far: a growth frees what the last build left
     uint64_t *keys, *keys_alt, *keys3;  // keys3: the third buffer of the high-word sort
     uint32_t *vals, *vals_alt, *vals3;
     int* overflow;                       // a run of equal high words longer than kFixupRun
@@ -88,12 +89,32 @@ struct Layout {
     int m = 0;
 };
 Layout g_layout[kMaxDevices];  // guarded by g_ws_mu
+
+// The last BuildQuadTree on each device, for SortParticles: its child array
+// and sizes, and the workspace (with its allocation count) that still holds
+// its sort permutation, tree and cell numbering.  BuildQuadTreeNoAlloc clears
+// it (its scratch is reused by the next call).
+struct Built {
+    const int* child = nullptr;
+    int n = 0, m = 0;
+    Workspace* w = nullptr;
+    unsigned gen = 0;
+};
+Built g_built[kMaxDevices];  // guarded by g_ws_mu
+
 int g_sms[kMaxDevices] = {};   // SM count per device, read once (guarded by g_ws_mu)
 
 int current_device() {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess) return -1;
     return dev;
+}
+
+void set_built(const Built& b) {
+    const int dev = current_device();
+    if (dev < 0 || dev >= kMaxDevices) return;
+    std::lock_guard<std::mutex> lk(g_ws_mu);
+    g_built[dev] = b;
 }
 
 void set_layout(const int* child, int m) {
@@ -153,6 +174,7 @@ Workspace* workspace(size_t n, size_t m) {
                    al(4 * 256) + al(16) + al(8) + 8 * al(4 * N) + al(16 * N) + 2 * al(16 * N) +
                    3 * al(4 * N) + 2 * al(4 * N) + al(4 * (size_t)nb) + al(4) + 2 * al(4 * M) +
                    al(12) + al(4);
+    ++w->gen;
     if (cudaMalloc(&w->base, bytes) != cudaSuccess) {
         w->base = nullptr;
         w->cap = w->mcap = 0;
@@ -437,6 +459,31 @@ __global__ void k_c_materialize(int n, int m, TreePtrs t, const uint64_t* skeys,
             }
         }
     }
+}
+
+// SortParticles from the last build (kernels.cu:299-335 computes the same by a
+// depth-first pass over the cells).  At every level a body's child index is
+// (x < mid) + 2 (y < mid) (kernels.cu:144-157), the digit its key holds
+// there, and every leaf holds one body, so the depth-first order over child
+// indices 0..3 is ascending key order: sorted[] is the sort permutation, and
+// a cell's start is the first sorted position of its bodies, the first body
+// of the tree node whose chain of cells (k_c_materialize) holds it.  The
+// same guards as k_c_materialize: nothing for cells it did not make.
+__global__ void k_c_sort_from_build(int n, int m, TreePtrs t, const uint32_t* perm,
+                                    const int* cbase, const int* total, int* start, int* sorted) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    sorted[q] = (int)perm[q];
+    if ((long long)n + *total > (long long)m) return;  // ST_CAPACITY
+    const int sp = t.split[q];
+    if (sp < 0) return;
+    const int pa = t.parent[q];
+    if (pa >= 0 && merged_into(sp, t.split[pa])) return;
+    const int L = sp >> 1;
+    if (L >= 32) return;  // ST_DUP
+    const int Lp = pa >= 0 ? (t.split[pa] >> 1) : 0;
+    const int b0 = n + cbase[q], first = t.first[q];
+    for (int k = 0; k < L - Lp; ++k) start[b0 + k] = first;
 }
 
 __global__ void k_c_com(float* x, float* y, const float* mass, const int* index, int n) {
@@ -1044,6 +1091,7 @@ void compat_BuildQuadTree(float* x, float* y, float* mass, int* count, int* star
         record(BH_ERR_ARG);
         return;
     }
+    set_built(Built{});  // until this build is enqueued
     if (n == 1) return;  // a lone body: no cells, *index stays n
     Workspace* w = workspace((size_t)n, (size_t)m);
     if (!w) {
@@ -1051,9 +1099,10 @@ void compat_BuildQuadTree(float* x, float* y, float* mass, int* count, int* star
         return;
     }
     set_layout(child, m);
-    record_cuda(enqueue_build(*w, x, y, mass, count, start, child, index, left, right, bottom, top,
-                              n, m, g_set.stream),
-                "BuildQuadTree");
+    const cudaError_t e = enqueue_build(*w, x, y, mass, count, start, child, index, left, right,
+                                        bottom, top, n, m, g_set.stream);
+    record_cuda(e, "BuildQuadTree");
+    set_built(e == cudaSuccess ? Built{child, n, m, w, w->gen} : Built{});
 }
 
 void compat_ComputeCentreOfMass(float* x, float* y, float* mass, int* index, int n) {
@@ -1066,6 +1115,23 @@ void compat_SortParticles(int* count, int* start, int* sorted, int* child, int* 
     if (n < 1) {
         record(BH_ERR_ARG);
         return;
+    }
+    {
+        // the arrays of the last BuildQuadTree on this device, its workspace
+        // not grown since: sorted[] and start[] from that build
+        Built b;
+        const int dev = current_device();
+        if (dev >= 0 && dev < kMaxDevices) {
+            std::lock_guard<std::mutex> lk(g_ws_mu);
+            b = g_built[dev];
+        }
+        if (b.child == child && b.n == n && b.w && b.w->base && b.w->gen == b.gen) {
+            const Workspace& w = *b.w;
+            k_c_sort_from_build<<<blocks_for(n, 256), 256, 0, g_set.stream>>>(
+                n, b.m, w.tree, w.vals_alt, w.cbase, w.total, start, sorted);
+            record_cuda(cudaGetLastError(), "SortParticles");
+            return;
+        }
     }
     // queues for every cell of the layout, on the current device's workspace
     const int mlimit = layout_m(child, n);
@@ -1283,6 +1349,7 @@ extern "C" int BuildQuadTreeNoAlloc(float* x, float* y, float* mass, int* count,
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return noalloc_result(cuda_fail(e, "cudaGetDevice"));
+    set_built(Built{});  // SortParticles walks this tree's cells: the scratch is reused
     int st_code = BH_OK;
     unsigned char* base = noalloc_scratch(dev, &st_code);
     if (!base) return noalloc_result(st_code);

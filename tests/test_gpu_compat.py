@@ -206,9 +206,10 @@ def test_two_systems_alternating(L):
 
 
 def test_unaligned_child_array(L):
-    """child[] 4 bytes off a 16-byte boundary (a caller's sub-array): SortParticles
-    reads its slots one by one there, and the whole update() gives exactly the
-    results of an aligned child[]."""
+    """child[] 4 bytes off a 16-byte boundary (a caller's sub-array): the whole
+    update() gives exactly the results of an aligned child[] (CalculateForces,
+    and a SortParticles without the build's workspace, read its slots one by
+    one there)."""
     g = gc.load("plummer2048")
     n = int(g["n"])
     outs = []
@@ -262,3 +263,42 @@ def test_dropin_update_matches_reference_mode(L, n):
     assert np.hypot(dax - eax, day - eay).max() <= 1e-5 * r
     ext = max(np.ptp(x), np.ptp(y))
     assert max(np.abs(dx1 - st["x"]).max(), np.abs(dy1 - st["y"]).max()) <= 1e-5 * ext
+
+
+@pytest.mark.parametrize("case", ["plummer2048", "plummer2e17"])
+def test_sort_particles_from_build_equals_traversal(L, case):
+    """SortParticles right after BuildQuadTree on the same arrays takes sorted[]
+    and start[] from the build (depth-first order is key order); on a copy of
+    the built count[] and child[] at other addresses it walks the cells level by
+    level, as kernels.cu:299-335 does.  Both give the same arrays."""
+    from stellarsolver_gb300 import dropin, models
+
+    if case == "plummer2048":
+        g = gc.load(case)
+        arrays = [g[k] for k in ("x", "y", "vx", "vy", "m")]
+    else:
+        arrays = models.plummer(1 << 17, 0x5EEDC0DF)
+    a = dropin.RefArrays(torch, *arrays)
+    n, m = a.n, a.m
+    bx = [P(b) for b in a.box]
+    L.bh_compat_clear_status()
+    L.ResetArrays(P(a.mutex), P(a.x), P(a.y), P(a.mass), P(a.count), P(a.start), P(a.sorted),
+                  P(a.child), P(a.index), *bx, n, m)
+    L.ComputeBoundingBox(P(a.mutex), P(a.x), P(a.y), *bx, n)
+    L.BuildQuadTree(P(a.x), P(a.y), P(a.mass), P(a.count), P(a.start), P(a.child), P(a.index),
+                    *bx, n, m)
+    L.ComputeCentreOfMass(P(a.x), P(a.y), P(a.mass), P(a.index), n)
+    torch.cuda.synchronize()
+    count2, start2, child2 = a.count.clone(), a.start.clone(), a.child.clone()
+    sorted2 = a.sorted.clone()
+    L.SortParticles(P(a.count), P(a.start), P(a.sorted), P(a.child), P(a.index), n)
+    L.SortParticles(P(count2), P(start2), P(sorted2), P(child2), P(a.index), n)
+    torch.cuda.synchronize()
+    assert L.bh_compat_status() == 0
+    cells = int(a.index.item())
+    assert cells > n
+    assert np.array_equal(a.sorted.cpu().numpy(), sorted2.cpu().numpy())
+    assert np.array_equal(a.start.cpu().numpy(), start2.cpu().numpy())
+    st = a.start[n:cells].cpu().numpy()
+    assert (st >= 0).all() and (st < n).all()
+    assert np.array_equal(np.sort(a.sorted[:n].cpu().numpy()), np.arange(n))
