@@ -10,7 +10,9 @@
 //              group; bodies always interact.  Lanes decide up to 32 stack
 //              nodes at once and stage the interactions, 32 at a time.  The
 //              interaction set is the reference's; only the summation order
-//              differs.
+//              differs.  Without output positions (out.x null) it writes only
+//              the accelerations, in the caller's order (the drop-in's
+//              CalculateForces).
 // k_walk_acc   PLAIN / MIXED modes.  Lanes test up to 32 stack nodes at once
 //              against the group (geometric rule on the group's nearest body,
 //              relative rule on its |a_old|); accepted cells and the bodies of
@@ -540,7 +542,12 @@ static __global__ void __launch_bounds__(kVoteWarps * 32) k_walk_vote(Segs segs,
         if (overflow && lane == 0) atomicOr(status, ST_STACK);
         my_inter += (unsigned long long)(entries * cnt);
         float wl = 0.0f, wr = 0.0f, wb = 0.0f, wt = 0.0f;  // new positions' box, from the origin
-        if (valid) {
+        if (valid && !out.x) {
+            // forces only (the drop-in's CalculateForces, kernels.cu:340-435): the
+            // accelerations in the caller's order, id[] the caller index
+            out.ax[in.id[j]] = ax;
+            out.ay[in.id[j]] = ay;
+        } else if (valid) {
             // kernels.cu:529-533: v += dt*a; x += d*dt*v
             float vx = __fadd_rn(in.vx[j], __fmul_rn(dt, ax));
             float vy = __fadd_rn(in.vy[j], __fmul_rn(dt, ay));

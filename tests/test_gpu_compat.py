@@ -230,13 +230,13 @@ def test_unaligned_child_array(L):
 
 @pytest.mark.parametrize("n", [1 << 17, (1 << 18) + 333])
 def test_dropin_update_matches_reference_mode(L, n):
-    """The drop-in update() (reference layout, cooperative-grid SortParticles,
-    batched warp-vote CalculateForces) against the engine's REFERENCE mode on
-    the same Plummer state, two independent paths to the reference's step:
-    sorted[] equals the engine's permutation (both are the bodies in key
-    order), the forces agree to 1e-5 of their RMS (the same interaction set,
-    summed in another order), and the integrated positions to 1e-5 of their
-    extent."""
+    """The drop-in update() (the reference layout, with SortParticles and
+    CalculateForces taken from BuildQuadTree's workspace) against the engine's
+    REFERENCE mode on the same Plummer state (its own step, box, tree and
+    graph): sorted[] equals the engine's permutation (both are the bodies in
+    key order), the forces agree to 1e-5 of their RMS (the same interaction
+    set, summed in another order), and the integrated positions to 1e-5 of
+    their extent."""
     from stellarsolver_gb300 import bh, dropin, models
 
     x, y, vx, vy, m = models.plummer(n, 0x5EEDC0DE)
@@ -266,11 +266,14 @@ def test_dropin_update_matches_reference_mode(L, n):
 
 
 @pytest.mark.parametrize("case", ["plummer2048", "plummer2e17"])
-def test_sort_particles_from_build_equals_traversal(L, case):
-    """SortParticles right after BuildQuadTree on the same arrays takes sorted[]
-    and start[] from the build (depth-first order is key order); on a copy of
-    the built count[] and child[] at other addresses it walks the cells level by
-    level, as kernels.cu:299-335 does.  Both give the same arrays."""
+def test_sort_and_forces_from_build_equal_the_layout_walks(L, case):
+    """SortParticles and CalculateForces right after BuildQuadTree on the same
+    arrays work from the build: sorted[] and start[] (depth-first order is key
+    order), and the vote walk on its compressed tree.  On a copy of the built
+    count[] and child[] at other addresses they walk the reference's layout:
+    the cells level by level (kernels.cu:299-335), the vote over child[]
+    (kernels.cu:340-435).  The arrays are identical and the forces agree to
+    1e-5 of their RMS (the same interaction set, summed in another order)."""
     from stellarsolver_gb300 import dropin, models
 
     if case == "plummer2048":
@@ -293,8 +296,17 @@ def test_sort_particles_from_build_equals_traversal(L, case):
     sorted2 = a.sorted.clone()
     L.SortParticles(P(a.count), P(a.start), P(a.sorted), P(a.child), P(a.index), n)
     L.SortParticles(P(count2), P(start2), P(sorted2), P(child2), P(a.index), n)
+    ax2, ay2 = a.ax.clone(), a.ay.clone()
+    L.CalculateForces(P(a.x), P(a.y), P(a.vx), P(a.vy), P(a.ax), P(a.ay), P(a.mass), P(a.sorted),
+                      P(a.child), bx[0], bx[1], n, 1.0)
+    L.CalculateForces(P(a.x), P(a.y), P(a.vx), P(a.vy), P(ax2), P(ay2), P(a.mass), P(sorted2),
+                      P(child2), bx[0], bx[1], n, 1.0)
     torch.cuda.synchronize()
     assert L.bh_compat_status() == 0
+    f1 = np.stack([a.ax[:n].cpu().numpy(), a.ay[:n].cpu().numpy()]).astype(np.float64)
+    f2 = np.stack([ax2[:n].cpu().numpy(), ay2[:n].cpu().numpy()]).astype(np.float64)
+    rms = np.sqrt(np.mean(np.sum(f2 ** 2, axis=0)))
+    assert np.abs(f1 - f2).max() <= 1e-5 * rms
     cells = int(a.index.item())
     assert cells > n
     assert np.array_equal(a.sorted.cpu().numpy(), sorted2.cpu().numpy())
