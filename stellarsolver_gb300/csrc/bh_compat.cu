@@ -249,13 +249,17 @@ __global__ void k_c_setdraw(float* ptr, const float* x, const float* y, int n) {
 
 __global__ void k_c_reset(int* mutex, float* x, float* y, float* mass, int* count, int* start,
                           int* sorted, int* child, int* index, float* left, float* right,
-                          float* bottom, float* top, int n, int m) {
+                          float* bottom, float* top, int n, int m, int child16) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < m) {
-        child[4 * i] = -1;  // caller's pointer: no alignment assumed
-        child[4 * i + 1] = -1;
-        child[4 * i + 2] = -1;
-        child[4 * i + 3] = -1;
+        if (child16) {  // one 16-byte store when the caller's array allows it
+            reinterpret_cast<int4*>(child)[i] = make_int4(-1, -1, -1, -1);
+        } else {
+            child[4 * i] = -1;
+            child[4 * i + 1] = -1;
+            child[4 * i + 2] = -1;
+            child[4 * i + 3] = -1;
+        }
         if (i < n) {
             count[i] = 1;
         } else {
@@ -1071,9 +1075,10 @@ void compat_ResetArrays(int* mutex, float* x, float* y, float* mass, int* count,
         record(BH_ERR_ARG);
         return;
     }
+    const int child16 = (reinterpret_cast<uintptr_t>(child) & 15) == 0 ? 1 : 0;
     k_c_reset<<<blocks_for(m, 256), 256, 0, g_set.stream>>>(mutex, x, y, mass, count, start,
                                                             sorted, child, index, left, right,
-                                                            bottom, top, n, m);
+                                                            bottom, top, n, m, child16);
     record_cuda(cudaGetLastError(), "ResetArrays");
 }
 
