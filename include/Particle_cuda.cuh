@@ -55,11 +55,17 @@ void BuildQuadTree(float *x, float *y, float *mass, int *count, int *start, int 
 void ComputeCentreOfMass(float *x, float *y, float *mass, int *index, int n);
 
 /* Particle_cuda.cu:38-41 / kernels.cu:292-336: sorted[] = bodies in depth-first
- * order over child slots 0..3, start[cell] = first position of each cell. */
+ * order over child slots 0..3, start[cell] = first position of each cell.  On
+ * the arrays of the last BuildQuadTree on this device (same child array and
+ * n) both come from that build's workspace (depth-first order is its key
+ * order); otherwise the cells are walked level by level. */
 void SortParticles(int *count, int *start, int *sorted, int *child, int *index, int n);
 
 /* Particle_cuda.cu:44-47 / kernels.cu:340-435: warp-vote walk; g is unused,
- * as in the reference. */
+ * as in the reference.  Above 98,304 bodies, on the arrays of the last
+ * BuildQuadTree on this device, the walk runs on that build's compressed tree
+ * (the same interaction set; forces equal to 1e-5 of their RMS, the summation
+ * order differs); otherwise it walks child[]. */
 void CalculateForces(float *x, float *y, float *vx, float *vy, float *ax, float *ay, float *mass,
                      int *sorted, int *child, float *left, float *right, int n, float g);
 
