@@ -991,7 +991,8 @@ cudaError_t enqueue_build(Workspace& w, float* x, float* y, float* mass, int* co
                    (const uint32_t*)w.vals3, w.keys_alt, w.vals_alt, w.overflow,
                    (cudaGraphConditionalHandle)0, 0, (int*)nullptr, 0);
     if (e != cudaSuccess) return e;
-    {
+    if (!launch_full_sort_grid(w.keys, w.vals, w.keys_alt, w.vals_alt, w.keys3, w.vals3, n, w.hist,
+                               w.totals, tiles, w.overflow, st, &e)) {
         const uint64_t* ki = w.keys;
         const uint32_t* vi = w.vals;
         for (int ps = 0; ps < 8; ++ps) {
@@ -1003,6 +1004,7 @@ cudaError_t enqueue_build(Workspace& w, float* x, float* y, float* mass, int* co
             vi = vo;
         }
     }
+    if (e != cudaSuccess) return e;
     uint64_t* ka = w.keys_alt;
     uint32_t* va = w.vals_alt;
     k_c_gather3<<<nb, 256, 0, st>>>(n, va, x, y, mass, w.sx, w.sy, w.sm);

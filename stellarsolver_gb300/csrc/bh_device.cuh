@@ -18,9 +18,11 @@
 // last position is unused.  A child reference >= 0 is a node, < 0 is ~body.
 #pragma once
 
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <climits>
 
 namespace ssg {
@@ -342,20 +344,21 @@ static_assert(kSortThreads == 256, "one thread per digit in the sort kernels");
 // (twice as fast as aggregating equal digits with warp votes first).
 // The three pass kernels take `only_if`: when non-null they do nothing unless
 // *only_if is set (the fallback full sort of k_sort_fixup's overflow).
-static __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint64_t* __restrict__ keys,
-                                                             const uint32_t* __restrict__ vals, int n,
-                                                             int shift, int use_seg,
-                                                             const int* __restrict__ seg_of_pos,
-                                                             uint32_t* __restrict__ hist, int tiles,
-                                                             const int* __restrict__ only_if) {
-    pdl_wait();
-    if (only_if && *only_if == 0) return;
+// The three kernels of a pass are bodies over one tile (or one digit), so that
+// the full sort's cooperative kernel (k_full_sort_grid) runs the same code.
+// Each body starts with a block barrier: a block that loops over several tiles
+// must not reset its shared arrays while a slower thread still reads them.
+__device__ __forceinline__ void radix_hist_tile(int tile, const uint64_t* __restrict__ keys,
+                                                const uint32_t* __restrict__ vals, int n, int shift,
+                                                int use_seg, const int* __restrict__ seg_of_pos,
+                                                uint32_t* __restrict__ hist, int tiles) {
     constexpr int W = kSortThreads / 32;
     __shared__ uint32_t s_h[W][256];
+    __syncthreads();
     for (int i = threadIdx.x; i < W * 256; i += kSortThreads) (&s_h[0][0])[i] = 0u;
     __syncthreads();
     const int warp = threadIdx.x >> 5;
-    const int base = blockIdx.x * kSortTile;
+    const int base = tile * kSortTile;
     uint32_t dg[kSortItems];
 #pragma unroll
     for (int it = 0; it < kSortItems; ++it) {
@@ -371,17 +374,26 @@ static __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint64
     uint32_t t = 0;
 #pragma unroll
     for (int w = 0; w < W; ++w) t += s_h[w][threadIdx.x];
-    hist[threadIdx.x * tiles + blockIdx.x] = t;
+    hist[threadIdx.x * tiles + tile] = t;
 }
 
-// block d turns column d of hist into exclusive offsets; totals[d] = column sum
-static __global__ void __launch_bounds__(kSortThreads) k_radix_scan(uint32_t* __restrict__ hist, int tiles,
-                                                             uint32_t* __restrict__ totals,
+static __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint64_t* __restrict__ keys,
+                                                             const uint32_t* __restrict__ vals, int n,
+                                                             int shift, int use_seg,
+                                                             const int* __restrict__ seg_of_pos,
+                                                             uint32_t* __restrict__ hist, int tiles,
                                                              const int* __restrict__ only_if) {
     pdl_wait();
     if (only_if && *only_if == 0) return;
+    radix_hist_tile(blockIdx.x, keys, vals, n, shift, use_seg, seg_of_pos, hist, tiles);
+}
+
+// digit d: column d of hist into exclusive offsets; totals[d] = column sum
+__device__ __forceinline__ void radix_scan_digit(int d, uint32_t* __restrict__ hist, int tiles,
+                                                 uint32_t* __restrict__ totals) {
     __shared__ uint32_t s_tmp[kSortThreads / 32];
-    uint32_t* col = hist + (size_t)blockIdx.x * tiles;
+    __syncthreads();
+    uint32_t* col = hist + (size_t)d * tiles;
     uint32_t running = 0;
     for (int base = 0; base < tiles; base += kSortThreads) {
         int i = base + threadIdx.x;
@@ -391,7 +403,15 @@ static __global__ void __launch_bounds__(kSortThreads) k_radix_scan(uint32_t* __
         if (i < tiles) col[i] = running + ex;
         running += tot;
     }
-    if (threadIdx.x == 0) totals[blockIdx.x] = running;
+    if (threadIdx.x == 0) totals[d] = running;
+}
+
+static __global__ void __launch_bounds__(kSortThreads) k_radix_scan(uint32_t* __restrict__ hist, int tiles,
+                                                             uint32_t* __restrict__ totals,
+                                                             const int* __restrict__ only_if) {
+    pdl_wait();
+    if (only_if && *only_if == 0) return;
+    radix_scan_digit(blockIdx.x, hist, tiles, totals);
 }
 
 // Lanes of the warp holding the same 8-bit digit as this lane (valid lanes
@@ -411,13 +431,11 @@ __device__ __forceinline__ unsigned digit_peers(uint32_t d, bool valid) {
 // (earlier rounds of the warp) + (lower lanes with the same digit); warps are
 // then offset by the counts of lower warps.  Elements are staged in shared
 // memory in digit order and written out as contiguous runs.
-static __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(
-    const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
-    uint32_t* __restrict__ vout, int n, int shift, int use_seg, const int* __restrict__ seg_of_pos,
-    const uint32_t* __restrict__ hist, const uint32_t* __restrict__ totals, int tiles,
-    const int* __restrict__ only_if) {
-    pdl_wait();
-    if (only_if && *only_if == 0) return;
+__device__ __forceinline__ void radix_scatter_tile(
+    int tile, const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+    uint64_t* __restrict__ kout, uint32_t* __restrict__ vout, int n, int shift, int use_seg,
+    const int* __restrict__ seg_of_pos, const uint32_t* __restrict__ hist,
+    const uint32_t* __restrict__ totals, int tiles) {
     constexpr int W = kSortThreads / 32;
     constexpr int WCHUNK = 32 * kSortItems;
     __shared__ uint32_t s_wh[W][256];
@@ -427,14 +445,15 @@ static __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(
     __shared__ uint64_t s_k[kSortTile];
     __shared__ uint32_t s_v[kSortTile];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    __syncthreads();
     for (int i = tid; i < W * 256; i += kSortThreads) (&s_wh[0][0])[i] = 0u;
     {
         uint32_t tot;
         uint32_t ex = block_excl_scan<kSortThreads>(totals[tid], &tot, s_tmp);
-        s_gbase[tid] = ex + hist[(size_t)tid * tiles + blockIdx.x];
+        s_gbase[tid] = ex + hist[(size_t)tid * tiles + tile];
     }
     __syncthreads();
-    const int base = blockIdx.x * kSortTile;
+    const int base = tile * kSortTile;
     uint64_t k[kSortItems];
     uint32_t v[kSortItems];
     uint32_t rank[kSortItems];
@@ -492,6 +511,17 @@ static __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(
     }
 }
 
+static __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(
+    const uint64_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint64_t* __restrict__ kout,
+    uint32_t* __restrict__ vout, int n, int shift, int use_seg, const int* __restrict__ seg_of_pos,
+    const uint32_t* __restrict__ hist, const uint32_t* __restrict__ totals, int tiles,
+    const int* __restrict__ only_if) {
+    pdl_wait();
+    if (only_if && *only_if == 0) return;
+    radix_scatter_tile(blockIdx.x, kin, vin, kout, vout, n, shift, use_seg, seg_of_pos, hist, totals,
+                       tiles);
+}
+
 // The sort's fast path: P stable 8-bit passes over the key's top 8P bits (the
 // high word, bits `shift` = 64 - 8P .. 63), then k_sort_fixup.  Elements with
 // equal high words then form runs in input order; each run is put in
@@ -543,6 +573,67 @@ static __global__ void k_sort_fixup(int n, int shift, const uint64_t* __restrict
     }
     kout[a + rank] = k;
     vout[a + rank] = vin[i];
+}
+
+// The full sort (the fast path's fallback, when *only_if is set) as one
+// cooperative kernel: the eight 8-bit passes k0 -> kB -> kA -> ... -> kA of the
+// 24 pass kernels, every block looping over tiles and digits, a grid barrier
+// between the phases.  Every block returns at once when the flag is clear: one
+// launch where the stream-ordered fallback took 24 (about 1 us each on GB300
+// when they return at once).
+static __global__ void __launch_bounds__(kSortThreads) k_full_sort_grid(
+    const uint64_t* __restrict__ k0, const uint32_t* __restrict__ v0, uint64_t* __restrict__ kA,
+    uint32_t* __restrict__ vA, uint64_t* __restrict__ kB, uint32_t* __restrict__ vB, int n,
+    uint32_t* __restrict__ hist, uint32_t* __restrict__ totals, int tiles,
+    const int* __restrict__ only_if) {
+    pdl_wait();
+    if (*only_if == 0) return;
+    cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+    const uint64_t* ki = k0;
+    const uint32_t* vi = v0;
+    for (int ps = 0; ps < 8; ++ps) {
+        uint64_t* ko = (ps & 1) ? kA : kB;
+        uint32_t* vo = (ps & 1) ? vA : vB;
+        for (int t = blockIdx.x; t < tiles; t += gridDim.x)
+            radix_hist_tile(t, ki, vi, n, 8 * ps, 0, nullptr, hist, tiles);
+        grid.sync();
+        for (int d = blockIdx.x; d < 256; d += gridDim.x) radix_scan_digit(d, hist, tiles, totals);
+        grid.sync();
+        for (int t = blockIdx.x; t < tiles; t += gridDim.x)
+            radix_scatter_tile(t, ki, vi, ko, vo, n, 8 * ps, 0, nullptr, hist, totals, tiles);
+        grid.sync();
+        ki = ko;
+        vi = vo;
+    }
+}
+
+// Launch k_full_sort_grid over the resident grid of the current device; false
+// when no cooperative grid can be formed (the caller launches the 24 kernels).
+static bool launch_full_sort_grid(const uint64_t* k0, const uint32_t* v0, uint64_t* kA,
+                                  uint32_t* vA, uint64_t* kB, uint32_t* vB, int n, uint32_t* hist,
+                                  uint32_t* totals, int tiles, const int* only_if,
+                                  cudaStream_t st, cudaError_t* err) {
+    constexpr int kDevs = 64;
+    static std::atomic<int> s_grid[kDevs] = {};  // resident blocks per device, read once
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kDevs) return false;
+    int grid = s_grid[dev].load();
+    if (grid == 0) {
+        int bps = 0, sms = 0, coop = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_full_sort_grid, kSortThreads, 0) !=
+                cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess)
+            bps = 0;
+        grid = (coop && bps > 0 && sms > 0) ? bps * sms : -1;
+        s_grid[dev] = grid;
+    }
+    if (grid < 1) return false;
+    void* args[] = {(void*)&k0, (void*)&v0, (void*)&kA, (void*)&vA, (void*)&kB, (void*)&vB,
+                    (void*)&n, (void*)&hist, (void*)&totals, (void*)&tiles, (void*)&only_if};
+    *err = cudaLaunchCooperativeKernel((const void*)k_full_sort_grid, grid, kSortThreads, args, 0,
+                                       st);
+    return true;
 }
 
 // ------------------------------------------------------------------ (d) reorder

@@ -468,7 +468,13 @@ int enqueue_sort(bh_system* s, cudaStream_t st, cudaEvent_t* ev, bool keep_stats
         if (e != cudaSuccess) return cuda_fail(e, "conditional sort body");
         if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamEndCapture (sort body)");
     } else {
-        CK(full_sort(pdl, st, overflow));
+        // stream order: one cooperative kernel that returns at once unless the
+        // fixup set the flag (the 24 flag-gated kernels where none can be formed)
+        cudaError_t e = cudaSuccess;
+        if (!launch_full_sort_grid(k0, v0, kA, vA, kB, vB, n, s->hist, s->totals, s->tiles, overflow,
+                                   st, &e))
+            e = full_sort(pdl, st, overflow);
+        CK(e);
     }
     uint64_t *ka = kA, *kb = kB;
     uint32_t *va = vA, *vb = vB;

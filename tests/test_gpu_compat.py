@@ -314,3 +314,42 @@ def test_sort_and_forces_from_build_equal_the_layout_walks(L, case):
     st = a.start[n:cells].cpu().numpy()
     assert (st >= 0).all() and (st < n).all()
     assert np.array_equal(np.sort(a.sorted[:n].cpu().numpy()), np.arange(n))
+
+
+@pytest.mark.parametrize("packed", [0, 600])
+def test_build_with_the_full_sort(L, oracle, packed):
+    """600 bodies 1e-8 apart in one 2^-12 cell of the box make a run of equal
+    high key words longer than the fixup orders, so BuildQuadTree takes the
+    full 8-pass sort (one cooperative kernel; with `packed` 0 it returns at
+    once).  sorted[] equals the oracle's stable sort of the keys either way."""
+    from stellarsolver_gb300 import dropin
+
+    n = 8192
+    rng = np.random.default_rng(31 + packed)
+    x = rng.standard_normal(n).astype(np.float32)
+    y = rng.standard_normal(n).astype(np.float32)
+    i = np.arange(packed)
+    x[:packed] = np.float32(1e-3) + (i * 1e-8).astype(np.float32)
+    y[:packed] = np.float32(2e-3) + ((i % 7) * 1e-8).astype(np.float32)
+    perm = rng.permutation(n)
+    x, y = x[perm], y[perm]
+    m = np.full(n, 1.0 / n, np.float32)
+    z = np.zeros(n, np.float32)
+    box = oracle.bbox(x, y)
+    k = oracle.keys(x, y, box)
+    _, runs = np.unique(k >> np.uint64(40), return_counts=True)
+    assert (runs.max() > 256) == (packed > 0)
+    want, _ = oracle.sort_keys(k)
+    a = dropin.RefArrays(torch, x, y, z, z, m)
+    bx = [P(b) for b in a.box]
+    L.bh_compat_clear_status()
+    L.ResetArrays(P(a.mutex), P(a.x), P(a.y), P(a.mass), P(a.count), P(a.start), P(a.sorted),
+                  P(a.child), P(a.index), *bx, n, a.m)
+    L.ComputeBoundingBox(P(a.mutex), P(a.x), P(a.y), *bx, n)
+    L.BuildQuadTree(P(a.x), P(a.y), P(a.mass), P(a.count), P(a.start), P(a.child), P(a.index),
+                    *bx, n, a.m)
+    L.ComputeCentreOfMass(P(a.x), P(a.y), P(a.mass), P(a.index), n)
+    L.SortParticles(P(a.count), P(a.start), P(a.sorted), P(a.child), P(a.index), n)
+    torch.cuda.synchronize()
+    assert L.bh_compat_status() == 0
+    assert np.array_equal(a.sorted[:n].cpu().numpy(), want.astype(np.int32))
