@@ -240,6 +240,7 @@ int blocks_for(long long n, int t) { return (int)std::max<long long>(1, (n + t -
 // ------------------------------------------------------------------ simple kernels
 
 __global__ void k_c_setdraw(float* ptr, const float* x, const float* y, int n) {
+    pdl_wait();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
         ptr[2 * i] = x[i];
@@ -250,6 +251,7 @@ __global__ void k_c_setdraw(float* ptr, const float* x, const float* y, int n) {
 __global__ void k_c_reset(int* mutex, float* x, float* y, float* mass, int* count, int* start,
                           int* sorted, int* child, int* index, float* left, float* right,
                           float* bottom, float* top, int n, int m, int child16) {
+    pdl_wait();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < m) {
         if (child16) {  // one 16-byte store when the caller's array allows it
@@ -297,6 +299,7 @@ __device__ __forceinline__ void atomic_max_f(float* a, float v) {
 __global__ void __launch_bounds__(256) k_c_bbox(const float* x, const float* y, int n, float* left,
                                                 float* right, float* bottom, float* top,
                                                 int* status) {
+    pdl_wait();
     float l = x[0], r = x[0], b = y[0], t = y[0];
     bool bad = false;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -343,7 +346,10 @@ __global__ void __launch_bounds__(256) k_c_bbox(const float* x, const float* y, 
 }
 
 __global__ void k_c_box_to_ord(const float* left, const float* right, const float* bottom,
-                               const float* top, int* box_ord, int* seg_off, int n) {
+                               const float* top, int* box_ord, int* seg_off, int n,
+                               int* overflow) {
+    pdl_wait();
+    *overflow = 0;  // the sort's run overflow flag of this build
     box_ord[0] = f2ord(*left);
     box_ord[1] = f2ord(*right);
     box_ord[2] = f2ord(*bottom);
@@ -353,9 +359,11 @@ __global__ void k_c_box_to_ord(const float* left, const float* right, const floa
 }
 
 __global__ void k_c_gather3(int n, const uint32_t* perm, const float* x, const float* y,
-                            const float* m, float* sx, float* sy, float* sm) {
+                            const float* m, float* sx, float* sy, float* sm, int* counter) {
+    pdl_wait();
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j < n) {
+        counter[j] = 0;  // the moments' arrival counters
         uint32_t i = perm[j];
         sx[j] = x[i];
         sy[j] = y[i];
@@ -366,6 +374,7 @@ __global__ void k_c_gather3(int n, const uint32_t* perm, const float* x, const f
 // cells of the reference tree owned by each branching node: its chain of
 // single-child cells and itself (the root node owns levels 1..L)
 __global__ void k_c_ncells(int n, const int* split, const int* parent, int* ncell) {
+    pdl_wait();
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
     int sp = split[q], c = 0;
@@ -381,6 +390,7 @@ __global__ void k_c_ncells(int n, const int* split, const int* parent, int* ncel
 
 // exclusive scan of n ints in blocks of 1024
 __global__ void __launch_bounds__(1024) k_c_scan_block(const int* in, int* out, int* bsum, int n) {
+    pdl_wait();
     __shared__ uint32_t tmp[32];
     int i = blockIdx.x * 1024 + threadIdx.x;
     uint32_t v = i < n ? (uint32_t)in[i] : 0u;
@@ -391,6 +401,7 @@ __global__ void __launch_bounds__(1024) k_c_scan_block(const int* in, int* out, 
 }
 
 __global__ void __launch_bounds__(1024) k_c_scan_top(int* bsum, int nb, int* total) {
+    pdl_wait();
     __shared__ uint32_t tmp[32];
     uint32_t run = 0;
     for (int base = 0; base < nb; base += 1024) {
@@ -405,6 +416,7 @@ __global__ void __launch_bounds__(1024) k_c_scan_top(int* bsum, int nb, int* tot
 }
 
 __global__ void k_c_scan_add(int* out, const int* bsum, int n) {
+    pdl_wait();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] += bsum[i / 1024];
 }
@@ -417,6 +429,7 @@ __global__ void k_c_materialize(int n, int m, TreePtrs t, const uint64_t* skeys,
                                 const uint32_t* perm, const int* cbase, const int* total,
                                 NodeSums sums, int* child, int* count, int* start, float* x,
                                 float* y, float* mass, int* index, int* status) {
+    pdl_wait();
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
     const int tot = *total;
@@ -484,6 +497,7 @@ __global__ void k_c_materialize(int n, int m, TreePtrs t, const uint64_t* skeys,
 // same guards as k_c_materialize: nothing for cells it did not make.
 __global__ void k_c_sort_from_build(int n, int m, TreePtrs t, const uint32_t* perm,
                                     const int* cbase, const int* total, int* start, int* sorted) {
+    pdl_wait();
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
     sorted[q] = (int)perm[q];
@@ -500,6 +514,7 @@ __global__ void k_c_sort_from_build(int n, int m, TreePtrs t, const uint32_t* pe
 }
 
 __global__ void k_c_com(float* x, float* y, const float* mass, const int* index, int n) {
+    pdl_wait();
     int end = *index;
     for (int i = n + blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
         x[i] = __fdiv_rn(x[i], mass[i]);  // kernels.cu:283-284
@@ -710,6 +725,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_c_forces_vote(
     const int* __restrict__ sorted, const int* __restrict__ child, const float* left,
     const float* right, int n, int mlimit, float theta, float eps2, float* ax, float* ay,
     int* status) {
+    pdl_wait();
     __shared__ int s_node[WARPS][STACK];
     __shared__ float s_dp[WARPS][STACK];
     __shared__ float4 s_stage[WARPS][32];
@@ -911,6 +927,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_c_forces_vote(
 
 __global__ void k_c_integrate(float* x, float* y, float* vx, float* vy, const float* ax,
                               const float* ay, int n, float dt, float ddt) {
+    pdl_wait();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
         float v = __fadd_rn(vx[i], __fmul_rn(dt, ax[i]));  // kernels.cu:529-533
@@ -946,13 +963,12 @@ int fetch_status(Workspace* w) {
 cudaError_t enqueue_build(Workspace& w, float* x, float* y, float* mass, int* count, int* start,
                           int* child, int* index, float* left, float* right, float* bottom,
                           float* top, int n, int m, cudaStream_t st) {
-    cudaError_t e = cudaMemsetAsync(w.counter, 0, sizeof(int) * n, st);  // moments' arrivals
-    if (e != cudaSuccess) return e;
     const int nb = blocks_for(n, 256);
-    k_c_box_to_ord<<<1, 1, 0, st>>>(left, right, bottom, top, w.box_ord, w.seg_off, n);
-    Segs segs{1, w.seg_off, nullptr};
-    e = cudaMemsetAsync(w.overflow, 0, sizeof(int), st);
+    cudaError_t e = launch_pdl(k_c_box_to_ord, 1, 1, 0, st, (const float*)left, (const float*)right,
+                               (const float*)bottom, (const float*)top, w.box_ord, w.seg_off, n,
+                               w.overflow);
     if (e != cudaSuccess) return e;
+    Segs segs{1, w.seg_off, nullptr};
     // the kernels that wait for their predecessor (pdl_wait) are launched with
     // programmatic serialisation: each one's launch overlaps the previous one's
     // tail, which matters for the flag-gated full sort that returns at once
@@ -1007,22 +1023,30 @@ cudaError_t enqueue_build(Workspace& w, float* x, float* y, float* mass, int* co
     if (e != cudaSuccess) return e;
     uint64_t* ka = w.keys_alt;
     uint32_t* va = w.vals_alt;
-    k_c_gather3<<<nb, 256, 0, st>>>(n, va, x, y, mass, w.sx, w.sy, w.sm);
-    e = launch_pdl(k_build, nb, 256, 0, st, (const uint64_t*)ka, n, segs, w.tree, w.status);
+    e = launch_pdl(k_c_gather3, nb, 256, 0, st, n, (const uint32_t*)va, (const float*)x,
+                   (const float*)y, (const float*)mass, w.sx, w.sy, w.sm, w.counter);
+    if (e == cudaSuccess)
+        e = launch_pdl(k_build, nb, 256, 0, st, (const uint64_t*)ka, n, segs, w.tree, w.status);
     if (e == cudaSuccess)
         e = launch_pdl(k_moments, (n + kMomentsThreads - 1) / kMomentsThreads, kMomentsThreads, 0,
                        st, n, 0, (const float*)w.sx, (const float*)w.sy, (const float*)w.sm,
                        (const int4*)w.tree.climb, (const int*)w.tree.leaf_parent, w.counter, w.sums,
                        w.status);
     if (e != cudaSuccess) return e;
-    k_c_ncells<<<nb, 256, 0, st>>>(n, w.tree.split, w.tree.parent, w.ncell);
+    // the cell numbering and the reference layout, each kernel launched while
+    // its predecessor drains (pdl_wait)
     const int sb = blocks_for(n, 1024);
-    k_c_scan_block<<<sb, 1024, 0, st>>>(w.ncell, w.cbase, w.bsum, n);
-    k_c_scan_top<<<1, 1024, 0, st>>>(w.bsum, sb, w.total);
-    k_c_scan_add<<<nb, 256, 0, st>>>(w.cbase, w.bsum, n);
-    k_c_materialize<<<nb, 256, 0, st>>>(n, m, w.tree, ka, va, w.cbase, w.total, w.sums, child,
-                                        count, start, x, y, mass, index, w.status);
-    return cudaGetLastError();
+    e = launch_pdl(k_c_ncells, nb, 256, 0, st, n, (const int*)w.tree.split,
+                   (const int*)w.tree.parent, w.ncell);
+    if (e == cudaSuccess)
+        e = launch_pdl(k_c_scan_block, sb, 1024, 0, st, (const int*)w.ncell, w.cbase, w.bsum, n);
+    if (e == cudaSuccess) e = launch_pdl(k_c_scan_top, 1, 1024, 0, st, w.bsum, sb, w.total);
+    if (e == cudaSuccess) e = launch_pdl(k_c_scan_add, nb, 256, 0, st, w.cbase, (const int*)w.bsum, n);
+    if (e == cudaSuccess)
+        e = launch_pdl(k_c_materialize, nb, 256, 0, st, n, m, w.tree, (const uint64_t*)ka,
+                       (const uint32_t*)va, (const int*)w.cbase, (const int*)w.total, w.sums, child,
+                       count, start, x, y, mass, index, w.status);
+    return e;
 }
 
 }  // namespace
@@ -1066,8 +1090,9 @@ namespace ssg {
 
 void compat_SetDrawArray(float* ptr, float* x, float* y, int n) {
     if (n <= 0) return;
-    k_c_setdraw<<<blocks_for(n, 256), 256, 0, g_set.stream>>>(ptr, x, y, n);
-    record_cuda(cudaGetLastError(), "SetDrawArray");
+    record_cuda(launch_pdl(k_c_setdraw, blocks_for(n, 256), 256, 0, g_set.stream, ptr,
+                           (const float*)x, (const float*)y, n),
+                "SetDrawArray");
 }
 
 void compat_ResetArrays(int* mutex, float* x, float* y, float* mass, int* count, int* start, int* sorted,
@@ -1078,10 +1103,10 @@ void compat_ResetArrays(int* mutex, float* x, float* y, float* mass, int* count,
         return;
     }
     const int child16 = (reinterpret_cast<uintptr_t>(child) & 15) == 0 ? 1 : 0;
-    k_c_reset<<<blocks_for(m, 256), 256, 0, g_set.stream>>>(mutex, x, y, mass, count, start,
-                                                            sorted, child, index, left, right,
-                                                            bottom, top, n, m, child16);
-    record_cuda(cudaGetLastError(), "ResetArrays");
+    record_cuda(launch_pdl(k_c_reset, blocks_for(m, 256), 256, 0, g_set.stream, mutex, x, y, mass,
+                           count, start, sorted, child, index, left, right, bottom, top, n, m,
+                           child16),
+                "ResetArrays");
 }
 
 void compat_ComputeBoundingBox(int* mutex, float* x, float* y, float* left, float* right, float* bottom,
@@ -1097,8 +1122,9 @@ void compat_ComputeBoundingBox(int* mutex, float* x, float* y, float* left, floa
         return;
     }
     int blocks = std::min(blocks_for(n, 256), 1024);
-    k_c_bbox<<<blocks, 256, 0, g_set.stream>>>(x, y, n, left, right, bottom, top, w->status);
-    record_cuda(cudaGetLastError(), "ComputeBoundingBox");
+    record_cuda(launch_pdl(k_c_bbox, blocks, 256, 0, g_set.stream, (const float*)x, (const float*)y,
+                           n, left, right, bottom, top, w->status),
+                "ComputeBoundingBox");
 }
 
 void compat_BuildQuadTree(float* x, float* y, float* mass, int* count, int* start, int* child, int* index,
@@ -1122,8 +1148,9 @@ void compat_BuildQuadTree(float* x, float* y, float* mass, int* count, int* star
 }
 
 void compat_ComputeCentreOfMass(float* x, float* y, float* mass, int* index, int n) {
-    k_c_com<<<1024, 256, 0, g_set.stream>>>(x, y, mass, index, n);
-    record_cuda(cudaGetLastError(), "ComputeCentreOfMass");
+    record_cuda(launch_pdl(k_c_com, 1024, 256, 0, g_set.stream, x, y, (const float*)mass,
+                           (const int*)index, n),
+                "ComputeCentreOfMass");
 }
 
 void compat_SortParticles(int* count, int* start, int* sorted, int* child, int* index, int n) {
@@ -1143,9 +1170,10 @@ void compat_SortParticles(int* count, int* start, int* sorted, int* child, int* 
         }
         if (b.child == child && b.n == n && b.w && b.w->base && b.w->gen == b.gen) {
             const Workspace& w = *b.w;
-            k_c_sort_from_build<<<blocks_for(n, 256), 256, 0, g_set.stream>>>(
-                n, b.m, w.tree, w.vals_alt, w.cbase, w.total, start, sorted);
-            record_cuda(cudaGetLastError(), "SortParticles");
+            record_cuda(launch_pdl(k_c_sort_from_build, blocks_for(n, 256), 256, 0, g_set.stream, n,
+                                   b.m, w.tree, (const uint32_t*)w.vals_alt, (const int*)w.cbase,
+                                   (const int*)w.total, start, sorted),
+                        "SortParticles");
             return;
         }
     }
@@ -1215,9 +1243,11 @@ void compat_CalculateForces(float* x, float* y, float* vx, float* vy, float* ax,
             cudaStream_t st = g_set.stream;
             const Segs segs{1, w.seg_off, nullptr};
             const int nb = blocks_for(n, 256);
-            k_records<<<nb, 256, 0, st>>>(n, segs, 0, g_set.theta, 1.0f, (const int*)w.box_ord,
-                                          (const uint64_t*)w.keys_alt, w.tree, w.sums, w.rec);
             cudaError_t e = cudaMemsetAsync(w.work, 0, sizeof(int), st);
+            if (e == cudaSuccess)
+                e = launch_pdl(k_records, nb, 256, 0, st, n, segs, 0, g_set.theta, 1.0f,
+                               (const int*)w.box_ord, (const uint64_t*)w.keys_alt, w.tree, w.sums,
+                               w.rec);
             if (e == cudaSuccess) {
                 const WalkIn in{w.sx, w.sy, nullptr, nullptr, w.sm, nullptr, nullptr,
                                 reinterpret_cast<const int*>(w.vals_alt), nullptr, nullptr};
@@ -1227,10 +1257,9 @@ void compat_CalculateForces(float* x, float* y, float* vx, float* vy, float* ax,
                 const Groups gr{(n + 31) / 32, nullptr};
                 const int blocks =
                     std::min(blocks_for(gr.ngroups, kVoteWarps), 16 * device_sms());
-                k_walk_vote<<<blocks, kVoteWarps * 32, 0, st>>>(
-                    segs, gr, in, (const float4*)w.rec.A, (const int4*)w.rec.C, g_set.eps2, 0.0f,
-                    0.0f, out, w.status, w.inter, w.work);
-                e = cudaGetLastError();
+                e = launch_pdl(k_walk_vote, blocks, kVoteWarps * 32, 0, st, segs, gr, in,
+                               (const float4*)w.rec.A, (const int4*)w.rec.C, g_set.eps2, 0.0f, 0.0f,
+                               out, w.status, w.inter, w.work);
             }
             record_cuda(e, "CalculateForces");
             return;
@@ -1245,24 +1274,26 @@ void compat_CalculateForces(float* x, float* y, float* vx, float* vy, float* ax,
     constexpr int W = 4, S = 1024;
     // a grid-stride loop over the warp groups: at most 16 blocks per SM
     int blocks = std::min(blocks_for((n + 31) / 32, W), 16 * device_sms());
-    k_c_forces_vote<W, S><<<blocks, W * 32, 0, g_set.stream>>>(x, y, mass, sorted, child, left,
-                                                             right, n, mlimit, g_set.theta,
-                                                             g_set.eps2, ax, ay, w->status);
-    record_cuda(cudaGetLastError(), "CalculateForces");
+    record_cuda(launch_pdl(k_c_forces_vote<W, S>, blocks, W * 32, 0, g_set.stream, (const float*)x,
+                           (const float*)y, (const float*)mass, (const int*)sorted,
+                           (const int*)child, (const float*)left, (const float*)right, n, mlimit,
+                           g_set.theta, g_set.eps2, ax, ay, w->status),
+                "CalculateForces");
 }
 
 void compat_IntegrateParticles(float* x, float* y, float* vx, float* vy, float* ax, float* ay, int n,
                         float dt, float d) {
     if (n <= 0) return;
-    k_c_integrate<<<blocks_for(n, 256), 256, 0, g_set.stream>>>(x, y, vx, vy, ax, ay, n, dt,
-                                                                d * dt);
-    record_cuda(cudaGetLastError(), "IntegrateParticles");
+    record_cuda(launch_pdl(k_c_integrate, blocks_for(n, 256), 256, 0, g_set.stream, x, y, vx, vy,
+                           (const float*)ax, (const float*)ay, n, dt, d * dt),
+                "IntegrateParticles");
 }
 
 void compat_FillOutputArray(float* x, float* y, float* out, int n) {
     if (n <= 0) return;
-    k_c_setdraw<<<blocks_for(n, 256), 256, 0, g_set.stream>>>(out, x, y, n);
-    record_cuda(cudaGetLastError(), "FillOutputArray");
+    record_cuda(launch_pdl(k_c_setdraw, blocks_for(n, 256), 256, 0, g_set.stream, out,
+                           (const float*)x, (const float*)y, n),
+                "FillOutputArray");
 }
 
 }  // namespace ssg
