@@ -349,7 +349,7 @@ __global__ void k_c_box_to_ord(const float* left, const float* right, const floa
                                const float* top, int* box_ord, int* seg_off, int n,
                                int* overflow) {
     pdl_wait();
-    *overflow = 0;  // the sort's run overflow flag of this build
+    *overflow = 0;  // the run overflow flag of the sort that follows
     box_ord[0] = f2ord(*left);
     box_ord[1] = f2ord(*right);
     box_ord[2] = f2ord(*bottom);
@@ -1133,7 +1133,7 @@ void compat_BuildQuadTree(float* x, float* y, float* mass, int* count, int* star
         record(BH_ERR_ARG);
         return;
     }
-    set_built(Built{});  // until this build is enqueued
+    set_built(Built{});  // none until the tree below is enqueued
     if (n == 1) return;  // a lone body: no cells, *index stays n
     Workspace* w = workspace((size_t)n, (size_t)m);
     if (!w) {
