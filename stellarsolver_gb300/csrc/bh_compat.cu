@@ -221,10 +221,10 @@ Workspace* workspace(size_t n, size_t m) {
     w->qa = (int*)take(4 * M);
     w->qb = (int*)take(4 * M);
     w->qcount = (int*)take(12);
-    w->rec.A = (float4*)take(16 * N);
+    w->rec.A = (float4*)take(16 * kRecStride * N);  // A and D interleaved
     w->rec.B = nullptr;
     w->rec.C = (int4*)take(16 * N);
-    w->rec.D = (int4*)take(16 * N);
+    w->rec.D = reinterpret_cast<int4*>(w->rec.A) + 1;
     w->inter = (unsigned long long*)take(8);
     w->work = (int*)take(4);
     w->status = (int*)take(4);

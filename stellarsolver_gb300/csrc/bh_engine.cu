@@ -923,10 +923,10 @@ int system_create(const bh_params* p, const int* sizes, int nseg, int device, bh
     s->tree.climb = carve<int4>(c, N);
     s->sums.s0 = carve<float4>(c, N);
     s->sums.s1 = carve<float4>(c, N);
-    s->rec.A = carve<float4>(c, N);
+    s->rec.A = carve<float4>(c, kRecStride * N);  // A and D interleaved
     s->rec.B = carve<float4>(c, N);
     s->rec.C = carve<int4>(c, N);
-    s->rec.D = carve<int4>(c, N);
+    s->rec.D = reinterpret_cast<int4*>(s->rec.A) + 1;
     s->ax = carve<float>(c, N);
     s->ay = carve<float>(c, N);
     s->status = carve<int>(c, 1);

@@ -441,7 +441,7 @@ static __global__ void __launch_bounds__(kVoteWarps * 32) k_walk_vote(Segs segs,
         auto flush_cells = [&](int k) {  // the last k entries of clist
             __syncwarp();
             if (lane < k) {
-                const float4 A = recA[clist[ccnt - k + lane]];
+                const float4 A = recA[kRecStride * (clist[ccnt - k + lane])];
                 stage[lane] = make_float4(A.x, A.y, A.z, 0.0f);
             }
             __syncwarp();
@@ -478,7 +478,7 @@ static __global__ void __launch_bounds__(kVoteWarps * 32) k_walk_vote(Segs segs,
             float4 A = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             bool acc = false, need = false;
             if (node >= 0) {
-                A = recA[node];
+                A = recA[kRecStride * node];
                 // lower bound of min_b r_b: the box's nearest point
                 const float nx = fminf(fmaxf(A.x, gx0), gx1), ny = fminf(fmaxf(A.y, gy0), gy1);
                 const float rlo = ref_r_only(A.x, A.y, nx, ny, eps2);
@@ -717,8 +717,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_frontier(Segs segs, int nsupers,
         int4 C = make_int4(kNoChild, kNoChild, kNoChild, kNoChild);
         if (node >= 0) {
             // the children's record with the node's: one L2 round trip per round
-            const float4 A = recA[node];
-            const int4 D = recD[node];
+            const float4 A = recA[kRecStride * node];
+            const int4 D = recD[kRecStride * node];
             const int4 Cn = recC[node];
             const float fx = fmaxf(fabsf(A.x - bx0), fabsf(A.x - bx1));
             const float fy = fmaxf(fabsf(A.y - by0), fabsf(A.y - by1));
@@ -779,12 +779,12 @@ __global__ void __launch_bounds__(WARPS * 32) k_frontier(Segs segs, int nsupers,
         int node = -1;
         if (e < nf) {
             node = stack[e];
-            const float4 A = recA[node];
+            const float4 A = recA[kRecStride * node];
             const float ddx = fmaxf(fmaxf(bx0 - A.x, A.x - bx1), 0.0f);
             const float ddy = fmaxf(fmaxf(by0 - A.y, A.y - by1), 0.0f);
             const float d2 = fmaf(ddx, ddx, ddy * ddy);
             if (d2 > A.w)
-                acc = __int_as_float(recD[node].z) <= aa * kRuleMargin * d2 * d2 * sqrt_approx(d2);
+                acc = __int_as_float(recD[kRecStride * node].z) <= aa * kRuleMargin * d2 * d2 * sqrt_approx(d2);
         }
         const unsigned am = __ballot_sync(kFull, acc), tm = __ballot_sync(kFull, e < nf && !acc);
         if (acc) out[kFrontierCap - 1 - (na + __popc(am & lt))] = node;
@@ -1050,7 +1050,7 @@ __device__ __forceinline__ void eval_batches(unsigned char* wbase, const float4*
             bodies_sum<BPL>(bxy, bm, k, px, py, npx, npy, eps2, ox, oy);
         } else {
             if (lane < k) {
-                const float4 A = recA[v], B = recB[v];
+                const float4 A = recA[kRecStride * v], B = recB[v];
                 reinterpret_cast<float*>(cp.xy + q)[h] = A.x;
                 reinterpret_cast<float*>(cp.xy + q)[2 + h] = A.y;
                 reinterpret_cast<float*>(cp.mh + q)[h] = A.z;
@@ -1408,7 +1408,7 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
             __syncwarp();
             if (lane < k) {
                 const int node = clist[ccnt - k + lane];
-                const float4 A = recA[node], B = recB[node];
+                const float4 A = recA[kRecStride * node], B = recB[node];
                 const int q = lane >> 1, h = lane & 1;
                 reinterpret_cast<float*>(cpair.xy + q)[h] = A.x;
                 reinterpret_cast<float*>(cpair.xy + q)[2 + h] = A.y;
@@ -1554,8 +1554,8 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
             float d2 = 0.0f;
             bool need = false;
             if (node >= 0) {
-                A = recA[node];
-                D = recD[node];
+                A = recA[kRecStride * node];
+                D = recD[kRecStride * node];
                 if (ESTIMATE) A.w = __int_as_float(D.w);  // bootstrap opening radius
                 const float ddx = fmaxf(fmaxf(gx0 - A.x, A.x - gx1), 0.0f);
                 const float ddy = fmaxf(fmaxf(gy0 - A.y, A.y - gy1), 0.0f);
