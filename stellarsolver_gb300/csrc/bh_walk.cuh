@@ -697,61 +697,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_frontier(Segs segs, int nsupers,
         by0 = fminf(by0, __shfl_xor_sync(kFull, by0, o));
         by1 = fmaxf(by1, __shfl_xor_sync(kFull, by1, o));
     }
-    int* out = list + (size_t)S * kFrontierCap;
-    bool bad = hi - lo < 2;  // no tree: the walk has nothing to start from
-    int top = 0, nf = 0, rounds = 0;
-    if (!bad) {
-        if (lane == 0) stack[0] = lo;  // the system's root
-        top = 1;
-    }
-    while (top > 0 && !bad) {
-        const int k = min(32, top);
-        if (++rounds > kMaxWalkRounds || top + 3 * k > kFrontierStack) {
-            bad = true;  // not a valid tree, or too wide a frontier: walks start at the root
-            break;
-        }
-        __syncwarp();
-        const int node = lane < k ? stack[top - 1 - lane] : -1;
-        top -= k;
-        bool open = false;
-        int4 C = make_int4(kNoChild, kNoChild, kNoChild, kNoChild);
-        if (node >= 0) {
-            // the children's record with the node's: one L2 round trip per round
-            const float4 A = recA[kRecStride * node];
-            const int4 D = recD[kRecStride * node];
-            const int4 Cn = recC[node];
-            const float fx = fmaxf(fabsf(A.x - bx0), fabsf(A.x - bx1));
-            const float fy = fmaxf(fabsf(A.y - by0), fabsf(A.y - by1));
-            if (D.y > bucket && fmaf(fx, fx, fy * fy) <= A.w) {
-                C = Cn;
-                open = (C.x >= 0 || C.x == kNoChild) && (C.y >= 0 || C.y == kNoChild) &&
-                       (C.z >= 0 || C.z == kNoChild) && (C.w >= 0 || C.w == kNoChild);
-            }
-        }
-        const int nn = open ? (C.x >= 0) + (C.y >= 0) + (C.z >= 0) + (C.w >= 0) : 0;
-        const unsigned fm = __ballot_sync(kFull, node >= 0 && !open);
-        int ntot;
-        const int noff = warp_excl_scan(nn, &ntot);
-        __syncwarp();  // every lane has read its stack slot before children overwrite it
-        if (open) {
-            int* w = stack + top + noff;
-            if (C.x >= 0) *w++ = C.x;
-            if (C.y >= 0) *w++ = C.y;
-            if (C.z >= 0) *w++ = C.z;
-            if (C.w >= 0) *w++ = C.w;
-        }
-        if (node >= 0 && !open) {
-            const int idx = nf + __popc(fm & lt);
-            if (idx < kFrontierCap) out[idx] = node;
-        }
-        top += ntot;
-        nf += __popc(fm);
-    }
-    if (bad || nf > kFrontierCap) {
-        if (lane == 0) count[S] = make_int2(-1, 0);
-        return;
-    }
-    // the smallest relative-rule scale over the super-group's groups
+    // the smallest relative-rule scale over the super-group's groups (taken
+    // before the traversal, which classifies each frontier node as it stops)
     float aa = __int_as_float(0x7f800000);
     if (alpha > 0.0f) {
         for (int g0 = s0 + lane * gw; g0 < s1; g0 += 32 * gw) {
@@ -768,31 +715,77 @@ __global__ void __launch_bounds__(WARPS * 32) k_frontier(Segs segs, int nsupers,
         for (int o = 16; o > 0; o >>= 1) aa = fminf(aa, __shfl_xor_sync(kFull, aa, o));
         aa *= 0.999f;
     }
-    // split the frontier: nodes to test to the front, accepted cells to the back
-    __syncwarp();
-    for (int e = lane; e < nf; e += 32) stack[e] = out[e];
-    __syncwarp();
-    int nt = 0, na = 0;
-    for (int base = 0; base < nf; base += 32) {
-        const int e = base + lane;
-        bool acc = false;
-        int node = -1;
-        if (e < nf) {
-            node = stack[e];
-            const float4 A = recA[kRecStride * node];
-            const float ddx = fmaxf(fmaxf(bx0 - A.x, A.x - bx1), 0.0f);
-            const float ddy = fmaxf(fmaxf(by0 - A.y, A.y - by1), 0.0f);
-            const float d2 = fmaf(ddx, ddx, ddy * ddy);
-            if (d2 > A.w)
-                acc = __int_as_float(recD[kRecStride * node].z) <= aa * kRuleMargin * d2 * d2 * sqrt_approx(d2);
-        }
-        const unsigned am = __ballot_sync(kFull, acc), tm = __ballot_sync(kFull, e < nf && !acc);
-        if (acc) out[kFrontierCap - 1 - (na + __popc(am & lt))] = node;
-        if (e < nf && !acc) out[nt + __popc(tm & lt)] = node;
-        na += __popc(am);
-        nt += __popc(tm);
+    // The frontier in traversal order, split as it is found: nodes to test from
+    // the front of the list, accepted cells from the back.
+    int* out = list + (size_t)S * kFrontierCap;
+    bool bad = hi - lo < 2;  // no tree: the walk has nothing to start from
+    int top = 0, nt = 0, na = 0, rounds = 0;
+    if (!bad) {
+        if (lane == 0) stack[0] = lo;  // the system's root
+        top = 1;
     }
-    if (lane == 0) count[S] = make_int2(nt, na);
+    while (top > 0 && !bad) {
+        const int k = min(32, top);
+        if (++rounds > kMaxWalkRounds || top + 3 * k > kFrontierStack) {
+            bad = true;  // not a valid tree, or too wide a frontier: walks start at the root
+            break;
+        }
+        __syncwarp();
+        const int node = lane < k ? stack[top - 1 - lane] : -1;
+        top -= k;
+        bool open = false, acc = false;
+        int4 C = make_int4(kNoChild, kNoChild, kNoChild, kNoChild);
+        if (node >= 0) {
+            // the children's record with the node's: one L2 round trip per round
+            const float4 A = recA[kRecStride * node];
+            const int4 D = recD[kRecStride * node];
+            const int4 Cn = recC[node];
+            const float fx = fmaxf(fabsf(A.x - bx0), fabsf(A.x - bx1));
+            const float fy = fmaxf(fabsf(A.y - by0), fabsf(A.y - by1));
+            if (D.y > bucket && fmaf(fx, fx, fy * fy) <= A.w) {
+                C = Cn;
+                open = (C.x >= 0 || C.x == kNoChild) && (C.y >= 0 || C.y == kNoChild) &&
+                       (C.z >= 0 || C.z == kNoChild) && (C.w >= 0 || C.w == kNoChild);
+            }
+            if (!open) {
+                // a frontier node: accepted by every group of the super-group
+                // when its box's nearest point is beyond the opening radius and
+                // the relative rule holds there at the smallest group scale
+                const float ddx = fmaxf(fmaxf(bx0 - A.x, A.x - bx1), 0.0f);
+                const float ddy = fmaxf(fmaxf(by0 - A.y, A.y - by1), 0.0f);
+                const float d2 = fmaf(ddx, ddx, ddy * ddy);
+                if (d2 > A.w)
+                    acc = __int_as_float(D.z) <= aa * kRuleMargin * d2 * d2 * sqrt_approx(d2);
+            }
+        }
+        const int nn = open ? (C.x >= 0) + (C.y >= 0) + (C.z >= 0) + (C.w >= 0) : 0;
+        const unsigned am = __ballot_sync(kFull, node >= 0 && !open && acc);
+        const unsigned tm = __ballot_sync(kFull, node >= 0 && !open && !acc);
+        int ntot;
+        const int noff = warp_excl_scan(nn, &ntot);
+        __syncwarp();  // every lane has read its stack slot before children overwrite it
+        if (open) {
+            int* w = stack + top + noff;
+            if (C.x >= 0) *w++ = C.x;
+            if (C.y >= 0) *w++ = C.y;
+            if (C.z >= 0) *w++ = C.z;
+            if (C.w >= 0) *w++ = C.w;
+        }
+        if (node >= 0 && !open) {
+            // in bounds whatever the count; a list over kFrontierCap is discarded
+            if (acc) {
+                const int idx = na + __popc(am & lt);
+                if (idx < kFrontierCap) out[kFrontierCap - 1 - idx] = node;
+            } else {
+                const int idx = nt + __popc(tm & lt);
+                if (idx < kFrontierCap) out[idx] = node;
+            }
+        }
+        top += ntot;
+        nt += __popc(tm);
+        na += __popc(am);
+    }
+    if (lane == 0) count[S] = (bad || nt + na > kFrontierCap) ? make_int2(-1, 0) : make_int2(nt, na);
 }
 
 // Below this many lanes the exact group distance is taken cooperatively
