@@ -1541,8 +1541,9 @@ __global__ void __launch_bounds__(256, BPL == 1 ? 4 : 3) k_walk_acc(AccShape sha
             // group's bodies is needed only when the box test is inconclusive,
             // i.e. d_box <= ropen < d_box + box diagonal, for some lane.
             float4 A = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            // the children are loaded with the node's records (not after the
-            // decision): an opened node then costs no second round trip
+            // the children's record is loaded after the decision, for the
+            // opened nodes only (loading it with A and D, for every tested node
+            // or only where the box test already opens the node, measured slower)
             int4 C = make_int4(kNoChild, kNoChild, kNoChild, kNoChild);
             float d2 = 0.0f;
             bool need = false;
