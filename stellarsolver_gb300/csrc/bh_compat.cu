@@ -73,6 +73,8 @@ struct Workspace {
     int *qa, *qb;
     int* qcount;  // three level counters of the SortParticles queues
     Records rec;  // REFERENCE walk records of the last build's tree (CalculateForces)
+    int* flist;    // CalculateForces: the reference rule's walk frontiers (k_frontier)
+    int2* fcount;
     unsigned long long* inter;  // CalculateForces: interactions (the walk's counter)
     int* work;                  // CalculateForces: the walk's group counter
     int* status;
@@ -176,7 +178,8 @@ Workspace* workspace(size_t n, size_t m) {
     size_t bytes = 3 * al(8 * N) + 3 * al(4 * N) + al(4) + al(4 * 256 * (size_t)tiles) +
                    al(4 * 256) + al(16) + al(8) + 8 * al(4 * N) + al(16 * N) + 2 * al(16 * N) +
                    3 * al(4 * N) + 2 * al(4 * N) + al(4 * (size_t)nb) + al(4) + 2 * al(4 * M) +
-                   al(12) + 3 * al(16 * N) + al(8) + al(4) + al(4);
+                   al(12) + 3 * al(16 * N) + al(8) + al(4) + al(4) +
+                   al(4 * (size_t)num_supers((int)N) * kFrontierCap) + al(8 * (size_t)num_supers((int)N));
     ++w->gen;
     if (cudaMalloc(&w->base, bytes) != cudaSuccess) {
         w->base = nullptr;
@@ -225,6 +228,8 @@ Workspace* workspace(size_t n, size_t m) {
     w->rec.B = nullptr;
     w->rec.C = (int4*)take(16 * N);
     w->rec.D = reinterpret_cast<int4*>(w->rec.A) + 1;
+    w->flist = (int*)take(4 * (size_t)num_supers((int)N) * kFrontierCap);
+    w->fcount = (int2*)take(8 * (size_t)num_supers((int)N));
     w->inter = (unsigned long long*)take(8);
     w->work = (int*)take(4);
     w->status = (int*)take(4);
@@ -1248,6 +1253,16 @@ void compat_CalculateForces(float* x, float* y, float* vx, float* vy, float* ax,
                 e = launch_pdl(k_records, nb, 256, 0, st, n, segs, 0, g_set.theta, 1.0f,
                                (const int*)w.box_ord, (const uint64_t*)w.keys_alt, w.tree, w.sums,
                                w.rec);
+            // the vote rule's walk frontiers, one warp per 512 consecutive bodies
+            constexpr int kFW = 8;
+            const int nsup = num_supers(n);
+            if (e == cudaSuccess)
+                e = launch_pdl(k_frontier<kFW, true>, (nsup + kFW - 1) / kFW, kFW * 32, 0, st, segs,
+                               nsup, (const float*)w.sx, (const float*)w.sy, (const float*)nullptr,
+                               (const float4*)w.rec.A, (const int4*)w.rec.C, (const int4*)w.rec.D,
+                               1, 32, 0.0f, w.flist, w.fcount, (const int*)nullptr,
+                               (const int*)nullptr, (const int*)nullptr, (const int*)nullptr,
+                               (int*)nullptr, (int*)nullptr, g_set.eps2);
             if (e == cudaSuccess) {
                 const WalkIn in{w.sx, w.sy, nullptr, nullptr, w.sm, nullptr, nullptr,
                                 reinterpret_cast<const int*>(w.vals_alt), nullptr, nullptr};
@@ -1259,7 +1274,8 @@ void compat_CalculateForces(float* x, float* y, float* vx, float* vy, float* ax,
                     std::min(blocks_for(gr.ngroups, kVoteWarps), 16 * device_sms());
                 e = launch_pdl(k_walk_vote, blocks, kVoteWarps * 32, 0, st, segs, gr, in,
                                (const float4*)w.rec.A, (const int4*)w.rec.C, g_set.eps2, 0.0f, 0.0f,
-                               out, w.status, w.inter, w.work);
+                               out, w.status, w.inter, w.work,
+                               Frontier{w.flist, w.fcount, nullptr});
             }
             record_cuda(e, "CalculateForces");
             return;

@@ -175,7 +175,7 @@ cudaError_t launch_walk(const StepArgs& a, cudaStream_t st, int part) {
         int grid = std::min(a.walk_grid_ref, (a.groups.ngroups + kVoteWarps - 1) / kVoteWarps);
         if (grid < 1) grid = 1;
         return launch_pdl(k_walk_vote, grid, kVoteWarps * 32, 0, st, a.segs, a.groups, a.in, a.recA,
-                          a.recC, a.eps2, a.dt, a.ddt, a.out, a.status, a.inter, a.work);
+                          a.recC, a.eps2, a.dt, a.ddt, a.out, a.status, a.inter, a.work, a.frontier);
     }
     if (a.bpl == 2)
         return a.mode == BH_MODE_MIXED ? launch_acc<true, 2>(a, st, part)
@@ -576,14 +576,20 @@ int enqueue_step(bh_system* s, cudaStream_t st, cudaEvent_t* ev = nullptr, int b
     StepArgs a = step_args(s);
     if (with_boot) CK(launch_walk(a, st, 0));
     CK(mark(7));
+    constexpr int kFW = 8;  // warps (super-groups) per block
+    const int fblocks = (s->nsupers + kFW - 1) / kFW;
     if (a.mode != BH_MODE_REFERENCE) {
-        constexpr int kFW = 8;  // warps (super-groups) per block
-        const int blocks = (s->nsupers + kFW - 1) / kFW;
-        CK(launch_pdl(k_frontier<kFW>, blocks, kFW * 32, 0, st, a.segs, s->nsupers, a.in.x, a.in.y,
+        CK(launch_pdl(k_frontier<kFW>, fblocks, kFW * 32, 0, st, a.segs, s->nsupers, a.in.x, a.in.y,
                       a.in.amag, a.recA, a.recC, a.recD, a.bucket, 32 * a.bpl, a.alpha, s->flist,
                       s->fcount, a.frontier.sup_off, a.in.gcost,
                       s->nseg > 1 ? (a.bpl == 2 ? s->gseg_off2 : s->gseg_off) : nullptr,
-                      s->mean_cost, s->heavy, s->work + kWorkHeavy));
+                      s->mean_cost, s->heavy, s->work + kWorkHeavy, a.eps2));
+    } else {
+        // the reference rule's frontiers (leaves hold one body: bucket 1)
+        CK(launch_pdl(k_frontier<kFW, true>, fblocks, kFW * 32, 0, st, a.segs, s->nsupers, a.in.x,
+                      a.in.y, (const float*)nullptr, a.recA, a.recC, a.recD, 1, 32, 0.0f, s->flist,
+                      s->fcount, a.frontier.sup_off, (const int*)nullptr, (const int*)nullptr,
+                      (const int*)nullptr, (int*)nullptr, (int*)nullptr, a.eps2));
     }
     CK(mark(8));
     CK(launch_walk(a, st, 1));

@@ -342,6 +342,49 @@ __host__ __device__ constexpr int acc_warp_bytes(AccShape sh, bool share = false
            ((sh.stack * 4 + 15) & ~15) + ((acc_body_cap(sh.bucket) * 4 + 15) & ~15);
 }
 
+// ------------------------------------------------------------------ shared frontier
+//
+// Consecutive groups open the same nodes near the top of the tree.  For each
+// super-group of 2^kSuperLog2 consecutive bodies of one system (counted from
+// the system's first body, so a system gets the same frontiers alone and in a
+// batch), k_frontier opens once every node that each of its groups would
+// open, and keeps the nodes where that stops: the frontier.  The main accuracy
+// walk of a group starts from its super-group's frontier instead of the root,
+// and tests and decides exactly the nodes it would have tested from the root
+// (orc_frontier_check restates this on the CPU).  k_frontier also lists the
+// super-group's heavy walk groups (Heavy).
+//
+// A node is opened for all groups when it is not a leaf bucket, all its
+// children are nodes, and the farthest corner of the super-group's box lies
+// within its opening radius: far^2 <= ropen^2.  Every distance a group's rule
+// can use (box lower bound, extreme-body bound, exact minimum) is a float
+// expression of the same form over coordinates inside that box, and is
+// monotone in them, so it is <= far^2 and the group does not accept the node.
+// A frontier node is accepted by all groups when the super-group box's
+// nearest point lies beyond its opening radius and the relative rule holds
+// there with the smallest group scale a_g of the super-group (taken 0.1 %
+// low, for the groups' own float sums); those cells go to every group's cell
+// list untested.  list[S] holds the nodes to test from the front and the
+// accepted cells from the back; count[S] = (nodes to test, accepted cells).
+//
+// The REFERENCE walk (k_walk_vote) starts from frontiers of the reference's
+// rule (k_frontier<.., true>): a group opens a cell iff one of its bodies has
+// r_b < dp (kernels.cu:395-406), so the cell is opened for all when r of the
+// super-group box's corner farthest from the centre of mass is below dp (every
+// body's r is at most that: each float step of r is monotone in |dx|, |dy|),
+// and approximated by all when dp <= r of the box's nearest point.
+
+constexpr int kSuperLog2 = 9;         // 512 bodies per super-group
+constexpr int kFrontierCap = 512;     // frontier entries kept per super-group
+constexpr int kFrontierStack = 1024;  // traversal stack per warp of k_frontier
+
+struct Frontier {
+    const int* list = nullptr;     // [super-group][kFrontierCap]
+    const int2* count = nullptr;   // [super-group]: (nodes to test, accepted cells); x = -1: start
+                                   // from the root; null: off
+    const int* sup_off = nullptr;  // [nseg+1] first super-group of each system (null: one system)
+};
+
 // ------------------------------------------------------------------ REFERENCE walk, batched
 //
 // k_walk_vote gives the reference's interaction set with the accuracy walk's
@@ -370,7 +413,8 @@ static __global__ void __launch_bounds__(kVoteWarps * 32) k_walk_vote(Segs segs,
                                                                WalkOut out,
                                                                int* __restrict__ status,
                                                                unsigned long long* __restrict__ inter_total,
-                                                               int* __restrict__ work) {
+                                                               int* __restrict__ work,
+                                                               Frontier fr) {
     pdl_wait();
     __shared__ int s_stack[kVoteWarps][kVoteStack];
     __shared__ float4 s_stage[kVoteWarps][32];  // staged entries: x, y, m
@@ -421,9 +465,20 @@ static __global__ void __launch_bounds__(kVoteWarps * 32) k_walk_vote(Segs segs,
         long long entries = 0;
         bool overflow = false;
         int top = 0, ccnt = 0, bcnt = 0, rounds = 0;
+        const int* fl = nullptr;  // the super-group's frontier (k_frontier<.., true>), if any
+        int nacc = 0;             // its cells that every group approximates
         if (hi - lo >= 2) {
-            if (lane == 0) stack[0] = lo;  // the system's root
-            top = 1;
+            const int S = (fr.sup_off ? __ldg(fr.sup_off + sg) : 0) + ((gstart - lo) >> kSuperLog2);
+            const int2 fc = fr.count ? fr.count[S] : make_int2(-1, 0);
+            if (fc.x >= 0 && 2 * fc.x <= kVoteStack) {
+                fl = fr.list + (size_t)S * kFrontierCap;
+                for (int e = lane; e < fc.x; e += 32) stack[e] = fl[e];
+                top = fc.x;
+                nacc = fc.y;
+            } else {
+                if (lane == 0) stack[0] = lo;  // the system's root
+                top = 1;
+            }
         }
         // k entries of staged (x, y, m), with the reference's arithmetic
         auto interact = [&](int k) {
@@ -458,6 +513,15 @@ static __global__ void __launch_bounds__(kVoteWarps * 32) k_walk_vote(Segs segs,
             interact(k);
             bcnt -= k;
         };
+        // cells every group of the super-group approximates: straight to the cell list
+        for (int base = 0; base < nacc; base += 32) {
+            const int k = min(32, nacc - base);
+            __syncwarp();
+            if (lane < k) clist[ccnt + lane] = fl[kFrontierCap - 1 - (base + lane)];
+            ccnt += k;
+            __syncwarp();
+            while (ccnt >= 32) flush_cells(32);
+        }
         while (top > 0) {
             if (rounds == kMaxWalkRounds) {  // far beyond any valid tree: report, do not loop
                 if (lane == 0) atomicOr(status, ST_TREE);
@@ -573,41 +637,6 @@ static __global__ void __launch_bounds__(kVoteWarps * 32) k_walk_vote(Segs segs,
     if (lane == 0 && my_inter) atomicAdd(inter_total, my_inter);
 }
 
-// ------------------------------------------------------------------ shared frontier
-//
-// Consecutive groups open the same nodes near the top of the tree.  For each
-// super-group of 2^kSuperLog2 consecutive bodies of one system (counted from
-// the system's first body, so a system gets the same frontiers alone and in a
-// batch), k_frontier opens once every node that each of its groups would
-// open, and keeps the nodes where that stops: the frontier.  The main accuracy
-// walk of a group starts from its super-group's frontier instead of the root,
-// and tests and decides exactly the nodes it would have tested from the root
-// (orc_frontier_check restates this on the CPU).  k_frontier also lists the
-// super-group's heavy walk groups (Heavy).
-//
-// A node is opened for all groups when it is not a leaf bucket, all its
-// children are nodes, and the farthest corner of the super-group's box lies
-// within its opening radius: far^2 <= ropen^2.  Every distance a group's rule
-// can use (box lower bound, extreme-body bound, exact minimum) is a float
-// expression of the same form over coordinates inside that box, and is
-// monotone in them, so it is <= far^2 and the group does not accept the node.
-// A frontier node is accepted by all groups when the super-group box's
-// nearest point lies beyond its opening radius and the relative rule holds
-// there with the smallest group scale a_g of the super-group (taken 0.1 %
-// low, for the groups' own float sums); those cells go to every group's cell
-// list untested.  list[S] holds the nodes to test from the front and the
-// accepted cells from the back; count[S] = (nodes to test, accepted cells).
-constexpr int kSuperLog2 = 9;         // 512 bodies per super-group
-constexpr int kFrontierCap = 512;     // frontier entries kept per super-group
-constexpr int kFrontierStack = 1024;  // traversal stack per warp of k_frontier
-
-struct Frontier {
-    const int* list = nullptr;     // [super-group][kFrontierCap]
-    const int2* count = nullptr;   // [super-group]: (nodes to test, accepted cells); x = -1: start
-                                   // from the root; null: off
-    const int* sup_off = nullptr;  // [nseg+1] first super-group of each system (null: one system)
-};
-
 __host__ __device__ __forceinline__ int num_supers(int n) {
     return (n + (1 << kSuperLog2) - 1) >> kSuperLog2;
 }
@@ -615,7 +644,7 @@ __host__ __device__ __forceinline__ int num_supers(int n) {
 // One warp per super-group (positions x, y and |a_old| in key order; walk
 // records of the systems' trees; sup_off: first super-group of each system,
 // null for one; gw: bodies per walk group; alpha: the relative rule's).
-template <int WARPS>
+template <int WARPS, bool VOTE = false>
 __global__ void __launch_bounds__(WARPS * 32) k_frontier(Segs segs, int nsupers,
                                                          const float* __restrict__ x,
                                                          const float* __restrict__ y,
@@ -631,7 +660,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_frontier(Segs segs, int nsupers,
                                                          const int* __restrict__ gseg_off,
                                                          const int* __restrict__ mean_cost,
                                                          int* __restrict__ heavy,
-                                                         int* __restrict__ nheavy) {
+                                                         int* __restrict__ nheavy, float eps2) {
     pdl_wait();
     __shared__ int s_stack[WARPS][kFrontierStack];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -654,7 +683,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_frontier(Segs segs, int nsupers,
     const int lo = segs.off[sg], hi = segs.off[sg + 1];
     const int s0 = lo + ((S - (segs.nseg > 1 ? __ldg(sup_off + sg) : 0)) << kSuperLog2);
     const int s1 = min(hi, s0 + (1 << kSuperLog2));
-    {
+    if (!VOTE) {
         // this super-group's heavy walk groups (at most 32: gw >= 32 bodies).
         // Load k of a lane reads position s0 + 32 k + lane: the 32-body slice
         // k of the super-group, which belongs to group (32 k) / gw.
@@ -700,7 +729,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_frontier(Segs segs, int nsupers,
     // the smallest relative-rule scale over the super-group's groups (taken
     // before the traversal, which classifies each frontier node as it stops)
     float aa = __int_as_float(0x7f800000);
-    if (alpha > 0.0f) {
+    if (!VOTE && alpha > 0.0f) {
         for (int g0 = s0 + lane * gw; g0 < s1; g0 += 32 * gw) {
             const int g1 = min(s1, g0 + gw);
             float amin = __int_as_float(0x7f800000), asum = 0.0f;
@@ -740,14 +769,31 @@ __global__ void __launch_bounds__(WARPS * 32) k_frontier(Segs segs, int nsupers,
             const float4 A = recA[kRecStride * node];
             const int4 D = recD[kRecStride * node];
             const int4 Cn = recC[node];
-            const float fx = fmaxf(fabsf(A.x - bx0), fabsf(A.x - bx1));
-            const float fy = fmaxf(fabsf(A.y - by0), fabsf(A.y - by1));
-            if (D.y > bucket && fmaf(fx, fx, fy * fy) <= A.w) {
+            bool within;
+            if (VOTE) {
+                // the reference's rule (kernels.cu:395-406): a group opens the node
+                // iff one of its bodies has r < dp; r of the box corner farthest
+                // from the centre of mass bounds every body's r from above
+                const float fxp =
+                    fabsf(__fsub_rn(A.x, bx0)) >= fabsf(__fsub_rn(A.x, bx1)) ? bx0 : bx1;
+                const float fyp =
+                    fabsf(__fsub_rn(A.y, by0)) >= fabsf(__fsub_rn(A.y, by1)) ? by0 : by1;
+                within = ref_r_only(A.x, A.y, fxp, fyp, eps2) < A.w;
+            } else {
+                const float fx = fmaxf(fabsf(A.x - bx0), fabsf(A.x - bx1));
+                const float fy = fmaxf(fabsf(A.y - by0), fabsf(A.y - by1));
+                within = fmaf(fx, fx, fy * fy) <= A.w;
+            }
+            if (D.y > bucket && within) {
                 C = Cn;
                 open = (C.x >= 0 || C.x == kNoChild) && (C.y >= 0 || C.y == kNoChild) &&
                        (C.z >= 0 || C.z == kNoChild) && (C.w >= 0 || C.w == kNoChild);
             }
-            if (!open) {
+            if (!open && VOTE) {
+                // every group approximates it: dp <= r of the box's nearest point
+                const float nx = fminf(fmaxf(A.x, bx0), bx1), ny = fminf(fmaxf(A.y, by0), by1);
+                acc = A.w <= ref_r_only(A.x, A.y, nx, ny, eps2);
+            } else if (!open) {
                 // a frontier node: accepted by every group of the super-group
                 // when its box's nearest point is beyond the opening radius and
                 // the relative rule holds there at the smallest group scale
