@@ -401,6 +401,46 @@ struct Frontier {
 constexpr int kVoteWarps = 4;
 constexpr int kVoteStack = 1024;
 
+// k staged entries (positions xy[e], masses m[e]) added to (ax, ay) in entry
+// order with the reference's arithmetic (kernels.cu:403-411): d = c - p,
+// r = (dx dx + dy dy) + eps2 uncontracted, f = ((m ri) ri) ri, a += f d.
+// Two entries at a time in packed FP32x2 operations, each element rounded as
+// the scalar operation is, and one accumulation chain, so the sums are those of
+// the scalar loop bit for bit.  FTZ (eps2 a normal float, so r >= eps2 is never
+// a denormal): rsqrt.approx.ftz, equal to rsqrtf for every normal argument.
+template <bool FTZ>
+__device__ __forceinline__ void vote_interact(const float2* __restrict__ xy,
+                                              const float* __restrict__ m, int k, float px,
+                                              float py, float eps2, float& ax, float& ay) {
+    const float2 np = make_float2(-px, -py);
+    const float2 e2 = make_float2(eps2, eps2);
+    float2 acc = make_float2(ax, ay);
+    int e = 0;
+    for (; e + 1 < k; e += 2) {
+        const float4 c = *reinterpret_cast<const float4*>(xy + e);  // two entries' x, y
+        const float2 mm = *reinterpret_cast<const float2*>(m + e);
+        const float2 d0 = __fadd2_rn(make_float2(c.x, c.y), np);
+        const float2 d1 = __fadd2_rn(make_float2(c.z, c.w), np);
+        const float2 q0 = __fmul2_rn(d0, d0), q1 = __fmul2_rn(d1, d1);
+        const float2 r = __fadd2_rn(make_float2(__fadd_rn(q0.x, q0.y), __fadd_rn(q1.x, q1.y)), e2);
+        const float2 ri = FTZ ? make_float2(rsqrt_ftz(r.x), rsqrt_ftz(r.y))
+                              : make_float2(rsqrtf(r.x), rsqrtf(r.y));
+        const float2 f = __fmul2_rn(__fmul2_rn(__fmul2_rn(mm, ri), ri), ri);
+        acc = __ffma2_rn(make_float2(f.x, f.x), d0, acc);
+        acc = __ffma2_rn(make_float2(f.y, f.y), d1, acc);
+    }
+    if (e < k) {
+        const float2 c = xy[e];
+        float dx, dy;
+        const float r = ref_r(c.x, c.y, px, py, eps2, &dx, &dy);
+        const float ri = FTZ ? rsqrt_ftz(r) : rsqrtf(r);
+        const float f = m[e] * ri * ri * ri;
+        acc = __ffma2_rn(make_float2(f, f), make_float2(dx, dy), acc);
+    }
+    ax = acc.x;
+    ay = acc.y;
+}
+
 __device__ __forceinline__ float ref_r_only(float cx, float cy, float px, float py, float eps2) {
     float dx, dy;
     return ref_r(cx, cy, px, py, eps2, &dx, &dy);
@@ -417,14 +457,17 @@ static __global__ void __launch_bounds__(kVoteWarps * 32) k_walk_vote(Segs segs,
                                                                Frontier fr) {
     pdl_wait();
     __shared__ int s_stack[kVoteWarps][kVoteStack];
-    __shared__ float4 s_stage[kVoteWarps][32];  // staged entries: x, y, m
+    __shared__ __align__(16) float2 s_sxy[kVoteWarps][32];  // staged entries: x, y
+    __shared__ __align__(8) float s_sm[kVoteWarps][32];     // and m
     __shared__ float2 s_gp[kVoteWarps][32];     // the group's positions
     __shared__ int s_clist[kVoteWarps][64];
     __shared__ int s_blist[kVoteWarps][32 + 128];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned lt = lanemask_lt();
     int* stack = s_stack[warp];
-    float4* stage = s_stage[warp];
+    float2* sxy = s_sxy[warp];
+    float* smass = s_sm[warp];
+    const bool ftz = eps2 >= 0x1p-126f;  // a normal float
     float2* gp = s_gp[warp];
     int* clist = s_clist[warp];
     int* blist = s_blist[warp];
@@ -482,22 +525,18 @@ static __global__ void __launch_bounds__(kVoteWarps * 32) k_walk_vote(Segs segs,
         }
         // k entries of staged (x, y, m), with the reference's arithmetic
         auto interact = [&](int k) {
-            for (int e = 0; e < k; ++e) {
-                const float4 c = stage[e];
-                float dx, dy;
-                const float r = ref_r(c.x, c.y, px, py, eps2, &dx, &dy);
-                const float ri = rsqrtf(r);  // kernels.cu:407-411
-                const float f = c.z * ri * ri * ri;
-                ax = fmaf(f, dx, ax);
-                ay = fmaf(f, dy, ay);
-            }
+            if (ftz)
+                vote_interact<true>(sxy, smass, k, px, py, eps2, ax, ay);
+            else
+                vote_interact<false>(sxy, smass, k, px, py, eps2, ax, ay);
             entries += k;
         };
         auto flush_cells = [&](int k) {  // the last k entries of clist
             __syncwarp();
             if (lane < k) {
                 const float4 A = recA[kRecStride * (clist[ccnt - k + lane])];
-                stage[lane] = make_float4(A.x, A.y, A.z, 0.0f);
+                sxy[lane] = make_float2(A.x, A.y);
+                smass[lane] = A.z;
             }
             __syncwarp();
             interact(k);
@@ -507,7 +546,8 @@ static __global__ void __launch_bounds__(kVoteWarps * 32) k_walk_vote(Segs segs,
             __syncwarp();
             if (lane < k) {
                 const int b = blist[bcnt - k + lane];
-                stage[lane] = make_float4(in.x[b], in.y[b], in.m[b], 0.0f);
+                sxy[lane] = make_float2(in.x[b], in.y[b]);
+                smass[lane] = in.m[b];
             }
             __syncwarp();
             interact(k);
