@@ -703,8 +703,8 @@ static __global__ void k_build(const uint64_t* __restrict__ k, int n, Segs segs,
     int j = i + l * d;
     int dnode = kdelta(k, i, j, lo, hi);
     int sp = 0;
-    for (int div = 2;; div <<= 1) {
-        int step = (l + div - 1) / div;
+    for (int sh = 1;; ++sh) {
+        const int step = ((l - 1) >> sh) + 1;  // ceil(l / 2^sh) for l >= 1, no division
         if (kdelta(k, i, i + (sp + step) * d, lo, hi) > dnode) sp += step;
         if (step <= 1) break;
     }
