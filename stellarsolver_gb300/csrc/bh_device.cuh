@@ -655,6 +655,14 @@ __device__ __forceinline__ int kdelta(const uint64_t* __restrict__ k, int i, int
     return a != b ? __clzll(a ^ b) : 64 + __clz(i ^ j);
 }
 
+// kdelta with key i already in a register (ki = k[i]).
+__device__ __forceinline__ int kdelta_i(const uint64_t* __restrict__ k, uint64_t ki, int i, int j,
+                                        int lo, int hi) {
+    if (j < lo || j > hi) return -1;
+    const uint64_t b = k[j];
+    return ki != b ? __clzll(ki ^ b) : 64 + __clz(i ^ j);
+}
+
 struct TreePtrs {
     int *left, *right, *parent, *leaf_parent, *split, *first, *last;
     int4* climb;  // per internal node: left, right, parent, w = (split << 1) | inside one
@@ -692,20 +700,21 @@ static __global__ void k_build(const uint64_t* __restrict__ k, int n, Segs segs,
         t.parent[i] = -1;
         t.climb[i].z = -1;
     }
-    int dl = kdelta(k, i, i - 1, lo, hi), dr = kdelta(k, i, i + 1, lo, hi);
+    const uint64_t ki = k[i];
+    int dl = kdelta_i(k, ki, i, i - 1, lo, hi), dr = kdelta_i(k, ki, i, i + 1, lo, hi);
     int d = dr > dl ? 1 : -1;
     int dmin = min(dl, dr);
     int lmax = 2;
-    while (kdelta(k, i, i + lmax * d, lo, hi) > dmin) lmax <<= 1;
+    while (kdelta_i(k, ki, i, i + lmax * d, lo, hi) > dmin) lmax <<= 1;
     int l = 0;
     for (int step = lmax >> 1; step >= 1; step >>= 1)
-        if (kdelta(k, i, i + (l + step) * d, lo, hi) > dmin) l += step;
+        if (kdelta_i(k, ki, i, i + (l + step) * d, lo, hi) > dmin) l += step;
     int j = i + l * d;
-    int dnode = kdelta(k, i, j, lo, hi);
+    int dnode = kdelta_i(k, ki, i, j, lo, hi);
     int sp = 0;
     for (int sh = 1;; ++sh) {
         const int step = ((l - 1) >> sh) + 1;  // ceil(l / 2^sh) for l >= 1, no division
-        if (kdelta(k, i, i + (sp + step) * d, lo, hi) > dnode) sp += step;
+        if (kdelta_i(k, ki, i, i + (sp + step) * d, lo, hi) > dnode) sp += step;
         if (step <= 1) break;
     }
     int g = i + sp * d + min(d, 0);
@@ -733,8 +742,7 @@ static __global__ void k_build(const uint64_t* __restrict__ k, int n, Segs segs,
     t.first[i] = a;
     t.last[i] = b;
     // .z (parent) is written by the parent's thread
-    t.climb[i].x = lc;
-    t.climb[i].y = rc;
+    *reinterpret_cast<int2*>(&t.climb[i].x) = make_int2(lc, rc);
     t.climb[i].w = (dnode << 1) | ((a >> kMomentsLog2) == (b >> kMomentsLog2) ? 1 : 0);
 }
 
